@@ -1,0 +1,190 @@
+/*
+ * gbcc.h -- C ABI of the GB300 closed-shell CCSD(T) library (libgbcc.so).
+ *
+ * Plain pointers and sizes only.  Every tensor crossing this boundary is a
+ * float64 buffer in the reference's dense layout: first index fastest
+ * (column-major), index order as in the reference's CTF index strings, e.g.
+ * T2[a,b,i,j] at a + Nv*(b + Nv*(i + No*j)).  The vertex is Gamma[G,p,q] with
+ * the No holes first, then the Nv particles (Np = No + Nv).
+ *
+ * No function throws.  Each returns a gbcc_status; gbcc_last_error() gives the
+ * message of the last failure on that context.
+ */
+#ifndef GBCC_H
+#define GBCC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBCC_ABI_VERSION 1
+
+typedef enum {
+  GBCC_OK = 0,
+  GBCC_NOT_CONVERGED = 1,    /* maxIterations reached; results are valid */
+  GBCC_DIIS_SINGULAR = 2,    /* DIIS subspace matrix singular (dsysv info != 0) */
+  GBCC_DIVERGED = 3,         /* NaN/Inf in the energy or amplitude norms */
+  GBCC_OOM = 4,              /* device allocation failed / over HBM budget */
+  GBCC_BAD_ARG = 5,
+  GBCC_CUDA_ERROR = 6,
+  GBCC_TIMEOUT = 7,          /* a bounded device wait gave up */
+  GBCC_COMPLEX_UNSUPPORTED = 8, /* vertex has a non-zero imaginary part */
+  GBCC_NO_DEVICE = 9
+} gbcc_status;
+
+/* arithmetic of the dense contractions */
+typedef enum {
+  GBCC_PREC_FP64 = 0,   /* every contraction in IEEE float64 */
+  GBCC_PREC_EMU = 1     /* float64 emulated on the bf16 tensor cores (split
+                           operands, exact fp32 partial sums, fp64 combine);
+                           update, DIIS and energies stay float64 */
+} gbcc_precision;
+
+typedef struct gbcc_ctx gbcc_ctx;
+typedef struct gbcc_solver gbcc_solver;
+
+/* ---------------------------------------------------------------- context */
+/* One context per host thread / stream.  `stream` is a cudaStream_t (NULL:
+ * the context creates its own non-blocking stream). */
+gbcc_status gbcc_ctx_create(int device, void *stream, gbcc_ctx **out);
+void gbcc_ctx_destroy(gbcc_ctx *ctx);
+const char *gbcc_last_error(const gbcc_ctx *ctx);
+const char *gbcc_status_string(int status);
+int gbcc_abi_version(void);
+/* Number of kernels this context has launched so far (all entry points). */
+uint64_t gbcc_ctx_kernel_launches(const gbcc_ctx *ctx);
+/* Analytic FP64-equivalent flops issued to the contraction engine so far. */
+double gbcc_ctx_flops(const gbcc_ctx *ctx);
+void *gbcc_ctx_stream(const gbcc_ctx *ctx);
+
+/* ------------------------------------------------------------- CCSD input */
+/* Replaces ClusterSinglesDoublesAlgorithm::run<double> +
+ * CcsdEnergyFromCoulombIntegrals::getResiduum (real path)
+ * (src/algorithms/ClusterSinglesDoublesAlgorithm.cxx:38-128,
+ *  src/algorithms/CcsdEnergyFromCoulombIntegrals.cxx:27-494).
+ * Argument names and defaults are those of the reference's YAML keys
+ * (ClusterSinglesDoublesAlgorithm.hpp:42-46, .cxx:48-63; LinearMixer.cxx:17;
+ *  DiisMixer.cxx:55; CcsdEnergyFromCoulombIntegrals.cxx:123-124,324,375-384). */
+typedef struct {
+  int mixer;                     /* 0 = "LinearMixer" (default), 1 = "DiisMixer" */
+  int max_residua;               /* maxResidua, default 4 */
+  double mixing_ratio;           /* mixingRatio, default 1.0 */
+  int max_iterations;            /* maxIterations, default 16 */
+  double energy_convergence;     /* energyConvergence (relative), default 1e-6 */
+  double amplitudes_convergence; /* amplitudesConvergence, default 1e-5 */
+  double level_shift;            /* levelShift, default 0 */
+  int distinguishable;           /* distinguishable, default 0 */
+  int ppl;                       /* ppl, default 1 */
+  int integrals_slice_size;      /* integralsSliceSize, default -1 (auto) */
+  double integrals_slice_factor; /* integralsSliceFactor, < 0: not given */
+  int precision;                 /* gbcc_precision, default GBCC_PREC_FP64 */
+  int emu_slices;                /* bf16 slices per operand for GBCC_PREC_EMU
+                                    (0 = library default) */
+} gbcc_ccsd_opts;
+
+void gbcc_ccsd_opts_default(gbcc_ccsd_opts *opts);
+
+typedef struct {
+  int No, Nv, NG;
+  const double *eps_h;        /* HoleEigenEnergies [No] */
+  const double *eps_p;        /* ParticleEigenEnergies [Nv] */
+  const double *gamma;        /* CoulombVertex real part [NG,Np,Np] */
+  const double *gamma_imag;   /* optional imaginary part; must be all zero */
+  /* optional integrals; any NULL one is built on the device from gamma
+   * exactly as CoulombIntegralsFromVertex does */
+  const double *Vabij;        /* PPHHCoulombIntegrals [Nv,Nv,No,No] */
+  const double *Vaibj;        /* PHPHCoulombIntegrals [Nv,No,Nv,No] */
+  const double *Vijkl;        /* HHHHCoulombIntegrals [No,No,No,No] */
+  const double *Vijka;        /* HHHPCoulombIntegrals [No,No,No,Nv] */
+  const double *init_T1;      /* initialSinglesAmplitudes [Nv,No] or NULL */
+  const double *init_T2;      /* initialDoublesAmplitudes [Nv,Nv,No,No] or NULL */
+} gbcc_ccsd_in;
+
+typedef struct {
+  double energy;              /* CcsdEnergy */
+  double direct, exchange;    /* last iteration's energy terms */
+  int iterations;
+  int converged;
+  double *T1;                 /* optional caller buffer [Nv,No]  (CcsdSinglesAmplitudes) */
+  double *T2;                 /* optional caller buffer [Nv,Nv,No,No] (CcsdDoublesAmplitudes) */
+  double *pair_energy;        /* optional caller buffer [No,No] (PairEnergy) */
+  double *energy_history;     /* optional [max_iterations]: energy of each iteration */
+} gbcc_ccsd_out;
+
+/* One-call solve from host buffers (uploads, builds integrals, iterates,
+ * downloads).  Returns GBCC_NOT_CONVERGED when maxIterations was reached
+ * (results still valid, as the reference only warns). */
+gbcc_status gbcc_ccsd_solve(gbcc_ctx *ctx, const gbcc_ccsd_in *in,
+                            const gbcc_ccsd_opts *opts, gbcc_ccsd_out *out);
+
+/* Device-resident solver: setup uploads inputs and builds integrals once;
+ * step runs n more iterations (stopping early on convergence);
+ * amplitudes can then be read back or handed to the (T) step. */
+gbcc_status gbcc_ccsd_setup(gbcc_ctx *ctx, const gbcc_ccsd_in *in,
+                            const gbcc_ccsd_opts *opts, gbcc_solver **out);
+gbcc_status gbcc_ccsd_step(gbcc_solver *s, int n, double *energy,
+                           int *converged);
+gbcc_status gbcc_ccsd_result(gbcc_solver *s, gbcc_ccsd_out *out);
+/* Device pointers of the current amplitudes (T1 then T2). */
+gbcc_status gbcc_ccsd_device_amplitudes(gbcc_solver *s, const double **T1,
+                                        const double **T2);
+void gbcc_ccsd_destroy(gbcc_solver *s);
+
+/* One residual evaluation R(T) for iteration index `it` (it == 0 without
+ * initial doubles gives the MP2 start R2 = Vabij), for parity tests.
+ * Host buffers in and out. */
+gbcc_status gbcc_ccsd_residual(gbcc_ctx *ctx, const gbcc_ccsd_in *in,
+                               const gbcc_ccsd_opts *opts, int it,
+                               const double *T1, const double *T2,
+                               double *R1, double *R2);
+
+/* ---------------------------------------------------------------- (T) */
+/* Replaces CcsdPerturbativeTriples::run (src/algorithms/CcsdPerturbativeTriples.cxx:119-248).
+ * e_total = e_ccsd + E_(T) (the reference's CcsdPerturbativeTriplesEnergy),
+ * e_t = E_(T) alone. Vabij / Vijka may be NULL (built from gamma). */
+typedef struct {
+  int No, Nv, NG;
+  const double *eps_h, *eps_p, *gamma, *gamma_imag;
+  const double *Vabij;   /* PPHHCoulombIntegrals */
+  const double *Vijka;   /* HHHPCoulombIntegrals */
+  const double *T1;      /* CcsdSinglesAmplitudes */
+  const double *T2;      /* CcsdDoublesAmplitudes */
+  double e_ccsd;         /* CcsdEnergy */
+} gbcc_triples_in;
+
+gbcc_status gbcc_triples(gbcc_ctx *ctx, const gbcc_triples_in *in,
+                         int precision, double *e_total, double *e_t);
+/* (T) from a device-resident CCSD solver (no amplitude round trip). */
+gbcc_status gbcc_triples_from_solver(gbcc_solver *s, int precision,
+                                     double *e_total, double *e_t);
+
+/* ------------------------------------------------------ Coulomb integrals */
+/* Replaces CoulombIntegralsFromVertex::calculateRealIntegrals for the blocks
+ * the CCSD/(T) steps read (src/algorithms/CoulombIntegralsFromVertex.cxx:395-491).
+ * Any NULL output is skipped.  Host buffers. */
+gbcc_status gbcc_coulomb_integrals(gbcc_ctx *ctx, int No, int Nv, int NG,
+                                   const double *gamma, double *Vabij,
+                                   double *Vaibj, double *Vijkl, double *Vijka,
+                                   double *Vijab);
+
+/* ------------------------------------------------------- building blocks */
+/* C[M,N] = alpha * op(A) op(B) + beta * C, column-major, device pointers,
+ * stream-ordered on the context stream.  trans: 0 = N, 1 = T. */
+gbcc_status gbcc_dgemm(gbcc_ctx *ctx, int transA, int transB, int64_t M,
+                       int64_t N, int64_t K, double alpha, const double *A,
+                       int64_t lda, const double *B, int64_t ldb, double beta,
+                       double *C, int64_t ldc, int precision);
+
+/* CCSD energy terms (direct, exchange) of device amplitudes, as
+ * ClusterSinglesDoublesAlgorithm::getEnergy (.cxx:131-197). Device pointers. */
+gbcc_status gbcc_energy(gbcc_ctx *ctx, int No, int Nv, const double *T1,
+                        const double *T2, const double *Vabij, double *direct,
+                        double *exchange);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBCC_H */

@@ -1,0 +1,203 @@
+"""Python front end of the GPU CCSD(T) path (calls libgbcc through its C ABI).
+
+Tensors are numpy arrays in the reference's index order (``T2[a, b, i, j]``,
+``gamma[G, p, q]``); they are converted to the column-major buffers of the
+ABI here.  Keyword names follow the oracle / reference YAML keys.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import capi
+from .capi import fortran_flat, from_fortran_flat, ptr
+
+__all__ = ["make_opts", "CcsdInput", "ccsd_solve", "ccsd_residual", "Solver",
+           "triples", "coulomb_integrals", "energy"]
+
+
+def make_opts(mixer="LinearMixer", max_residua=4, mixing_ratio=1.0,
+              max_iterations=16, energy_convergence=1e-6,
+              amplitudes_convergence=1e-5, level_shift=0.0, distinguishable=0,
+              ppl=1, slice_size=-1, slice_factor=None, precision="fp64",
+              emu_slices=0):
+    o = capi.CcsdOpts()
+    capi.load().gbcc_ccsd_opts_default(C.byref(o))
+    o.mixer = {"LinearMixer": 0, "DiisMixer": 1}[mixer]
+    o.max_residua = int(max_residua)
+    o.mixing_ratio = float(mixing_ratio)
+    o.max_iterations = int(max_iterations)
+    o.energy_convergence = float(energy_convergence)
+    o.amplitudes_convergence = float(amplitudes_convergence)
+    o.level_shift = float(level_shift)
+    o.distinguishable = int(distinguishable)
+    o.ppl = int(ppl)
+    o.integrals_slice_size = int(slice_size)
+    o.integrals_slice_factor = -1.0 if slice_factor is None else float(slice_factor)
+    o.precision = {"fp64": capi.PREC_FP64, "emu": capi.PREC_EMU}[precision]
+    o.emu_slices = int(emu_slices)
+    return o
+
+
+class CcsdInput:
+    """Owns the column-major host buffers behind a ``gbcc_ccsd_in``."""
+
+    def __init__(self, eps_h, eps_p, gamma, ints=None, initial=None):
+        eps_h = np.ascontiguousarray(eps_h, dtype=np.float64)
+        eps_p = np.ascontiguousarray(eps_p, dtype=np.float64)
+        self.No, self.Nv, self.NG = eps_h.size, eps_p.size, gamma.shape[0]
+        self._keep = [eps_h, eps_p]
+        s = capi.CcsdIn()
+        s.No, s.Nv, s.NG = self.No, self.Nv, self.NG
+        s.eps_h, s.eps_p = ptr(eps_h), ptr(eps_p)
+        g = fortran_flat(gamma)
+        self._keep.append(g)
+        s.gamma = ptr(g)
+        ints = ints or {}
+        for key, field in (("PPHH", "Vabij"), ("PHPH", "Vaibj"),
+                           ("HHHH", "Vijkl"), ("HHHP", "Vijka")):
+            if key in ints and ints[key] is not None:
+                f = fortran_flat(ints[key])
+                self._keep.append(f)
+                setattr(s, field, ptr(f))
+        if initial is not None:
+            t1, t2 = fortran_flat(initial[0]), fortran_flat(initial[1])
+            self._keep += [t1, t2]
+            s.init_T1, s.init_T2 = ptr(t1), ptr(t2)
+        self.s = s
+
+
+def ccsd_solve(ctx, eps_h, eps_p, gamma, ints=None, initial=None,
+               want_amplitudes=True, pair_energy=False, **opts):
+    inp = CcsdInput(eps_h, eps_p, gamma, ints, initial)
+    o = make_opts(**opts)
+    No, Nv = inp.No, inp.Nv
+    out = capi.CcsdOut()
+    t1 = np.zeros(Nv * No) if want_amplitudes else None
+    t2 = np.zeros(Nv * Nv * No * No) if want_amplitudes else None
+    pe = np.zeros(No * No) if pair_energy else None
+    hist = np.zeros(max(o.max_iterations, 1))
+    out.T1, out.T2, out.pair_energy, out.energy_history = ptr(t1), ptr(t2), ptr(pe), ptr(hist)
+    st = ctx.check(ctx.lib.gbcc_ccsd_solve(ctx.h, C.byref(inp.s), C.byref(o),
+                                           C.byref(out)),
+                   allow=(capi.OK, capi.NOT_CONVERGED))
+    r = {"energy": out.energy, "direct": out.direct, "exchange": out.exchange,
+         "iterations": out.iterations, "converged": bool(out.converged),
+         "status": st, "history": hist[:out.iterations].copy()}
+    if want_amplitudes:
+        r["T1"] = from_fortran_flat(t1, (Nv, No))
+        r["T2"] = from_fortran_flat(t2, (Nv, Nv, No, No))
+    if pair_energy:
+        r["pair_energy"] = from_fortran_flat(pe, (No, No))
+    return r
+
+
+def ccsd_residual(ctx, it, T1, T2, eps_h, eps_p, gamma, ints=None,
+                  initial=None, **opts):
+    inp = CcsdInput(eps_h, eps_p, gamma, ints, initial)
+    o = make_opts(**opts)
+    No, Nv = inp.No, inp.Nv
+    t1, t2 = fortran_flat(T1), fortran_flat(T2)
+    r1 = np.zeros(Nv * No)
+    r2 = np.zeros(Nv * Nv * No * No)
+    ctx.check(ctx.lib.gbcc_ccsd_residual(ctx.h, C.byref(inp.s), C.byref(o),
+                                         int(it), ptr(t1), ptr(t2), ptr(r1),
+                                         ptr(r2)))
+    return (from_fortran_flat(r1, (Nv, No)),
+            from_fortran_flat(r2, (Nv, Nv, No, No)))
+
+
+class Solver:
+    """Device-resident solver: inputs uploaded once, iterations on demand."""
+
+    def __init__(self, ctx, eps_h, eps_p, gamma, ints=None, initial=None,
+                 **opts):
+        self.ctx = ctx
+        self.inp = CcsdInput(eps_h, eps_p, gamma, ints, initial)
+        self.opts = make_opts(**opts)
+        h = C.c_void_p()
+        ctx.check(ctx.lib.gbcc_ccsd_setup(ctx.h, C.byref(self.inp.s),
+                                          C.byref(self.opts), C.byref(h)))
+        self.h = h
+
+    def step(self, n=1):
+        e = C.c_double()
+        conv = C.c_int()
+        self.ctx.check(self.ctx.lib.gbcc_ccsd_step(self.h, int(n), C.byref(e),
+                                                   C.byref(conv)))
+        return e.value, bool(conv.value)
+
+    def result(self, amplitudes=True):
+        No, Nv = self.inp.No, self.inp.Nv
+        out = capi.CcsdOut()
+        t1 = np.zeros(Nv * No) if amplitudes else None
+        t2 = np.zeros(Nv * Nv * No * No) if amplitudes else None
+        out.T1, out.T2 = ptr(t1), ptr(t2)
+        self.ctx.check(self.ctx.lib.gbcc_ccsd_result(self.h, C.byref(out)))
+        r = {"energy": out.energy, "iterations": out.iterations,
+             "converged": bool(out.converged)}
+        if amplitudes:
+            r["T1"] = from_fortran_flat(t1, (Nv, No))
+            r["T2"] = from_fortran_flat(t2, (Nv, Nv, No, No))
+        return r
+
+    def triples(self, precision="fp64"):
+        et, etot = C.c_double(), C.c_double()
+        p = {"fp64": capi.PREC_FP64, "emu": capi.PREC_EMU}[precision]
+        self.ctx.check(self.ctx.lib.gbcc_triples_from_solver(
+            self.h, p, C.byref(etot), C.byref(et)))
+        return et.value, etot.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.gbcc_ccsd_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def triples(ctx, eps_h, eps_p, gamma, T1, T2, e_ccsd=0.0, Vabij=None,
+            Vijka=None, precision="fp64"):
+    """Returns (E_(T), E_CCSD + E_(T))."""
+    eps_h = np.ascontiguousarray(eps_h, dtype=np.float64)
+    eps_p = np.ascontiguousarray(eps_p, dtype=np.float64)
+    s = capi.TriplesIn()
+    s.No, s.Nv, s.NG = eps_h.size, eps_p.size, gamma.shape[0]
+    keep = [eps_h, eps_p]
+    s.eps_h, s.eps_p = ptr(eps_h), ptr(eps_p)
+    for name, arr in (("gamma", gamma), ("T1", T1), ("T2", T2),
+                      ("Vabij", Vabij), ("Vijka", Vijka)):
+        if arr is not None:
+            f = fortran_flat(arr)
+            keep.append(f)
+            setattr(s, name, ptr(f))
+    s.e_ccsd = float(e_ccsd)
+    et, etot = C.c_double(), C.c_double()
+    p = {"fp64": capi.PREC_FP64, "emu": capi.PREC_EMU}[precision]
+    ctx.check(ctx.lib.gbcc_triples(ctx.h, C.byref(s), p, C.byref(etot),
+                                   C.byref(et)))
+    del keep
+    return et.value, etot.value
+
+
+def coulomb_integrals(ctx, gamma, No):
+    NG, Np = gamma.shape[0], gamma.shape[1]
+    Nv = Np - No
+    g = fortran_flat(gamma)
+    vabij = np.zeros(Nv * Nv * No * No)
+    vaibj = np.zeros(Nv * Nv * No * No)
+    vijkl = np.zeros(No ** 4)
+    vijka = np.zeros(No ** 3 * Nv)
+    vijab = np.zeros(Nv * Nv * No * No)
+    ctx.check(ctx.lib.gbcc_coulomb_integrals(ctx.h, No, Nv, NG, ptr(g),
+                                             ptr(vabij), ptr(vaibj),
+                                             ptr(vijkl), ptr(vijka),
+                                             ptr(vijab)))
+    return {"PPHH": from_fortran_flat(vabij, (Nv, Nv, No, No)),
+            "PHPH": from_fortran_flat(vaibj, (Nv, No, Nv, No)),
+            "HHHH": from_fortran_flat(vijkl, (No, No, No, No)),
+            "HHHP": from_fortran_flat(vijka, (No, No, No, Nv)),
+            "HHPP": from_fortran_flat(vijab, (No, No, Nv, Nv))}

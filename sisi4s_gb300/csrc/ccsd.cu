@@ -1,0 +1,449 @@
+// Closed-shell real CCSD on the GPU: inputs, residual, mixers, driver.
+//
+// The residual mirrors CcsdEnergyFromCoulombIntegrals::getResiduum (real
+// path, src/algorithms/CcsdEnergyFromCoulombIntegrals.cxx:27-494) statement by
+// statement; each `C(...)` below is one contraction-engine call (permutes +
+// one GEMM) and is annotated with the reference line it replaces.  The order
+// of the statements is kept, so that the terms added after the P(ia,jb)
+// symmetrisation (:292) are not symmetrised.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "ccsd.hpp"
+
+namespace gbcc {
+
+namespace {
+Ten T1v(const FockLayout &L, double *p) { return ten(p, {L.Nv, L.No}); }
+Ten T2v(const FockLayout &L, double *p) {
+  return ten(p + L.off2, {L.Nv, L.Nv, L.No, L.No});
+}
+constexpr int SC_UPD = 0;      // [0..17]  jacobi sums
+constexpr int SC_EN = 20;      // [20..23] energy sums
+constexpr int SC_TT = 24;      // amp.amp from DIIS combine
+constexpr int SC_LAMBDA = 25;  // DIIS lambda
+constexpr int SC_LIN = 26;     // [26..27] linear mix sums
+constexpr int SC_STATUS = 30;  // DIIS status (as double)
+constexpr int SC_N = 32;
+}  // namespace
+
+std::unique_ptr<CcsdInputs> upload_inputs(Context &ctx, const gbcc_ccsd_in &in,
+                                          int precision, bool need_vaibj) {
+  require(in.No > 0 && in.Nv > 0 && in.NG > 0, "No, Nv, NG must be positive");
+  require(in.eps_h && in.eps_p, "eigenenergies are required");
+  auto p = std::make_unique<CcsdInputs>();
+  const int64_t No = in.No, Nv = in.Nv, NG = in.NG, Np = No + Nv;
+  p->No = No; p->Nv = Nv; p->NG = NG;
+  p->eps_h = OTen(ctx, {No});
+  p->eps_p = OTen(ctx, {Nv});
+  GBCC_CUDA(cudaMemcpyAsync(p->eps_h.p(), in.eps_h, 8 * No,
+                            cudaMemcpyHostToDevice, ctx.stream));
+  GBCC_CUDA(cudaMemcpyAsync(p->eps_p.p(), in.eps_p, 8 * Nv,
+                            cudaMemcpyHostToDevice, ctx.stream));
+  require(in.gamma != nullptr, "CoulombVertex is required");
+  {
+    OTen G(ctx, {NG, Np, Np});
+    if (in.gamma_imag) {
+      GBCC_CUDA(cudaMemcpyAsync(G.p(), in.gamma_imag, 8 * G.t.size(),
+                                cudaMemcpyHostToDevice, ctx.stream));
+      DBuf flag(ctx, sizeof(int));
+      any_nonzero(ctx, G.p(), G.t.size(), flag.as<int>());
+      int h = 0;
+      GBCC_CUDA(cudaMemcpyAsync(&h, flag.as<int>(), sizeof(int),
+                                cudaMemcpyDeviceToHost, ctx.stream));
+      GBCC_CUDA(cudaStreamSynchronize(ctx.stream));
+      if (h)
+        throw Error(GBCC_COMPLEX_UNSUPPORTED,
+                    "CoulombVertex has a non-zero imaginary part; only the real "
+                    "closed-shell path is implemented");
+    }
+    GBCC_CUDA(cudaMemcpyAsync(G.p(), in.gamma, 8 * G.t.size(),
+                              cudaMemcpyHostToDevice, ctx.stream));
+    // slices of CcsdEnergyFromCoulombIntegrals.cxx:70-78
+    p->Gai = OTen(ctx, {NG, Nv, No});
+    p->Gab = OTen(ctx, {NG, Nv, Nv});
+    p->Gij = OTen(ctx, {NG, No, No});
+    vertex_block(ctx, p->Gai.p(), G.p(), NG, Np, No, Nv, 0, No);
+    vertex_block(ctx, p->Gab.p(), G.p(), NG, Np, No, Nv, No, Nv);
+    vertex_block(ctx, p->Gij.p(), G.p(), NG, Np, 0, No, 0, No);
+  }
+  auto up = [&](OTen &dst, const double *src, std::initializer_list<int64_t> l) {
+    dst = OTen(ctx, l);
+    GBCC_CUDA(cudaMemcpyAsync(dst.p(), src, 8 * dst.t.size(),
+                              cudaMemcpyHostToDevice, ctx.stream));
+  };
+  // CoulombIntegralsFromVertex.cxx:395-417 for missing blocks
+  if (in.Vabij) up(p->Vabij, in.Vabij, {Nv, Nv, No, No});
+  else {
+    p->Vabij = OTen(ctx, {Nv, Nv, No, No});
+    contract(ctx, 1.0, p->Gai, "Gai", p->Gai, "Gbj", 0.0, p->Vabij, "abij", precision);
+  }
+  if (need_vaibj) {
+    if (in.Vaibj) up(p->Vaibj, in.Vaibj, {Nv, No, Nv, No});
+    else {
+      p->Vaibj = OTen(ctx, {Nv, No, Nv, No});
+      contract(ctx, 1.0, p->Gab, "Gab", p->Gij, "Gij", 0.0, p->Vaibj, "aibj", precision);
+    }
+    if (in.Vijkl) up(p->Vijkl, in.Vijkl, {No, No, No, No});
+    else {
+      p->Vijkl = OTen(ctx, {No, No, No, No});
+      contract(ctx, 1.0, p->Gij, "Gik", p->Gij, "Gjl", 0.0, p->Vijkl, "ijkl", precision);
+    }
+  }
+  if (in.Vijka) up(p->Vijka, in.Vijka, {No, No, No, Nv});
+  else {
+    p->Vijka = OTen(ctx, {No, No, No, Nv});
+    contract(ctx, 1.0, p->Gij, "Gik", p->Gai, "Gaj", 0.0, p->Vijka, "ijka", precision);
+  }
+  p->Vx = OTen(ctx, {Nv, Nv, No, No});
+  assign(ctx, 1.0, p->Vabij, "baij", 0.0, p->Vx, "abij");
+  return p;
+}
+
+Ccsd::Ccsd(Context &ctx, std::unique_ptr<CcsdInputs> in,
+           const gbcc_ccsd_opts &o, const double *init_T1_host,
+           const double *init_T2_host)
+    : ctx_(ctx), in_(std::move(in)), o_(o), L_(in_->Nv, in_->No) {
+  require(o_.max_residua >= 1 && o_.max_residua <= GBCC_MAX_DIIS,
+          "maxResidua must be in [1, 16]");
+  require(o_.mixer == 0 || o_.mixer == 1, "mixer must be LinearMixer or DiisMixer");
+  const int64_t Nv = L_.Nv, No = L_.No;
+  // integralsSliceSize (CcsdEnergyFromCoulombIntegrals.cxx:375-385)
+  if (o_.integrals_slice_size > 0) slice_ = o_.integrals_slice_size;
+  else if (o_.integrals_slice_factor >= 0) slice_ = (int64_t)(Nv * o_.integrals_slice_factor);
+  else {
+    // device default: the largest slice whose V_xycd (plus its GEMM-layout
+    // copy) stays within 4 GiB; the energy does not depend on the slicing
+    const double budget = 4.0 * 1024 * 1024 * 1024 / 16.0;
+    slice_ = (int64_t)std::floor(std::sqrt(budget / (double)(Nv * Nv)));
+  }
+  slice_ = std::max<int64_t>(1, std::min<int64_t>(slice_, Nv));
+  const size_t fb = sizeof(double) * L_.ntot;
+  T_.alloc(ctx_, fb);
+  R_.alloc(ctx_, fb);
+  fill(ctx_, T_.as<double>(), L_.ntot, 0.0);
+  if (init_T1_host)
+    GBCC_CUDA(cudaMemcpyAsync(T_.as<double>(), init_T1_host, 8 * L_.n1,
+                              cudaMemcpyHostToDevice, ctx_.stream));
+  if (init_T2_host) {
+    GBCC_CUDA(cudaMemcpyAsync(T_.as<double>() + L_.off2, init_T2_host,
+                              8 * L_.n2, cudaMemcpyHostToDevice, ctx_.stream));
+    init_doubles_ = true;
+  }
+  (void)No;
+  const int nb = reduction_blocks(ctx_, L_.ntot);
+  partials_.alloc(ctx_, sizeof(double) * nb * (2 + GBCC_MAX_DIIS + 4));
+  scal_.alloc(ctx_, sizeof(double) * SC_N);
+  fill(ctx_, scal_.as<double>(), SC_N, 0.0);
+  if (o_.mixer == 1) {
+    const int N = o_.max_residua;
+    slotA_.resize(N);
+    slotD_.resize(N);
+    B_.alloc(ctx_, sizeof(double) * (N + 1) * (N + 1));
+    std::vector<double> b((N + 1) * (N + 1), 0.0);
+    for (int i = 1; i <= N; ++i) b[0 + (N + 1) * i] = b[i + 0] = -1.0;  // DiisMixer.cxx:68-96
+    GBCC_CUDA(cudaMemcpyAsync(B_.as<double>(), b.data(), 8 * b.size(),
+                              cudaMemcpyHostToDevice, ctx_.stream));
+    w_.alloc(ctx_, sizeof(double) * GBCC_MAX_DIIS);
+    hist_slot_.alloc(ctx_, sizeof(int) * GBCC_MAX_DIIS * 2);
+  } else {
+    E_.alloc(ctx_, fb);
+    D_.alloc(ctx_, fb);
+    Lres_.alloc(ctx_, fb);
+  }
+  GBCC_CUDA(cudaMallocHost(&pinned_, sizeof(double) * SC_N));
+}
+
+Ccsd::~Ccsd() {
+  cudaStreamSynchronize(ctx_.stream);
+  if (pinned_) cudaFreeHost(pinned_);
+}
+
+void Ccsd::pair_energies(double *dev_out) {
+  double *T = T_.as<double>();
+  gbcc::pair_energy(ctx_, T, T + L_.off2, in_->Vabij.p(), in_->Vx.p(), L_.Nv,
+                    L_.No, dev_out);
+}
+
+void Ccsd::residual(int it, const double *Tp, double *Rp) {
+  Context &ctx = ctx_;
+  CcsdInputs &I = *in_;
+  const int prec = o_.precision;
+  const int64_t No = L_.No, Nv = L_.Nv, NG = I.NG;
+  const bool dist = o_.distinguishable != 0;
+  auto C = [&](double al, const Ten &A, const char *ia, const Ten &B,
+               const char *ib, double be, const Ten &Cc, const char *ic) {
+    contract(ctx, al, A, ia, B, ib, be, Cc, ic, prec);
+  };
+  Ten T1 = T1v(L_, const_cast<double *>(Tp)), T2 = T2v(L_, const_cast<double *>(Tp));
+  Ten R1 = T1v(L_, Rp), R2 = T2v(L_, Rp);
+  fill(ctx, Rp, L_.ntot, 0.0);                                     // :37-38
+  const Ten &V = I.Vabij, &Vx = I.Vx;
+  if (it == 0 && !init_doubles_) {                                 // :47-51
+    copy(ctx, R2.p, V.p, L_.n2);
+    return;
+  }
+  const Ten &Vaibj = I.Vaibj, &Vijkl = I.Vijkl, &Vijka = I.Vijka;
+  const Ten &Gai = I.Gai, &Gab = I.Gab, &Gij = I.Gij;
+
+  OTen X(ctx, {Nv, Nv, No, No});                                   // :136-138
+  outer_add(ctx, X.p(), T2.p, T1.p, 1.0, Nv, No);
+  OTen Kac(ctx, {Nv, Nv}), Kki(ctx, {No, No});
+  {
+    OTen Lac(ctx, {Nv, Nv}), Lki(ctx, {No, No});
+    C(-2.0, V, "cdkl", X, "adkl", 0.0, Kac, "ac");                 // :146
+    C(1.0, Vx, "cdkl", X, "adkl", 1.0, Kac, "ac");                 // :147 V["dckl"]
+    if (!dist) copy(ctx, Lac.p(), Kac.p(), Nv * Nv);               // :151
+    else {
+      OTen Y(ctx, {Nv, Nv, No, No});                               // :154-156
+      outer_add(ctx, Y.p(), T2.p, T1.p, 2.0, Nv, No);
+      C(-1.0, V, "cdkl", Y, "adkl", 0.0, Lac, "ac");               // :157-158
+      C(0.5, Vx, "cdkl", Y, "adkl", 1.0, Lac, "ac");               // :159-160
+    }
+    {
+      OTen t(ctx, {NG});                                           // :162-163
+      C(1.0, Gai, "Gdk", T1, "dk", 0.0, t, "G");
+      C(2.0, Gab, "Gca", t, "G", 1.0, Lac, "ac");
+      OTen Q(ctx, {NG, Nv, No});                                   // :166-167
+      C(1.0, Gab, "Gda", T1, "dk", 0.0, Q, "Gak");
+      C(-1.0, Gai, "Gck", Q, "Gak", 1.0, Lac, "ac");
+    }
+    C(2.0, V, "cdkl", X, "cdil", 0.0, Kki, "ki");                  // :172
+    C(-1.0, Vx, "cdkl", X, "cdil", 1.0, Kki, "ki");                // :173 V["dckl"]
+    if (!dist) copy(ctx, Lki.p(), Kki.p(), No * No);               // :177
+    else {
+      OTen Y(ctx, {Nv, Nv, No, No});                               // :180-182
+      outer_add(ctx, Y.p(), T2.p, T1.p, 2.0, Nv, No);
+      C(1.0, V, "cdkl", Y, "cdil", 0.0, Lki, "ki");                // :183-184
+      C(-0.5, Vx, "cdkl", Y, "cdil", 1.0, Lki, "ki");              // :185-186
+    }
+    C(2.0, Vijka, "klic", T1, "cl", 1.0, Lki, "ki");               // :188
+    C(-1.0, Vijka, "lkic", T1, "cl", 1.0, Lki, "ki");              // :189
+    C(1.0, Lac, "ac", T2, "cbij", 1.0, R2, "abij");                // :192
+    C(-1.0, Lki, "ki", T2, "abkj", 1.0, R2, "abij");               // :195
+  }
+  {
+    OTen dGai(ctx, {NG, Nv, No});                                  // :200-206
+    copy(ctx, dGai.p(), Gai.p, Gai.size());
+    C(-1.0, Gij, "Gki", T1, "ak", 1.0, dGai, "Gai");
+    OTen Z(ctx, {NG, Nv, No});                                     // :208-209
+    C(1.0, Gab, "Gbc", T1, "cj", 0.0, Z, "Gbj");
+    C(1.0, dGai, "Gai", Z, "Gbj", 1.0, R2, "abij");
+    C(-1.0, Vijka, "jika", T1, "bk", 1.0, R2, "abij");             // :213
+    OTen W(ctx, {Nv, No, No, No});                                 // :214-215
+    C(1.0, V, "acik", T1, "cj", 0.0, W, "aikj");
+    C(-1.0, T1, "bk", W, "aikj", 1.0, R2, "abij");
+  }
+  {
+    OTen Xakic(ctx, {Nv, No, No, Nv});                             // :218-252
+    {
+      OTen dGai(ctx, {NG, Nv, No});                                // :222-231
+      copy(ctx, dGai.p(), Gai.p, Gai.size());
+      C(-1.0, Gij, "Gil", T1, "al", 1.0, dGai, "Gai");
+      C(1.0, Gab, "Gad", T1, "di", 1.0, dGai, "Gai");
+      C(1.0, dGai, "Gai", Gai, "Gck", 0.0, Xakic, "akic");         // :234-235
+    }
+    OTen Y(ctx, {Nv, Nv, No, No});                                 // :238-240
+    outer_add(ctx, Y.p(), T2.p, T1.p, 2.0, Nv, No);
+    C(-0.5, V, "dclk", Y, "dail", 1.0, Xakic, "akic");             // :242
+    C(1.0, V, "dclk", T2, "adil", 1.0, Xakic, "akic");             // :243
+    if (!dist) C(-0.5, V, "cdlk", T2, "adil", 1.0, Xakic, "akic"); // :245
+    axpby(ctx, L_.n2, 2.0, T2.p, 0.0, Y.p());                      // :248
+    assign(ctx, -1.0, T2, "bckj", 1.0, Y, "cbkj");                 // :249
+    C(1.0, Xakic, "akic", Y, "cbkj", 1.0, R2, "abij");             // :251
+  }
+  {
+    OTen Xakci(ctx, {Nv, No, Nv, No});                             // :254-293
+    {
+      OTen dGab(ctx, {NG, Nv, Nv}), dGij(ctx, {NG, No, No});
+      copy(ctx, dGab.p(), Gab.p, Gab.size());
+      copy(ctx, dGij.p(), Gij.p, Gij.size());
+      C(-1.0, Gai, "Gcl", T1, "al", 1.0, dGab, "Gac");             // :270
+      C(1.0, Gai, "Gdk", T1, "di", 1.0, dGij, "Gki");              // :273
+      C(1.0, dGab, "Gac", dGij, "Gki", 0.0, Xakci, "akci");        // :277-280
+    }
+    if (!dist) C(-0.5, V, "cdlk", T2, "dail", 1.0, Xakci, "akci"); // :284
+    C(-1.0, Xakci, "akci", T2, "cbkj", 1.0, R2, "abij");           // :288
+    C(-1.0, Xakci, "bkci", T2, "ackj", 1.0, R2, "abij");           // :289
+    OTen Rc(ctx, {Nv, Nv, No, No});                                // :292
+    copy(ctx, Rc.p(), R2.p, L_.n2);
+    assign(ctx, 1.0, Rc, "baji", 1.0, R2, "abij");
+  }
+  axpby(ctx, L_.n2, 1.0, V.p, 1.0, R2.p);                          // :301
+  {
+    OTen Xklij(ctx, {No, No, No, No});                             // :305-333
+    copy(ctx, Xklij.p(), Vijkl.p, No * No * No * No);              // :308
+    C(1.0, Vijka, "klic", T1, "cj", 1.0, Xklij, "klij");           // :309
+    C(1.0, Vijka, "lkjc", T1, "ci", 1.0, Xklij, "klij");           // :310
+    C(1.0, Xklij, "klij", X, "abkl", 1.0, R2, "abij");             // :313
+    if (!dist) C(1.0, V, "cdkl", X, "cdij", 0.0, Xklij, "klij");   // :317
+    else {
+      OTen Wq(ctx, {Nv, No, No, No});                              // :319
+      C(1.0, V, "cdkl", T1, "dj", 0.0, Wq, "cklj");
+      C(1.0, T1, "ci", Wq, "cklj", 0.0, Xklij, "klij");
+    }
+    if (o_.ppl) C(1.0, Xklij, "klij", T2, "abkl", 1.0, R2, "abij");  // :330
+    else C(1.0, Xklij, "klij", X, "abkl", 1.0, R2, "abij");          // :332
+  }
+  if (o_.ppl) {                                                    // :374-452
+    OTen dG(ctx, {NG, Nv, Nv});                                    // :392-400
+    copy(ctx, dG.p(), Gab.p, Gab.size());
+    C(-1.0, Gai, "Gbk", T1, "ak", 1.0, dG, "Gab");
+    const int64_t s = slice_;
+    const int64_t ns = (Nv + s - 1) / s;                           // :387
+    std::vector<OTen> sl;                                          // :402-416
+    for (int64_t v = 0; v < ns; ++v) {
+      const int64_t x0 = v * s, nx = std::min(s, Nv - x0);
+      sl.emplace_back(ctx, std::initializer_list<int64_t>{NG, nx, Nv});
+      gather_slice(ctx, sl.back().p(), dG.p(), NG, Nv, x0, nx);
+    }
+    for (int64_t m = 0; m < ns; ++m) {                             // :418
+      for (int64_t n = m; n < ns; ++n) {                           // :419
+        const int64_t nx = sl[n].t.lens[1], ny = sl[m].t.lens[1];
+        OTen Vs(ctx, {nx, ny, Nv, Nv});                            // :425-434
+        C(1.0, sl[n], "Gxc", sl[m], "Gyd", 0.0, Vs, "xycd");
+        OTen Rxy(ctx, {nx, ny, No, No});                           // :443
+        C(1.0, Vs, "xycd", X, "cdij", 0.0, Rxy, "xyij");
+        const int64_t a0 = n * s, b0 = m * s;                      // :444-447
+        slice_add(ctx, R2.p, Rxy.p(), Nv, No, a0, b0, nx, ny, a0 > b0);
+      }
+    }
+  }
+  {
+    C(1.0, Kac, "ac", T1, "ci", 1.0, R1, "ai");                    // :466
+    C(-1.0, Kki, "ki", T1, "ak", 1.0, R1, "ai");                   // :467
+    OTen Kck(ctx, {Nv, No});
+    C(2.0, V, "cdkl", T1, "dl", 0.0, Kck, "ck");                   // :470
+    C(-1.0, Vx, "cdkl", T1, "dl", 1.0, Kck, "ck");                 // :471 V["dckl"]
+    C(2.0, Kck, "ck", T2, "caki", 1.0, R1, "ai");                  // :474
+    C(-1.0, Kck, "ck", T2, "caik", 1.0, R1, "ai");                 // :475
+    OTen u(ctx, {No, No});                                         // :476
+    C(1.0, Kck, "ck", T1, "ci", 0.0, u, "ki");
+    C(1.0, T1, "ak", u, "ki", 1.0, R1, "ai");
+    C(2.0, V, "acik", T1, "ck", 1.0, R1, "ai");                    // :477
+    C(-1.0, Vaibj, "ciak", T1, "ck", 1.0, R1, "ai");               // :478
+    OTen H(ctx, {NG, Nv, No});                                     // :480-483
+    C(1.0, Gai, "Gdk", X, "cdik", 0.0, H, "Gci");
+    C(2.0, Gab, "Gca", H, "Gci", 1.0, R1, "ai");
+    C(1.0, Gai, "Gck", X, "cdik", 0.0, H, "Gdi");                  // :484-487
+    C(-1.0, Gab, "Gda", H, "Gdi", 1.0, R1, "ai");
+    C(-2.0, Vijka, "klic", X, "ackl", 1.0, R1, "ai");              // :489
+    C(1.0, Vijka, "lkic", X, "ackl", 1.0, R1, "ai");               // :490
+  }
+}
+
+IterInfo Ccsd::iterate() {
+  Context &ctx = ctx_;
+  double *sc = scal_.as<double>();
+  const int64_t n = L_.ntot;
+  residual(it_, T_.as<double>(), R_.as<double>());                 // :95
+  IterInfo info;
+  double *amp = nullptr;
+  if (o_.mixer == 1) {                                             // DiisMixer
+    const int N = o_.max_residua;
+    const int k = next_;
+    if (!slotA_[k].bytes()) {
+      slotA_[k].alloc(ctx, 8 * n);
+      slotD_[k].alloc(ctx, 8 * n);
+    }
+    std::vector<const double *> hist;
+    std::vector<int> hslot;
+    for (int i = 0; i < N; ++i)
+      if (i != k && slotD_[i].bytes() && (i < count_ || count_ == N)) {
+        hist.push_back(slotD_[i].as<double>());
+        hslot.push_back(i);
+      }
+    jacobi_update(ctx, L_, R_.as<double>(), T_.as<double>(),
+                  slotA_[k].as<double>(), slotD_[k].as<double>(),
+                  in_->eps_h.p(), in_->eps_p.p(), o_.level_shift,
+                  (int)hist.size(), hist.data(), partials_.as<double>(),
+                  sc + SC_UPD);                                    // :96-98
+    if (!hslot.empty())
+      GBCC_CUDA(cudaMemcpyAsync(hist_slot_.as<int>(), hslot.data(),
+                                sizeof(int) * hslot.size(),
+                                cudaMemcpyHostToDevice, ctx.stream));
+    if (count_ < N) ++count_;                                      // DiisMixer.cxx:141
+    // status as int in the double slot SC_STATUS (reinterpreted)
+    diis_solve(ctx, B_.as<double>(), N, k, count_, sc + SC_UPD,
+               (int)hslot.size(), hist_slot_.as<int>(), w_.as<double>(),
+               sc + SC_LAMBDA, reinterpret_cast<int *>(sc + SC_STATUS));
+    std::vector<const double *> src;
+    for (int j = 0; j < count_; ++j) src.push_back(slotA_[(k + N - j) % N].as<double>());
+    diis_combine(ctx, count_, src.data(), w_.as<double>(), T_.as<double>(), n,
+                 partials_.as<double>(), sc + SC_TT);              // :160-174
+    next_ = (k + 1) % N;                                           // :179
+    amp = T_.as<double>();
+  } else {                                                         // LinearMixer
+    jacobi_update(ctx, L_, R_.as<double>(), T_.as<double>(), E_.as<double>(),
+                  D_.as<double>(), in_->eps_h.p(), in_->eps_p.p(),
+                  o_.level_shift, 0, nullptr, partials_.as<double>(),
+                  sc + SC_UPD);
+    if (have_last_ && o_.mixing_ratio != 1.0) {
+      linear_mix(ctx, E_.as<double>(), D_.as<double>(), T_.as<double>(),
+                 Lres_.as<double>(), o_.mixing_ratio, n,
+                 partials_.as<double>(), sc + SC_LIN);
+      // convergence sums come from the mixed vectors
+      copy(ctx, sc + SC_UPD, sc + SC_LIN, 2);
+    }
+    have_last_ = true;
+    std::swap(T_, E_);                                             // amplitudes = last
+    std::swap(Lres_, D_);
+    amp = T_.as<double>();
+  }
+  energy_terms(ctx, amp, amp + L_.off2, in_->Vabij.p(), in_->Vx.p(), L_.Nv,
+               L_.No, partials_.as<double>(), sc + SC_EN);         // :102
+  GBCC_CUDA(cudaMemcpyAsync(pinned_, sc, sizeof(double) * SC_N,
+                            cudaMemcpyDeviceToHost, ctx.stream));
+  GBCC_CUDA(cudaStreamSynchronize(ctx.stream));
+  const double *h = pinned_;
+  const double spins = 2.0;
+  double d = 0.5 * spins * spins * h[SC_EN + 0];                   // :170-172
+  d = d + 0.5 * spins * spins * h[SC_EN + 1];
+  double x = (-0.5) * spins * h[SC_EN + 2];                        // :175-177
+  x = x + (-0.5) * spins * h[SC_EN + 3];
+  info.direct = d;
+  info.exchange = x;
+  info.energy = d + x;                                             // :189
+  info.dtdt = h[SC_UPD + 0];
+  info.tt = (o_.mixer == 1) ? h[SC_TT] : h[SC_UPD + 1];
+  info.lambda = h[SC_LAMBDA];
+  int st = 0;
+  std::memcpy(&st, h + SC_STATUS, sizeof(int));
+  info.diis_status = (o_.mixer == 1) ? st : 0;
+  return info;
+}
+
+gbcc_status Ccsd::run(int n, double *energy, int *converged) {
+  gbcc_status st = GBCC_OK;
+  for (int c = 0; c < n && !converged_; ++c) {
+    if (it_ >= o_.max_iterations) break;
+    IterInfo info = iterate();
+    e_ = info.energy;
+    dir_ = info.direct;
+    exc_ = info.exchange;
+    hist_.push_back(e_);
+    ++it_;
+    if (info.diis_status) {
+      st = GBCC_DIIS_SINGULAR;
+      break;
+    }
+    if (!std::isfinite(e_) || !std::isfinite(info.dtdt) || !std::isfinite(info.tt)) {
+      st = GBCC_DIVERGED;
+      break;
+    }
+    // ClusterSinglesDoublesAlgorithm.cxx:103-106
+    if (std::abs((e_ - prev_) / e_) < std::abs(o_.energy_convergence) &&
+        std::abs(info.dtdt / info.tt) <
+            std::abs(o_.amplitudes_convergence * o_.amplitudes_convergence)) {
+      converged_ = true;
+      break;
+    }
+    prev_ = e_;
+  }
+  if (energy) *energy = e_;
+  if (converged) *converged = converged_ ? 1 : 0;
+  return st;
+}
+
+}  // namespace gbcc

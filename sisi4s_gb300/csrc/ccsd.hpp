@@ -1,0 +1,74 @@
+// Device-resident closed-shell CCSD solver.
+#pragma once
+
+#include <memory>
+#include <vector>
+
+#include "ccsd_kernels.hpp"
+
+namespace gbcc {
+
+struct CcsdInputs {
+  int64_t No = 0, Nv = 0, NG = 0;
+  OTen eps_h, eps_p;          // [No], [Nv]
+  OTen Gai, Gab, Gij;         // [NG,Nv,No], [NG,Nv,Nv], [NG,No,No]
+  OTen Vabij, Vx, Vaibj, Vijkl, Vijka;  // Vx[a,b,i,j] = Vabij[b,a,i,j]
+};
+
+// Upload eps and Gamma, slice the vertex blocks, upload or build the
+// integrals (CoulombIntegralsFromVertex.cxx:395-417).
+std::unique_ptr<CcsdInputs> upload_inputs(Context &ctx, const gbcc_ccsd_in &in,
+                                          int precision, bool need_vaibj);
+
+struct IterInfo {
+  double energy = 0, direct = 0, exchange = 0, dtdt = 0, tt = 0, lambda = 0;
+  int diis_status = 0;
+};
+
+class Ccsd {
+ public:
+  Ccsd(Context &ctx, std::unique_ptr<CcsdInputs> in, const gbcc_ccsd_opts &o,
+       const double *init_T1_host, const double *init_T2_host);
+  ~Ccsd();
+  Ccsd(const Ccsd &) = delete;
+  Ccsd &operator=(const Ccsd &) = delete;
+  // R = residual(it, T) into R_ (parity entry point uses it directly)
+  void residual(int it, const double *T, double *R);
+  // one full iteration; returns the host-side info
+  IterInfo iterate();
+  // runs up to n iterations; returns status
+  gbcc_status run(int n, double *energy, int *converged);
+  const double *amplitudes() const { return T_.as<double>(); }
+  const FockLayout &layout() const { return L_; }
+  CcsdInputs &inputs() { return *in_; }
+  Context &ctx() { return ctx_; }
+  int iterations_done() const { return it_; }
+  bool converged() const { return converged_; }
+  double energy() const { return e_; }
+  double direct() const { return dir_; }
+  double exchange() const { return exc_; }
+  const std::vector<double> &history() const { return hist_; }
+  void pair_energies(double *dev_out);
+  int64_t slice_size() const { return slice_; }
+
+ private:
+  Context &ctx_;
+  std::unique_ptr<CcsdInputs> in_;
+  gbcc_ccsd_opts o_;
+  FockLayout L_;
+  bool init_doubles_ = false;
+  int64_t slice_ = 0;
+  DBuf T_, R_;                 // current amplitudes, residual
+  DBuf E_, D_, Lres_;          // linear mixer: estimate, change, last change
+  std::vector<DBuf> slotA_, slotD_;  // DIIS history
+  DBuf B_, w_, scal_, partials_, hist_slot_;
+  int next_ = 0, count_ = 0;
+  bool have_last_ = false;
+  int it_ = 0;
+  bool converged_ = false;
+  double e_ = 0, prev_ = 0, dir_ = 0, exc_ = 0;
+  std::vector<double> hist_;
+  double *pinned_ = nullptr;
+};
+
+}  // namespace gbcc

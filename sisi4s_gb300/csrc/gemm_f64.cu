@@ -1,0 +1,227 @@
+// FP64 GEMM for sm_103a: C[M,N] = alpha op(A) op(B) + beta C, column-major.
+//
+// GB300 has no float64 kind for tcgen05.mma and a float64 rate far below its
+// bf16 rate, so the plain-FP64 path is bound by the FP64 FMA pipe, not by
+// HBM: a 64x64 block tile with 4x4 outputs per thread needs 0.25 bytes of
+// shared memory per flop and ~0.03 bytes of global memory per flop, far below
+// what the SM delivers.  The kernel therefore optimises for keeping the FP64
+// pipe fed: operand tiles are staged in shared memory with a register
+// prefetch of the next k-tile, so the global loads of tile k+1 overlap the
+// FMAs of tile k.
+#include "internal.hpp"
+
+namespace gbcc {
+namespace {
+
+constexpr int BM = 64, BN = 64, BK = 16, NT = 256;
+
+struct PtrBatch {
+  const double *const *A;
+  const double *const *B;
+  double *const *C;
+};
+
+template <bool TA, bool TB>
+__device__ __forceinline__ void load_tiles(const double *__restrict__ A,
+                                           int64_t lda,
+                                           const double *__restrict__ B,
+                                           int64_t ldb, int64_t M, int64_t N,
+                                           int64_t K, int64_t m0, int64_t n0,
+                                           int64_t k0, double ra[4],
+                                           double rb[4]) {
+  const int t = threadIdx.x;
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    int64_t m, k;
+    if (!TA) {  // A(m,k) = A[m + k lda], m contiguous
+      m = m0 + (t % 64);
+      k = k0 + (t / 64) + 4 * r;
+    } else {  // A(m,k) = A[k + m lda], k contiguous
+      k = k0 + (t % 16);
+      m = m0 + (t / 16) + 16 * r;
+    }
+    ra[r] = (m < M && k < K) ? (TA ? A[k + m * lda] : A[m + k * lda]) : 0.0;
+  }
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    int64_t n, k;
+    if (!TB) {  // B(k,n) = B[k + n ldb], k contiguous
+      k = k0 + (t % 16);
+      n = n0 + (t / 16) + 16 * r;
+    } else {  // B(k,n) = B[n + k ldb], n contiguous
+      n = n0 + (t % 64);
+      k = k0 + (t / 64) + 4 * r;
+    }
+    rb[r] = (n < N && k < K) ? (TB ? B[n + k * ldb] : B[k + n * ldb]) : 0.0;
+  }
+}
+
+template <bool TA, bool TB>
+__device__ __forceinline__ void store_tiles(double (*As)[BM + 1],
+                                            double (*Bs)[BN + 1],
+                                            const double ra[4],
+                                            const double rb[4]) {
+  const int t = threadIdx.x;
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    int m, k;
+    if (!TA) {
+      m = t % 64;
+      k = t / 64 + 4 * r;
+    } else {
+      k = t % 16;
+      m = t / 16 + 16 * r;
+    }
+    As[k][m] = ra[r];
+  }
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    int n, k;
+    if (!TB) {
+      k = t % 16;
+      n = t / 16 + 16 * r;
+    } else {
+      n = t % 64;
+      k = t / 64 + 4 * r;
+    }
+    Bs[k][n] = rb[r];
+  }
+}
+
+template <bool TA, bool TB, bool PTR>
+__global__ void __launch_bounds__(NT)
+    dgemm_kernel(int64_t M, int64_t N, int64_t K, double alpha,
+                 const double *__restrict__ A0, int64_t lda,
+                 const double *__restrict__ B0, int64_t ldb, double beta,
+                 double *__restrict__ C0, int64_t ldc, int64_t sA, int64_t sB,
+                 int64_t sC, PtrBatch pb, int64_t tiles_m) {
+  __shared__ double As[BK][BM + 1];
+  __shared__ double Bs[BK][BN + 1];
+  const int64_t z = blockIdx.z + (int64_t)gridDim.z * blockIdx.y;
+  const double *A;
+  const double *B;
+  double *C;
+  if (PTR) {
+    A = pb.A[z];
+    B = pb.B[z];
+    C = pb.C[z];
+  } else {
+    A = A0 + z * sA;
+    B = B0 + z * sB;
+    C = C0 + z * sC;
+  }
+  const int64_t tm = blockIdx.x % tiles_m;
+  const int64_t tn = blockIdx.x / tiles_m;
+  const int64_t m0 = tm * BM, n0 = tn * BN;
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  double acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
+
+  double ra[4], rb[4];
+  load_tiles<TA, TB>(A, lda, B, ldb, M, N, K, m0, n0, 0, ra, rb);
+  for (int64_t k0 = 0; k0 < K; k0 += BK) {
+    store_tiles<TA, TB>(As, Bs, ra, rb);
+    __syncthreads();
+    if (k0 + BK < K)
+      load_tiles<TA, TB>(A, lda, B, ldb, M, N, K, m0, n0, k0 + BK, ra, rb);
+#pragma unroll
+    for (int kk = 0; kk < BK; ++kk) {
+      double a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = As[kk][tx + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) b[j] = Bs[kk][ty + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int64_t n = n0 + ty + 16 * j;
+    if (n >= N) continue;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int64_t m = m0 + tx + 16 * i;
+      if (m >= M) continue;
+      double *c = C + m + n * ldc;
+      double v = alpha * acc[i][j];
+      if (beta != 0.0) v = fma(beta, *c, v);
+      *c = v;
+    }
+  }
+}
+
+template <bool PTR>
+void launch(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
+            double alpha, const double *A, int64_t lda, const double *B,
+            int64_t ldb, double beta, double *C, int64_t ldc, int64_t batch,
+            int64_t sA, int64_t sB, int64_t sC, PtrBatch pb) {
+  if (M <= 0 || N <= 0 || batch <= 0) return;
+  const int64_t tiles_m = (M + BM - 1) / BM;
+  const int64_t tiles_n = (N + BN - 1) / BN;
+  require(tiles_m * tiles_n < (1LL << 31), "gemm: too many tiles");
+  // batch split into grid.z (<= 65535) x grid.y
+  int64_t gz = batch < 65535 ? batch : 65535;
+  while (batch % gz) --gz;
+  const int64_t gy = batch / gz;
+  require(gy <= 65535, "gemm: batch too large");
+  dim3 grid((unsigned)(tiles_m * tiles_n), (unsigned)gy, (unsigned)gz);
+  auto k00 = dgemm_kernel<false, false, PTR>;
+  auto k01 = dgemm_kernel<false, true, PTR>;
+  auto k10 = dgemm_kernel<true, false, PTR>;
+  auto k11 = dgemm_kernel<true, true, PTR>;
+  auto kern = ta ? (tb ? k11 : k10) : (tb ? k01 : k00);
+  kern<<<grid, NT, 0, ctx.stream>>>(M, N, K, alpha, A, lda, B, ldb, beta, C,
+                                    ldc, sA, sB, sC, pb, tiles_m);
+  GBCC_CHECK_LAUNCH(ctx);
+  ctx.flops += 2.0 * (double)M * (double)N * (double)K * (double)batch;
+}
+
+}  // namespace
+
+void gemm_f64(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
+              double alpha, const double *A, int64_t lda, const double *B,
+              int64_t ldb, double beta, double *C, int64_t ldc, int64_t batch,
+              int64_t sA, int64_t sB, int64_t sC) {
+  if (K == 0) {
+    // C = beta C
+    require(batch == 1 || sC >= ldc * N, "gemm: K=0 with overlapping batch");
+    for (int64_t z = 0; z < batch; ++z)
+      for (int64_t n = 0; n < N; ++n)
+        axpby(ctx, M, 0.0, C + z * sC + n * ldc, beta, C + z * sC + n * ldc);
+    return;
+  }
+  launch<false>(ctx, ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc,
+                batch, sA, sB, sC, PtrBatch{nullptr, nullptr, nullptr});
+}
+
+void gemm_f64_ptr(Context &ctx, bool ta, bool tb, int64_t M, int64_t N,
+                  int64_t K, double alpha, const double *const *A, int64_t lda,
+                  const double *const *B, int64_t ldb, double beta,
+                  double *const *C, int64_t ldc, int64_t batch) {
+  require(K > 0, "gemm_f64_ptr: K must be positive");
+  launch<true>(ctx, ta, tb, M, N, K, alpha, nullptr, lda, nullptr, ldb, beta,
+               nullptr, ldc, batch, 0, 0, 0, PtrBatch{A, B, C});
+}
+
+void gemm(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
+          double alpha, const double *A, int64_t lda, const double *B,
+          int64_t ldb, double beta, double *C, int64_t ldc, int64_t batch,
+          int64_t sA, int64_t sB, int64_t sC, int precision) {
+  const double fl = 2.0 * (double)M * (double)N * (double)K * (double)batch;
+  if (precision == GBCC_PREC_EMU && K > 0 && fl >= ctx.emu_min_flops) {
+    gemm_emu(ctx, ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, batch,
+             sA, sB, sC);
+    return;
+  }
+  gemm_f64(ctx, ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, batch,
+           sA, sB, sC);
+}
+
+}  // namespace gbcc

@@ -1,0 +1,181 @@
+// Internal declarations of libgbcc: context, device tensors, launch helpers
+// and the contraction engine.  Not part of the ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <array>
+#include <atomic>
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/gbcc.h"
+
+namespace gbcc {
+
+// Thrown inside the library and turned into a gbcc_status at the ABI.
+struct Error : std::runtime_error {
+  gbcc_status status;
+  Error(gbcc_status s, const std::string &m) : std::runtime_error(m), status(s) {}
+};
+
+#define GBCC_CUDA(call)                                                        \
+  do {                                                                         \
+    cudaError_t e_ = (call);                                                   \
+    if (e_ != cudaSuccess) {                                                   \
+      throw ::gbcc::Error(e_ == cudaErrorMemoryAllocation ? GBCC_OOM           \
+                                                          : GBCC_CUDA_ERROR,   \
+                          std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    }                                                                          \
+  } while (0)
+
+#define GBCC_CHECK_LAUNCH(ctx)                                                 \
+  do {                                                                         \
+    (ctx).launches++;                                                          \
+    cudaError_t e_ = cudaGetLastError();                                       \
+    if (e_ != cudaSuccess)                                                     \
+      throw ::gbcc::Error(GBCC_CUDA_ERROR,                                     \
+                          std::string("launch: ") + cudaGetErrorString(e_));   \
+  } while (0)
+
+inline void require(bool ok, const std::string &msg) {
+  if (!ok) throw Error(GBCC_BAD_ARG, msg);
+}
+
+struct Context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  std::string last_error;
+  uint64_t launches = 0;
+  double flops = 0.0;     // FP64-equivalent flops issued to GEMMs
+  int sm_count = 0;
+  // emulated-GEMM configuration
+  int emu_slices = 7;
+  // GEMMs smaller than this many flops stay in FP64 in precision mode
+  double emu_min_flops = 1e7;
+};
+
+// Stream-ordered device buffer (cudaMallocAsync on the context stream).
+class DBuf {
+ public:
+  DBuf() = default;
+  DBuf(Context &ctx, size_t bytes) { alloc(ctx, bytes); }
+  DBuf(const DBuf &) = delete;
+  DBuf &operator=(const DBuf &) = delete;
+  DBuf(DBuf &&o) noexcept { *this = std::move(o); }
+  DBuf &operator=(DBuf &&o) noexcept {
+    if (this != &o) {
+      release();
+      p_ = o.p_;
+      bytes_ = o.bytes_;
+      stream_ = o.stream_;
+      o.p_ = nullptr;
+      o.bytes_ = 0;
+    }
+    return *this;
+  }
+  ~DBuf() { release(); }
+  void alloc(Context &ctx, size_t bytes) {
+    release();
+    stream_ = ctx.stream;
+    bytes_ = bytes;
+    if (bytes == 0) return;
+    GBCC_CUDA(cudaMallocAsync(&p_, bytes, ctx.stream));
+  }
+  void release() {
+    if (p_) cudaFreeAsync(p_, stream_);
+    p_ = nullptr;
+    bytes_ = 0;
+  }
+  template <class T = double>
+  T *as() const { return static_cast<T *>(p_); }
+  size_t bytes() const { return bytes_; }
+
+ private:
+  void *p_ = nullptr;
+  size_t bytes_ = 0;
+  cudaStream_t stream_ = nullptr;
+};
+
+// Dense column-major FP64 tensor view (first index fastest), up to order 6.
+struct Ten {
+  double *p = nullptr;
+  int order = 0;
+  std::array<int64_t, 6> lens{};
+  int64_t size() const {
+    int64_t s = 1;
+    for (int d = 0; d < order; ++d) s *= lens[d];
+    return s;
+  }
+};
+
+inline Ten ten(double *p, std::initializer_list<int64_t> l) {
+  Ten t;
+  t.p = p;
+  t.order = static_cast<int>(l.size());
+  int d = 0;
+  for (auto x : l) t.lens[d++] = x;
+  return t;
+}
+
+// Owned tensor = buffer + view.
+struct OTen {
+  DBuf buf;
+  Ten t;
+  OTen() = default;
+  OTen(Context &ctx, std::initializer_list<int64_t> l) {
+    t = ten(nullptr, l);
+    buf.alloc(ctx, sizeof(double) * t.size());
+    t.p = buf.as<double>();
+  }
+  operator Ten &() { return t; }
+  operator const Ten &() const { return t; }
+  double *p() const { return t.p; }
+};
+
+// ---------------------------------------------------------------- kernels
+// GEMM: C[M,N] = alpha op(A) op(B) + beta C (column-major), batched with
+// constant strides.  precision: GBCC_PREC_FP64 or GBCC_PREC_EMU.
+void gemm(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
+          double alpha, const double *A, int64_t lda, const double *B,
+          int64_t ldb, double beta, double *C, int64_t ldc, int64_t batch = 1,
+          int64_t sA = 0, int64_t sB = 0, int64_t sC = 0,
+          int precision = GBCC_PREC_FP64);
+void gemm_f64(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
+              double alpha, const double *A, int64_t lda, const double *B,
+              int64_t ldb, double beta, double *C, int64_t ldc, int64_t batch,
+              int64_t sA, int64_t sB, int64_t sC);
+// pointer-array batched FP64 GEMM (device arrays of pointers)
+void gemm_f64_ptr(Context &ctx, bool ta, bool tb, int64_t M, int64_t N,
+                  int64_t K, double alpha, const double *const *A, int64_t lda,
+                  const double *const *B, int64_t ldb, double beta,
+                  double *const *C, int64_t ldc, int64_t batch);
+void gemm_emu(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
+              double alpha, const double *A, int64_t lda, const double *B,
+              int64_t ldb, double beta, double *C, int64_t ldc, int64_t batch,
+              int64_t sA, int64_t sB, int64_t sC);
+
+// dst[perm-out] = alpha * src + beta * dst, where dst index d of the output
+// tensor corresponds to src dimension perm[d]. dst_lens[d] = src.lens[perm[d]].
+void permute(Context &ctx, const Ten &src, const int *perm, double alpha,
+             double beta, Ten &dst);
+void fill(Context &ctx, double *p, int64_t n, double v);
+void copy(Context &ctx, double *dst, const double *src, int64_t n);
+// y = a*x + b*y  (elementwise, mul-then-add rounding, no FMA)
+void axpby(Context &ctx, int64_t n, double a, const double *x, double b,
+           double *y);
+
+// ------------------------------------------------------- contraction engine
+// C[ic] = alpha * A[ia] B[ib] + beta * C[ic]   (einsum-like on index strings;
+// every index of C appears in A or B; summed indices appear in both A and B).
+void contract(Context &ctx, double alpha, const Ten &A, const char *ia,
+              const Ten &B, const char *ib, double beta, const Ten &C,
+              const char *ic, int precision);
+// C[ic] = alpha * A[ia] + beta * C[ic]  (pure index permutation)
+void assign(Context &ctx, double alpha, const Ten &A, const char *ia,
+            double beta, const Ten &C, const char *ic);
+
+}  // namespace gbcc

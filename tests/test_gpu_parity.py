@@ -1,0 +1,181 @@
+"""CUDA path vs the oracle, through the C ABI (GPU)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from oracle.ccsd import ccsd as oracle_ccsd
+from oracle.ccsd import energy as oracle_energy
+from oracle.ccsd import residual as oracle_residual
+from oracle.coulomb import coulomb_integrals as oracle_ints
+from oracle.triples import triples_dense
+from oracle.ueg import UEG_GOLDEN, ueg_real_vertex
+from sisi4s_gb300 import capi
+from sisi4s_gb300 import ccsd as gpu
+from sisi4s_gb300.inputs import make_system
+
+pytestmark = pytest.mark.gpu
+
+# FP64 tolerances.  Contractions are summed in a different order than numpy,
+# so results agree to round-off: relative 1e-12 on residual elements and
+# 1e-10 Ha on energies (the parity gate of the FP64 path).
+RTOL_RES = 1e-12
+ETOL = 1e-10
+
+
+def _rand_amplitudes(Nv, No, seed, scale=0.02):
+    rng = np.random.default_rng(seed)
+    T1 = rng.normal(0, scale, (Nv, No))
+    T2 = rng.normal(0, scale, (Nv, Nv, No, No))
+    return T1, 0.5 * (T2 + T2.transpose(1, 0, 3, 2))
+
+
+def _rel(a, b):
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+def test_dgemm_all_transposes(ctx):
+    import torch  # device memory plumbing only
+    rng = np.random.default_rng(0)
+    for (ta, tb, M, N, K) in [(0, 0, 70, 33, 19), (1, 0, 64, 64, 64),
+                              (0, 1, 5, 130, 7), (1, 1, 129, 1, 300),
+                              (0, 0, 1, 1, 1000)]:
+        A = rng.normal(size=(K, M) if ta else (M, K))
+        B = rng.normal(size=(N, K) if tb else (K, N))
+        Cm = rng.normal(size=(M, N))
+        ref = 0.7 * ((A.T if ta else A) @ (B.T if tb else B)) - 0.3 * Cm
+        dA = torch.tensor(A.T.copy().ravel(), device="cuda")  # column-major
+        dB = torch.tensor(B.T.copy().ravel(), device="cuda")
+        dC = torch.tensor(Cm.T.copy().ravel(), device="cuda")
+        torch.cuda.synchronize()
+        lda = A.shape[0]
+        ldb = B.shape[0]
+        ctx.check(ctx.lib.gbcc_dgemm(ctx.h, ta, tb, M, N, K, 0.7, dA.data_ptr(),
+                                     lda, dB.data_ptr(), ldb, -0.3,
+                                     dC.data_ptr(), M, capi.PREC_FP64))
+        torch.cuda.synchronize()  # device-wide: also waits for the context stream
+        got = dC.cpu().numpy().reshape(N, M).T
+        assert np.abs(got - ref).max() < 1e-12 * max(1, np.abs(ref).max()) * np.sqrt(K)
+
+
+def test_coulomb_integrals_match_oracle(ctx):
+    s = make_system(6, 20, 48, seed=5)
+    got = gpu.coulomb_integrals(ctx, s.gamma, 6)
+    ref = oracle_ints(s.gamma, 6, keys=("PPHH", "PHPH", "HHHH", "HHHP", "HHPP"))
+    for k in ("PPHH", "PHPH", "HHHH", "HHHP", "HHPP"):
+        assert _rel(got[k], ref[k]) < 1e-13, k
+
+
+@pytest.mark.parametrize("No,Nv,NG,dist,ppl,slice_size", [
+    (4, 12, 30, 0, 1, -1),
+    (5, 17, 41, 0, 1, 5),     # reference default slicing (No), ragged last slice
+    (5, 17, 41, 1, 1, 3),     # distinguishable
+    (3, 9, 20, 0, 0, -1),     # ppl = 0
+    (1, 3, 5, 0, 1, 1),       # minimal sizes
+])
+def test_residual_matches_oracle(ctx, No, Nv, NG, dist, ppl, slice_size):
+    s = make_system(No, Nv, NG, seed=No * 100 + Nv)
+    ints = oracle_ints(s.gamma, No)
+    T1, T2 = _rand_amplitudes(Nv, No, seed=Nv)
+    r1, r2 = oracle_residual(1, T1, T2, ints, s.gamma, distinguishable=dist,
+                             ppl=ppl, slice_size=slice_size)
+    g1, g2 = gpu.ccsd_residual(ctx, 1, T1, T2, s.eps_h, s.eps_p, s.gamma,
+                               distinguishable=dist, ppl=ppl,
+                               slice_size=slice_size)
+    assert _rel(g1, r1) < RTOL_RES
+    assert _rel(g2, r2) < RTOL_RES
+
+
+def test_mp2_start_is_exact(ctx):
+    s = make_system(4, 12, 30, seed=1)
+    ints = oracle_ints(s.gamma, 4)
+    T1, T2 = _rand_amplitudes(12, 4, seed=0)
+    g1, g2 = gpu.ccsd_residual(ctx, 0, T1, T2, s.eps_h, s.eps_p, s.gamma,
+                               ints=ints)
+    assert np.array_equal(g2, ints["PPHH"]) and not g1.any()
+
+
+def test_energy_matches_oracle(ctx):
+    s = make_system(5, 15, 40, seed=2)
+    r = gpu.ccsd_solve(ctx, s.eps_h, s.eps_p, s.gamma, max_iterations=3)
+    ints = oracle_ints(s.gamma, 5)
+    e = oracle_energy(r["T1"], r["T2"], ints["PPHH"])
+    assert abs(e["value"] - r["energy"]) < 1e-12 * abs(e["value"])
+
+
+@pytest.mark.parametrize("mixer,ratio", [("LinearMixer", 1.0),
+                                         ("LinearMixer", 0.7),
+                                         ("DiisMixer", 1.0)])
+def test_iterations_match_oracle(ctx, mixer, ratio):
+    s = make_system(4, 14, 36, seed=8)
+    ints = oracle_ints(s.gamma, 4)
+    kw = dict(mixer=mixer, mixing_ratio=ratio, max_residua=3,
+              max_iterations=12, energy_convergence=1e-12,
+              amplitudes_convergence=1e-9)
+    ref = oracle_ccsd(s.eps_h, s.eps_p, ints, s.gamma, **kw)
+    got = gpu.ccsd_solve(ctx, s.eps_h, s.eps_p, s.gamma, **kw)
+    refh = [h["energy"]["value"] for h in ref["history"]]
+    assert got["iterations"] == ref["iterations"]
+    assert np.abs(np.array(got["history"]) - np.array(refh)).max() < ETOL
+    assert _rel(got["T2"], ref["T2"]) < 1e-9
+
+
+def test_c1_config_parity(ctx):
+    """No=10, Nv=50, NG=300, MP2 start, DIIS(5), energyConvergence 3e-11,
+    amplitudesConvergence 1e-7, maxIterations 100: same iteration count and
+    |E_GPU - E_oracle| <= 1e-10 Ha at every iteration."""
+    s = make_system(10, 50, 300, seed=1)
+    ints = oracle_ints(s.gamma, 10)
+    kw = dict(mixer="DiisMixer", max_residua=5, max_iterations=100,
+              energy_convergence=3e-11, amplitudes_convergence=1e-7)
+    ref = oracle_ccsd(s.eps_h, s.eps_p, ints, s.gamma, **kw)
+    got = gpu.ccsd_solve(ctx, s.eps_h, s.eps_p, s.gamma, **kw)
+    refh = np.array([h["energy"]["value"] for h in ref["history"]])
+    assert got["iterations"] == ref["iterations"]
+    assert got["converged"] == ref["converged"]
+    assert np.abs(np.array(got["history"]) - refh).max() < ETOL
+    assert abs(got["energy"] - ref["energy"]) < ETOL
+
+
+def test_ueg_golden_through_gpu(ctx):
+    """The reference golden CCSD and (T) energies reproduced on the GPU."""
+    g = UEG_GOLDEN
+    gamma, eh, ep = ueg_real_vertex(g["No"], g["Nv"], g["rs"])
+    r = gpu.ccsd_solve(ctx, eh, ep, gamma, **g["ccsd_settings"])
+    assert r["converged"]
+    assert abs(r["energy"] - g["ccsd"]) < 2e-9
+    et, etot = gpu.triples(ctx, eh, ep, gamma, r["T1"], r["T2"],
+                           e_ccsd=r["energy"])
+    assert abs(et - g["triples"]) < 1e-10
+    assert abs(etot - (r["energy"] + et)) < 1e-15
+
+
+@pytest.mark.parametrize("No,Nv,NG", [(3, 8, 20), (4, 11, 25), (1, 4, 6)])
+def test_triples_match_oracle(ctx, No, Nv, NG):
+    s = make_system(No, Nv, NG, seed=No + Nv)
+    ints = oracle_ints(s.gamma, No)
+    T1, T2 = _rand_amplitudes(Nv, No, seed=3, scale=0.05)
+    ref = triples_dense(s.eps_h, s.eps_p, T1, T2, ints["PPHH"], ints["HHHP"],
+                        s.gamma)
+    et, _ = gpu.triples(ctx, s.eps_h, s.eps_p, s.gamma, T1, T2)
+    assert abs(et - ref) < 1e-12 * max(1.0, abs(ref))
+
+
+def test_complex_vertex_is_rejected(ctx):
+    s = make_system(2, 4, 6, seed=1)
+    inp = gpu.CcsdInput(s.eps_h, s.eps_p, s.gamma)
+    im = np.zeros(s.gamma.size)
+    im[3] = 1e-3
+    inp.s.gamma_imag = capi.ptr(im)
+    o = gpu.make_opts()
+    out = capi.CcsdOut()
+    st = ctx.lib.gbcc_ccsd_solve(ctx.h, C.byref(inp.s), C.byref(o), C.byref(out))
+    assert st == capi.COMPLEX_UNSUPPORTED
+
+
+def test_deterministic_bits(ctx):
+    s = make_system(4, 12, 30, seed=6)
+    kw = dict(mixer="DiisMixer", max_iterations=6)
+    a = gpu.ccsd_solve(ctx, s.eps_h, s.eps_p, s.gamma, **kw)
+    b = gpu.ccsd_solve(ctx, s.eps_h, s.eps_p, s.gamma, **kw)
+    assert a["energy"] == b["energy"] and np.array_equal(a["T2"], b["T2"])

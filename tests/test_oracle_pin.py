@@ -1,0 +1,109 @@
+"""The oracle against the reference's own golden energies and internal
+consistency checks (CPU only)."""
+import numpy as np
+import pytest
+
+from oracle.ccsd import ccsd, mp2_energy, residual, residual_reference
+from oracle.coulomb import coulomb_integrals
+from oracle.mixers import DiisMixer
+from oracle.triples import permutation, triples_dense, triples_loop
+from oracle.ueg import UEG_GOLDEN, ueg_real_vertex
+from sisi4s_gb300.inputs import make_system
+
+
+@pytest.fixture(scope="module")
+def ueg():
+    g = UEG_GOLDEN
+    gamma, eh, ep = ueg_real_vertex(g["No"], g["Nv"], g["rs"])
+    ints = coulomb_integrals(gamma, g["No"])
+    return gamma, eh, ep, ints
+
+
+def test_ueg_mp2_matches_reference_golden(ueg):
+    gamma, eh, ep, ints = ueg
+    # cc4s.correct.out.yaml:148 secondOrder
+    assert abs(mp2_energy(eh, ep, ints["PPHH"]) - UEG_GOLDEN["mp2"]) < 1e-12
+
+
+def test_ueg_ccsd_and_triples_match_reference_golden(ueg):
+    gamma, eh, ep, ints = ueg
+    r = ccsd(eh, ep, ints, gamma, **UEG_GOLDEN["ccsd_settings"])
+    assert r["converged"]
+    # both codes stop at a relative energy change below 1e-8; the golden
+    # value carries that convergence error, the reference checks 1e-7
+    # (integration-tests/testis.py:256)
+    assert abs(r["energy"] - UEG_GOLDEN["ccsd"]) < 2e-9
+    et = triples_loop(eh, ep, r["T1"], r["T2"], ints["PPHH"], ints["HHHP"],
+                      gamma)
+    assert abs(et - UEG_GOLDEN["triples"]) < 1e-10
+
+
+def test_triples_loop_equals_dense_form(ueg):
+    gamma, eh, ep, ints = ueg
+    s = make_system(4, 10, 24, seed=3)
+    ints = coulomb_integrals(s.gamma, 4)
+    rng = np.random.default_rng(5)
+    T1 = rng.normal(0, 0.05, (10, 4))
+    T2 = rng.normal(0, 0.05, (10, 10, 4, 4))
+    T2 = 0.5 * (T2 + T2.transpose(1, 0, 3, 2))
+    a = triples_loop(s.eps_h, s.eps_p, T1, T2, ints["PPHH"], ints["HHHP"], s.gamma)
+    b = triples_dense(s.eps_h, s.eps_p, T1, T2, ints["PPHH"], ints["HHHP"], s.gamma)
+    assert abs(a - b) < 1e-13 * max(1.0, abs(a))
+
+
+def test_permutation_table():
+    # Permutation<3>(p) images, Permutation.hpp:52-62
+    assert [permutation(p) for p in range(6)] == [
+        [0, 1, 2], [1, 0, 2], [1, 2, 0], [0, 2, 1], [2, 0, 1], [2, 1, 0]]
+
+
+@pytest.mark.parametrize("dist,ppl", [(0, 1), (1, 1), (0, 0)])
+def test_vertex_and_stored_vabcd_formulations_agree(dist, ppl):
+    s = make_system(5, 14, 40, seed=11)
+    ints = coulomb_integrals(s.gamma, 5, keys=("PPHH", "PHPH", "HHHH", "HHHP",
+                                               "PPPP", "PPPH"))
+    rng = np.random.default_rng(2)
+    T1 = rng.normal(0, 0.02, (14, 5))
+    T2 = rng.normal(0, 0.02, (14, 14, 5, 5))
+    T2 = 0.5 * (T2 + T2.transpose(1, 0, 3, 2))
+    a = residual(1, T1, T2, ints, s.gamma, distinguishable=dist, ppl=ppl)
+    if dist == 0 and ppl == 1:
+        b = residual_reference(1, T1, T2, ints)
+        assert np.abs(a[0] - b[0]).max() < 1e-14
+        assert np.abs(a[1] - b[1]).max() < 1e-14
+    else:
+        assert np.all(np.isfinite(a[1]))
+
+
+def test_ladder_slicing_is_invariant():
+    s = make_system(4, 13, 30, seed=4)
+    ints = coulomb_integrals(s.gamma, 4)
+    rng = np.random.default_rng(9)
+    T1 = rng.normal(0, 0.02, (13, 4))
+    T2 = rng.normal(0, 0.02, (13, 13, 4, 4))
+    T2 = 0.5 * (T2 + T2.transpose(1, 0, 3, 2))
+    ref = residual(1, T1, T2, ints, s.gamma, slice_size=13)
+    for sl in (1, 3, 4, 5, 7):
+        r = residual(1, T1, T2, ints, s.gamma, slice_size=sl)
+        assert np.abs(r[1] - ref[1]).max() < 1e-14
+
+
+def test_mp2_start_equals_closed_form():
+    s = make_system(4, 12, 30, seed=2)
+    ints = coulomb_integrals(s.gamma, 4)
+    r = ccsd(s.eps_h, s.eps_p, ints, s.gamma, max_iterations=1)
+    assert abs(r["history"][0]["energy"]["value"]
+               - mp2_energy(s.eps_h, s.eps_p, ints["PPHH"])) < 1e-13
+
+
+def test_diis_ring_buffer_order():
+    # weights are read for i = (next + N - j) % N, newest first
+    m = DiisMixer(3)
+    rng = np.random.default_rng(0)
+    vecs = [(rng.normal(size=(2, 1)), rng.normal(size=(2, 2, 1, 1)))
+            for _ in range(5)]
+    for v in vecs:
+        m.append(v, (v[0] * 0.1, v[1] * 0.1))
+    assert m.count == 3 and m.next_index == 2
+    assert len(m.last_weights) == 3
+    assert abs(sum(m.last_weights) - 1.0) < 1e-12
