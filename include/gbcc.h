@@ -59,6 +59,11 @@ uint64_t gbcc_ctx_kernel_launches(const gbcc_ctx *ctx);
 /* Analytic FP64-equivalent flops issued to the contraction engine so far. */
 double gbcc_ctx_flops(const gbcc_ctx *ctx);
 void *gbcc_ctx_stream(const gbcc_ctx *ctx);
+/* Precision-mode parameters of this context: bf16 digits per operand of the
+ * emulated GEMM (4..8, default 6) and the smallest GEMM (in flops) that is
+ * emulated; smaller ones run in FP64 (default 1e7). */
+gbcc_status gbcc_ctx_set_emulation(gbcc_ctx *ctx, int emu_slices,
+                                   double emu_min_flops);
 
 /* ------------------------------------------------------------- CCSD input */
 /* Replaces ClusterSinglesDoublesAlgorithm::run<double> +

@@ -60,6 +60,7 @@ _SIGS = {
     "gbcc_ctx_kernel_launches": (C.c_uint64, [C.c_void_p]),
     "gbcc_ctx_flops": (C.c_double, [C.c_void_p]),
     "gbcc_ctx_stream": (C.c_void_p, [C.c_void_p]),
+    "gbcc_ctx_set_emulation": (C.c_int, [C.c_void_p, C.c_int, C.c_double]),
     "gbcc_ccsd_opts_default": (None, [C.POINTER(CcsdOpts)]),
     "gbcc_ccsd_solve": (C.c_int, [C.c_void_p, C.POINTER(CcsdIn),
                                   C.POINTER(CcsdOpts), C.POINTER(CcsdOut)]),
@@ -152,6 +153,10 @@ class Context:
         if st not in allow:
             raise GbccError(st, self.lib.gbcc_last_error(self.h).decode())
         return st
+
+    def set_emulation(self, slices=6, min_flops=1e7):
+        self.check(self.lib.gbcc_ctx_set_emulation(self.h, int(slices),
+                                                   float(min_flops)))
 
     @property
     def launches(self):

@@ -143,6 +143,15 @@ void *gbcc_ctx_stream(const gbcc_ctx *ctx) {
   return ctx ? static_cast<void *>(ctx->c.stream) : nullptr;
 }
 
+gbcc_status gbcc_ctx_set_emulation(gbcc_ctx *ctx, int emu_slices,
+                                   double emu_min_flops) {
+  if (!ctx || emu_slices < 4 || emu_slices > 8 || emu_min_flops < 0)
+    return GBCC_BAD_ARG;
+  ctx->c.emu_slices = emu_slices;
+  ctx->c.emu_min_flops = emu_min_flops;
+  return GBCC_OK;
+}
+
 void gbcc_ccsd_opts_default(gbcc_ccsd_opts *o) {
   if (!o) return;
   o->mixer = 0;

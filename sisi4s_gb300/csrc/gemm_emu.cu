@@ -1,9 +1,542 @@
-// placeholder, replaced by the emulated FP64 GEMM
+// FP64 GEMM emulated on the tcgen05 bf16 tensor cores (sm_103a).
+//
+//   C = alpha op(A) op(B) + beta C       (column-major FP64 in and out)
+//
+// Numerics (Ozaki-style fixed-point splitting).  Each row i of op(A) is
+// scaled by 2^-ea_i (ea_i = exponent of the row's max |.|) and rounded to an
+// integer X with F = 7 S fractional bits, which is then written as S balanced
+// base-128 digits d_0 (|d_0| <= 128) ... d_{S-1} (|d| <= 64), so
+//   A_ik = 2^ea_i sum_s d_s(i,k) 2^-7(s+1)   (error <= 2^(ea_i - 7S - 1)).
+// Columns of op(B) likewise.  Digits are exact in bf16.  The product keeps the
+// pairs (s, t) with s + t < S and accumulates every "diagonal" g = s + t in its
+// own FP32 TMEM accumulator: digit products and their sums stay integers below
+// 2^24 over a K-chunk of 512 (256 for S > 6), so the FP32 sums are exact.
+// After each chunk the epilogue warps fold the diagonals into a per-output
+// int64 fixed-point total (29 fractional bits below the g = 0 unit), still
+// exact up to the rounding of diagonals g >= 5.  FP64 is touched once per
+// output at the very end: C = 2^(ea_i + eb_j - 14 - 29) * total.  No FP64
+// arithmetic runs inside the K loop (GB300's FP64 rate is ~1/1600 of its bf16
+// tensor rate, so even one FP64 op per output per chunk would dominate).
+//
+// Data movement.  A split kernel writes the digits of A (B) as pre-tiled
+// operand panels: tiles of 128 (64) rows x 32 k in the no-swizzle K-major
+// core-matrix layout (8 rows x 16 B per core matrix, k-groups fastest), one
+// contiguous 8 KB (4 KB) block per tile and digit.  The GEMM kernel moves a
+// k-block of all S digit tiles of A and B into shared memory with 1-D bulk
+// copies (cp.async.bulk, the TMA engine) through a multi-stage mbarrier
+// pipeline.  Warp roles: warp 0 producer, warp 1 MMA issuer (one thread,
+// tcgen05.mma kind::f16, M=128 N=64 K=16), warps 2-9 epilogue (tcgen05.ld).
+// Every wait is bounded; on timeout the kernel records an error code, drains
+// what it issued (bounded) and frees its TMEM.
+#include <algorithm>
+#include <vector>
+
+#include <cuda_bf16.h>
+
 #include "internal.hpp"
+
 namespace gbcc {
-void gemm_emu(Context &, bool, bool, int64_t, int64_t, int64_t, double,
-              const double *, int64_t, const double *, int64_t, double,
-              double *, int64_t, int64_t, int64_t, int64_t, int64_t) {
-  throw Error(GBCC_BAD_ARG, "GBCC_PREC_EMU is not available in this build");
+namespace {
+
+constexpr int TM = 128;        // rows of an A tile / CTA tile M
+constexpr int TN = 64;         // rows of a B tile / CTA tile N
+constexpr int KB = 32;         // k per tile
+constexpr int A_TILE = TM * KB * 2;  // bytes
+constexpr int B_TILE = TN * KB * 2;
+constexpr int FRAC = 29;       // fractional bits of the int64 total (g=0 units)
+constexpr int NUM_THREADS = 320;     // 10 warps
+constexpr int SMEM_BUDGET = 220 * 1024;
+constexpr long long WAIT_LIMIT = 1LL << 26;
+
+enum : int { ERR_NONE = 0, ERR_FULL = 1, ERR_EMPTY = 2, ERR_ACCF = 3,
+             ERR_ACCE = 4, ERR_DRAIN = 5 };
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// bounded wait: false on timeout
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  for (long long i = 0; i < WAIT_LIMIT; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
+               "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src,
+                                         uint32_t bytes, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes "
+      "[%0], [%1], %2, [%3];" ::"r"(dst),
+      "l"(src), "r"(bytes), "r"(bar)
+      : "memory");
+}
+
+// no-swizzle K-major shared-memory matrix descriptor (tcgen05 format):
+// [0,14) start>>4, [16,30) LBO>>4 (K-adjacent core matrices),
+// [32,46) SBO>>4 (M/N-adjacent core matrices), [46,48) version = 1,
+// [61,64) layout = 0 (no swizzle)
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo,
+                                              uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr >> 4) & 0x3FFF);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+  d |= (uint64_t)1 << 46;
+  return d;
+}
+
+// kind::f16 instruction descriptor: D = F32, A = B = BF16, both K-major
+__host__ __device__ constexpr uint32_t instr_desc(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) |
+         ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t dtmem, uint64_t a, uint64_t b,
+                                         uint32_t idesc, uint32_t accum) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(dtmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(accum));
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          bar)
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
+        "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]),
+        "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+struct EmuArgs {
+  const __nv_bfloat16 *A;  // [S][mt][kt] tiles
+  const __nv_bfloat16 *B;  // [S][nt][kt] tiles
+  const int *ea, *eb;      // row / column exponents
+  double *C;
+  int64_t M, N, ldc;
+  int mt, nt, kt;          // tile counts
+  int kc_blocks;           // k-blocks per exact chunk
+  double alpha, beta;
+  int *err;
+};
+
+template <int S>
+__global__ void __launch_bounds__(NUM_THREADS, 1) emu_gemm_kernel(EmuArgs a) {
+  constexpr int STAGE_BYTES = S * (A_TILE + B_TILE);
+  constexpr int STAGES = (SMEM_BUDGET / STAGE_BYTES) > 4 ? 4 : (SMEM_BUDGET / STAGE_BYTES);
+  static_assert(STAGES >= 2, "not enough shared memory for two stages");
+  constexpr uint32_t TMEM_COLS = (S * TN <= 256) ? 256 : 512;
+  static_assert(S * TN <= 512, "too many diagonals for TMEM");
+
+  extern __shared__ __align__(1024) uint8_t smem[];
+  __shared__ __align__(8) uint64_t bar_full[4], bar_empty[4], bar_accf, bar_acce,
+      bar_drain;
+  __shared__ uint32_t tmem_base_sh;
+  __shared__ volatile int abort_sh;
+
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const int tile_m = blockIdx.x, tile_n = blockIdx.y;
+  const int nchunks = (a.kt + a.kc_blocks - 1) / a.kc_blocks;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(smem_u32(&bar_full[s]), 1);
+      mbar_init(smem_u32(&bar_empty[s]), 1);
+    }
+    mbar_init(smem_u32(&bar_accf), 1);
+    mbar_init(smem_u32(&bar_acce), 256);
+    mbar_init(smem_u32(&bar_drain), 1);
+    abort_sh = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile(
+        "tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+            smem_u32(&tmem_base_sh)),
+        "r"(TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_base_sh;
+  const uint32_t smem_base = smem_u32(smem);
+
+  if (warp == 0) {
+    // ------------------------------------------------------------ producer
+    if (lane == 0) {
+      const size_t a_slice = (size_t)a.mt * a.kt * (A_TILE / 2);
+      const size_t b_slice = (size_t)a.nt * a.kt * (B_TILE / 2);
+      int issued = 0;
+      for (int kb = 0; kb < a.kt; ++kb) {
+        const int st = kb % STAGES;
+        if (kb >= STAGES &&
+            !mbar_wait(smem_u32(&bar_empty[st]), ((kb / STAGES) - 1) & 1)) {
+          atomicCAS(a.err, 0, ERR_EMPTY);
+          abort_sh = 1;
+          break;
+        }
+        if (abort_sh) break;
+        const uint32_t full = smem_u32(&bar_full[st]);
+        mbar_expect_tx(full, STAGE_BYTES);
+        const uint32_t sbase = smem_base + st * STAGE_BYTES;
+        for (int s = 0; s < S; ++s) {
+          const __nv_bfloat16 *ga =
+              a.A + s * a_slice + ((size_t)tile_m * a.kt + kb) * (A_TILE / 2);
+          bulk_g2s(sbase + s * A_TILE, ga, A_TILE, full);
+        }
+        for (int s = 0; s < S; ++s) {
+          const __nv_bfloat16 *gb =
+              a.B + s * b_slice + ((size_t)tile_n * a.kt + kb) * (B_TILE / 2);
+          bulk_g2s(sbase + S * A_TILE + s * B_TILE, gb, B_TILE, full);
+        }
+        issued = kb + 1;
+      }
+      // never leave a bulk copy in flight: wait (bounded) for the last
+      // STAGES issued k-blocks to land
+      for (int kb = issued > STAGES ? issued - STAGES : 0; kb < issued; ++kb)
+        mbar_wait(smem_u32(&bar_full[kb % STAGES]), (kb / STAGES) & 1);
+    }
+  } else if (warp == 1) {
+    // ------------------------------------------------------------ MMA issuer
+    if (lane == 0) {
+      constexpr uint32_t idesc = instr_desc(TM, TN);
+      int kb = 0;
+      bool ok = true;
+      for (int c = 0; c < nchunks && ok; ++c) {
+        if (c > 0 && !mbar_wait(smem_u32(&bar_acce), (c - 1) & 1)) {
+          atomicCAS(a.err, 0, ERR_ACCE);
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        const int kend = min(a.kt, (c + 1) * a.kc_blocks);
+        uint32_t started = 0;  // bit g: diagonal g initialised in this chunk
+        for (; kb < kend; ++kb) {
+          const int st = kb % STAGES;
+          if (!mbar_wait(smem_u32(&bar_full[st]), (kb / STAGES) & 1)) {
+            atomicCAS(a.err, 0, ERR_FULL);
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t sbase = smem_base + st * STAGE_BYTES;
+#pragma unroll
+          for (int k16 = 0; k16 < KB / 16; ++k16) {
+#pragma unroll
+            for (int s = 0; s < S; ++s) {
+              const uint64_t da = smem_desc(sbase + s * A_TILE + k16 * 256, 128,
+                                            (KB / 8) * 128);
+#pragma unroll
+              for (int t = 0; t + s < S; ++t) {
+                const int g = s + t;
+                const uint64_t db =
+                    smem_desc(sbase + S * A_TILE + t * B_TILE + k16 * 256, 128,
+                              (KB / 8) * 128);
+                const uint32_t acc = (started >> g) & 1u;
+                mma_bf16(tmem + g * TN, da, db, idesc, acc);
+                started |= 1u << g;
+              }
+            }
+          }
+          mma_commit(smem_u32(&bar_empty[st]));
+        }
+        if (!ok) break;
+        mma_commit(smem_u32(&bar_accf));
+      }
+      // make sure every issued MMA finished before TMEM is released
+      mma_commit(smem_u32(&bar_drain));
+      if (!mbar_wait(smem_u32(&bar_drain), 0)) atomicCAS(a.err, 0, ERR_DRAIN);
+      if (!ok) abort_sh = 1;
+    }
+  } else {
+    // ------------------------------------------------------------ epilogue
+    const int ew = warp - 2;             // 0..7
+    const int quarter = warp & 3;        // TMEM lane quarter this warp may access
+    const int half = ew >> 2;            // column half
+    const int row = quarter * 32 + lane; // row within the tile
+    const uint32_t lane_addr = tmem + ((uint32_t)(quarter * 32) << 16);
+    long long tot[32];
+#pragma unroll
+    for (int j = 0; j < 32; ++j) tot[j] = 0;
+    for (int c = 0; c < nchunks; ++c) {
+      if (!mbar_wait(smem_u32(&bar_accf), c & 1)) {
+        atomicCAS(a.err, 0, ERR_ACCF);
+        break;
+      }
+      if (abort_sh) break;
+      tc_fence_after();
+#pragma unroll
+      for (int g = 0; g < S; ++g) {
+        const int sh = FRAC - 7 * g;
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+          float v[16];
+          tmem_ld16(lane_addr + g * TN + half * 32 + q * 16, v);
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const long long x = (long long)__float2ll_rn(v[j]);
+            long long y;
+            if (sh >= 0) y = x << sh;
+            else y = (x + (1LL << (-sh - 1))) >> (-sh);
+            tot[q * 16 + j] += y;
+          }
+        }
+      }
+      tc_fence_before();
+      mbar_arrive(smem_u32(&bar_acce));
+    }
+    // write out: C[m + n ldc], m = tile_m*128 + row, n = tile_n*64 + half*32 + j
+    const int64_t m = (int64_t)tile_m * TM + row;
+    if (m < a.M && !abort_sh) {
+      const int ea = a.ea[m];
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        const int64_t n = (int64_t)tile_n * TN + half * 32 + j;
+        if (n >= a.N) continue;
+        const int e = ea + a.eb[n] - 14 - FRAC;
+        double v = ldexp((double)tot[j], e) * a.alpha;
+        double *cp = a.C + m + n * a.ldc;
+        if (a.beta != 0.0) v = fma(a.beta, *cp, v);
+        *cp = v;
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(TMEM_COLS));
+  }
+}
+
+// ---------------------------------------------------------------- splitting
+// exponent e with max|x| < 2^e over one row (rows of op(A) / columns of op(B)).
+// Element (r, k) of the operand lives at base[r*rs + k*ks].
+__global__ void row_exponent_kernel(const double *__restrict__ base, int64_t R,
+                                    int64_t K, int64_t rs, int64_t ks,
+                                    int *__restrict__ e) {
+  // one warp per row
+  const int64_t r = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+  if (r >= R) return;
+  double m = 0.0;
+  for (int64_t k = threadIdx.x % 32; k < K; k += 32) m = fmax(m, fabs(base[r * rs + k * ks]));
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if (threadIdx.x % 32 == 0) {
+    int ex = 0;
+    if (m > 0.0) frexp(m, &ex);
+    e[r] = ex;
+  }
+}
+
+// same, one thread per row, for operands whose row index is contiguous (rs == 1)
+__global__ void row_exponent_cols_kernel(const double *__restrict__ base, int64_t R,
+                                         int64_t K, int64_t ks, int *__restrict__ e) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= R) return;
+  double m = 0.0;
+  for (int64_t k = 0; k < K; ++k) m = fmax(m, fabs(base[r + k * ks]));
+  int ex = 0;
+  if (m > 0.0) frexp(m, &ex);
+  e[r] = ex;
+}
+
+// fixed-point integer X = round(x 2^(F - e)) from the IEEE bits (integer ops)
+__device__ __forceinline__ long long to_fixed(double x, int e, int F) {
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+  const int ex = (int)((bits >> 52) & 0x7FF);
+  if (ex == 0) return 0;  // zero or subnormal (below any scale used here)
+  const long long mant = (long long)((bits & ((1ULL << 52) - 1)) | (1ULL << 52));
+  const int sh = ex - 1075 + F - e;  // x = mant 2^(ex-1075)
+  long long X;
+  if (sh >= 0) X = mant << sh;       // sh <= 10 since |x| < 2^e
+  else if (sh <= -63) X = 0;
+  else X = (mant + (1LL << (-sh - 1))) >> (-sh);
+  return (bits >> 63) ? -X : X;
+}
+
+// digits of one operand into tiles [S][rt][kt] of TR rows x 32 k.
+// One thread writes one 16-byte core-matrix row (8 consecutive k) per digit.
+template <int S, int TR>
+__global__ void split_kernel(const double *__restrict__ base, int64_t R,
+                             int64_t K, int64_t rs, int64_t ks,
+                             const int *__restrict__ e, int rt, int kt,
+                             __nv_bfloat16 *__restrict__ out) {
+  const int64_t segs = (int64_t)rt * TR * kt * (KB / 8);  // 16-byte segments per digit
+  const int64_t tile_elems = (int64_t)TR * KB;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < segs;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    // idx -> (row r in [0, rt*TR), k-group kg in [0, kt*4)) with r fastest
+    const int64_t r = idx % ((int64_t)rt * TR);
+    const int64_t kg = idx / ((int64_t)rt * TR);
+    const int64_t tr = r / TR, rr = r % TR;
+    const int64_t tk = kg / (KB / 8), kk = kg % (KB / 8);
+    // destination offset (elements) inside the digit plane
+    const int64_t off = (tr * kt + tk) * tile_elems +
+                        ((rr / 8) * (KB / 8) + kk) * 64 + (rr % 8) * 8;
+    long long d[S][8];
+    const int er = (r < R) ? e[r] : 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int64_t k = kg * 8 + j;
+      long long X = 0;
+      if (r < R && k < K) X = to_fixed(base[r * rs + k * ks], er, 7 * S);
+#pragma unroll
+      for (int s = S - 1; s >= 1; --s) {
+        const long long q = ((X + 64) & 127) - 64;
+        d[s][j] = q;
+        X = (X - q) >> 7;
+      }
+      d[0][j] = X;
+    }
+    const int64_t plane = (int64_t)rt * kt * tile_elems;
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+      __align__(16) __nv_bfloat16 v[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) v[j] = __float2bfloat16_rn((float)d[s][j]);
+      *reinterpret_cast<uint4 *>(out + s * plane + off) =
+          *reinterpret_cast<const uint4 *>(v);
+    }
+  }
+}
+
+template <int S>
+void run_emu(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
+             double alpha, const double *A, int64_t lda, const double *B,
+             int64_t ldb, double beta, double *C, int64_t ldc) {
+  const int mt = (int)((M + TM - 1) / TM);
+  const int nt = (int)((N + TN - 1) / TN);
+  const int kt = (int)((K + KB - 1) / KB);
+  require((int64_t)mt * nt < (1LL << 31) && nt <= 65535, "emu gemm: grid too large");
+  // strides of op(A)(m,k) and op(B)^T(n,k)
+  const int64_t ars = ta ? lda : 1, aks = ta ? 1 : lda;
+  const int64_t brs = tb ? 1 : ldb, bks = tb ? ldb : 1;
+  DBuf ea(ctx, sizeof(int) * M), eb(ctx, sizeof(int) * N);
+  DBuf asl(ctx, (size_t)S * mt * kt * A_TILE), bsl(ctx, (size_t)S * nt * kt * B_TILE);
+  DBuf err(ctx, sizeof(int));
+  GBCC_CUDA(cudaMemsetAsync(err.as<int>(), 0, sizeof(int), ctx.stream));
+  auto exponents = [&](const double *p, int64_t R, int64_t rs, int64_t ks, int *e) {
+    if (rs == 1 && R >= 4096)
+      row_exponent_cols_kernel<<<(unsigned)((R + 127) / 128), 128, 0, ctx.stream>>>(
+          p, R, K, ks, e);
+    else
+      row_exponent_kernel<<<(unsigned)((R + 7) / 8), 256, 0, ctx.stream>>>(p, R, K, rs,
+                                                                         ks, e);
+    GBCC_CHECK_LAUNCH(ctx);
+  };
+  exponents(A, M, ars, aks, ea.as<int>());
+  exponents(B, N, brs, bks, eb.as<int>());
+  auto grid_for = [&](int64_t segs) {
+    int64_t g = (segs + 255) / 256;
+    const int64_t cap = (int64_t)std::max(ctx.sm_count, 1) * 16;
+    return (unsigned)std::max<int64_t>(1, std::min(g, cap));
+  };
+  split_kernel<S, TM><<<grid_for((int64_t)mt * TM * kt * 4), 256, 0, ctx.stream>>>(
+      A, M, K, ars, aks, ea.as<int>(), mt, kt, asl.as<__nv_bfloat16>());
+  GBCC_CHECK_LAUNCH(ctx);
+  split_kernel<S, TN><<<grid_for((int64_t)nt * TN * kt * 4), 256, 0, ctx.stream>>>(
+      B, N, K, brs, bks, eb.as<int>(), nt, kt, bsl.as<__nv_bfloat16>());
+  GBCC_CHECK_LAUNCH(ctx);
+  constexpr int STAGE_BYTES = S * (A_TILE + B_TILE);
+  constexpr int STAGES = (SMEM_BUDGET / STAGE_BYTES) > 4 ? 4 : (SMEM_BUDGET / STAGE_BYTES);
+  const int smem = STAGES * STAGE_BYTES;
+  static bool attr_set = false;
+  if (!attr_set) {
+    GBCC_CUDA(cudaFuncSetAttribute(emu_gemm_kernel<S>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    attr_set = true;
+  }
+  EmuArgs args{};
+  args.A = asl.as<__nv_bfloat16>();
+  args.B = bsl.as<__nv_bfloat16>();
+  args.ea = ea.as<int>();
+  args.eb = eb.as<int>();
+  args.C = C;
+  args.M = M; args.N = N; args.ldc = ldc;
+  args.mt = mt; args.nt = nt; args.kt = kt;
+  args.kc_blocks = (S <= 6 ? 512 : 256) / KB;
+  args.alpha = alpha;
+  args.beta = beta;
+  args.err = err.as<int>();
+  emu_gemm_kernel<S><<<dim3(mt, nt), NUM_THREADS, smem, ctx.stream>>>(args);
+  GBCC_CHECK_LAUNCH(ctx);
+  int h = 0;
+  GBCC_CUDA(cudaMemcpyAsync(&h, err.as<int>(), sizeof(int), cudaMemcpyDeviceToHost,
+                            ctx.stream));
+  GBCC_CUDA(cudaStreamSynchronize(ctx.stream));
+  if (h != ERR_NONE)
+    throw Error(GBCC_TIMEOUT, "emulated GEMM: a bounded device wait gave up (code " +
+                                  std::to_string(h) + ")");
+}
+
+}  // namespace
+
+void gemm_emu(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
+              double alpha, const double *A, int64_t lda, const double *B,
+              int64_t ldb, double beta, double *C, int64_t ldc, int64_t batch,
+              int64_t sA, int64_t sB, int64_t sC) {
+  for (int64_t z = 0; z < batch; ++z) {
+    const double *Az = A + z * sA;
+    const double *Bz = B + z * sB;
+    double *Cz = C + z * sC;
+    switch (ctx.emu_slices) {
+      case 4: run_emu<4>(ctx, ta, tb, M, N, K, alpha, Az, lda, Bz, ldb, beta, Cz, ldc); break;
+      case 5: run_emu<5>(ctx, ta, tb, M, N, K, alpha, Az, lda, Bz, ldb, beta, Cz, ldc); break;
+      case 6: run_emu<6>(ctx, ta, tb, M, N, K, alpha, Az, lda, Bz, ldb, beta, Cz, ldc); break;
+      case 7: run_emu<7>(ctx, ta, tb, M, N, K, alpha, Az, lda, Bz, ldb, beta, Cz, ldc); break;
+      case 8: run_emu<8>(ctx, ta, tb, M, N, K, alpha, Az, lda, Bz, ldb, beta, Cz, ldc); break;
+      default: throw Error(GBCC_BAD_ARG, "emu_slices must be in [4, 8]");
+    }
+    ctx.flops += 2.0 * (double)M * (double)N * (double)K;
+  }
+}
+
 }  // namespace gbcc

@@ -53,7 +53,7 @@ struct Context {
   double flops = 0.0;     // FP64-equivalent flops issued to GEMMs
   int sm_count = 0;
   // emulated-GEMM configuration
-  int emu_slices = 7;
+  int emu_slices = 6;
   // GEMMs smaller than this many flops stay in FP64 in precision mode
   double emu_min_flops = 1e7;
 };
