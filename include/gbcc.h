@@ -65,6 +65,15 @@ void *gbcc_ctx_stream(const gbcc_ctx *ctx);
 gbcc_status gbcc_ctx_set_emulation(gbcc_ctx *ctx, int emu_slices,
                                    double emu_min_flops);
 
+/* Timing of the tensor-core GEMM kernel: enable (1) / disable (0) CUDA-event
+ * records around each of its launches on the context stream; stats returns
+ * the accumulated device milliseconds, the launches, the bf16 tensor flops of
+ * the emulation scheme (S(S+1)/2 products of 2MNK) and the FP64-equivalent
+ * flops (2MNK), and resets the counters. */
+gbcc_status gbcc_ctx_profile(gbcc_ctx *ctx, int enable);
+gbcc_status gbcc_ctx_gemm_stats(gbcc_ctx *ctx, double *ms, int64_t *launches,
+                                double *tc_flops, double *fp64_flops);
+
 /* ------------------------------------------------------------- CCSD input */
 /* Replaces ClusterSinglesDoublesAlgorithm::run<double> +
  * CcsdEnergyFromCoulombIntegrals::getResiduum (real path)

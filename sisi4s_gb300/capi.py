@@ -61,6 +61,9 @@ _SIGS = {
     "gbcc_ctx_flops": (C.c_double, [C.c_void_p]),
     "gbcc_ctx_stream": (C.c_void_p, [C.c_void_p]),
     "gbcc_ctx_set_emulation": (C.c_int, [C.c_void_p, C.c_int, C.c_double]),
+    "gbcc_ctx_profile": (C.c_int, [C.c_void_p, C.c_int]),
+    "gbcc_ctx_gemm_stats": (C.c_int, [C.c_void_p, _dp, C.POINTER(C.c_int64),
+                                      _dp, _dp]),
     "gbcc_ccsd_opts_default": (None, [C.POINTER(CcsdOpts)]),
     "gbcc_ccsd_solve": (C.c_int, [C.c_void_p, C.POINTER(CcsdIn),
                                   C.POINTER(CcsdOpts), C.POINTER(CcsdOut)]),
@@ -157,6 +160,17 @@ class Context:
     def set_emulation(self, slices=6, min_flops=1e7):
         self.check(self.lib.gbcc_ctx_set_emulation(self.h, int(slices),
                                                    float(min_flops)))
+
+    def profile(self, enable=True):
+        self.check(self.lib.gbcc_ctx_profile(self.h, 1 if enable else 0))
+
+    def gemm_stats(self):
+        ms, n = C.c_double(), C.c_int64()
+        tc, f64 = C.c_double(), C.c_double()
+        self.check(self.lib.gbcc_ctx_gemm_stats(self.h, C.byref(ms), C.byref(n),
+                                                C.byref(tc), C.byref(f64)))
+        return {"ms": ms.value, "launches": n.value, "tc_flops": tc.value,
+                "fp64_flops": f64.value}
 
     @property
     def launches(self):

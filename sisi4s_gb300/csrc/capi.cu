@@ -125,6 +125,8 @@ void gbcc_ctx_destroy(gbcc_ctx *ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->c.device);
   cudaStreamSynchronize(ctx->c.stream);
+  ctx->c.prof_harvest();
+  for (auto e : ctx->c.prof_pool) cudaEventDestroy(e);
   if (ctx->c.own_stream) cudaStreamDestroy(ctx->c.stream);
   delete ctx;
 }
@@ -150,6 +152,27 @@ gbcc_status gbcc_ctx_set_emulation(gbcc_ctx *ctx, int emu_slices,
   ctx->c.emu_slices = emu_slices;
   ctx->c.emu_min_flops = emu_min_flops;
   return GBCC_OK;
+}
+
+gbcc_status gbcc_ctx_profile(gbcc_ctx *ctx, int enable) {
+  if (!ctx) return GBCC_BAD_ARG;
+  ctx->c.prof = enable != 0;
+  return GBCC_OK;
+}
+
+gbcc_status gbcc_ctx_gemm_stats(gbcc_ctx *ctx, double *ms, int64_t *launches,
+                                double *tc_flops, double *fp64_flops) {
+  if (!ctx) return GBCC_BAD_ARG;
+  return guard(ctx, [&]() {
+    ctx->c.prof_harvest();
+    if (ms) *ms = ctx->c.prof_ms;
+    if (launches) *launches = ctx->c.prof_launches;
+    if (tc_flops) *tc_flops = ctx->c.prof_tc_flops;
+    if (fp64_flops) *fp64_flops = ctx->c.prof_fp64_flops;
+    ctx->c.prof_ms = ctx->c.prof_tc_flops = ctx->c.prof_fp64_flops = 0;
+    ctx->c.prof_launches = 0;
+    return GBCC_OK;
+  });
 }
 
 void gbcc_ccsd_opts_default(gbcc_ccsd_opts *o) {

@@ -506,8 +506,21 @@ void run_emu(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
   args.alpha = alpha;
   args.beta = beta;
   args.err = err.as<int>();
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  if (ctx.prof) {
+    ev0 = ctx.prof_event();
+    ev1 = ctx.prof_event();
+    GBCC_CUDA(cudaEventRecord(ev0, ctx.stream));
+  }
   emu_gemm_kernel<S><<<dim3(mt, nt), NUM_THREADS, smem, ctx.stream>>>(args);
   GBCC_CHECK_LAUNCH(ctx);
+  if (ctx.prof) {
+    GBCC_CUDA(cudaEventRecord(ev1, ctx.stream));
+    // algorithmic tensor-core work of the scheme: S(S+1)/2 bf16 products of
+    // the unpadded M x N x K problem
+    const double f = 2.0 * (double)M * (double)N * (double)K;
+    ctx.prof_recs.push_back({ev0, ev1, f * S * (S + 1) / 2.0, f});
+  }
   int h = 0;
   GBCC_CUDA(cudaMemcpyAsync(&h, err.as<int>(), sizeof(int), cudaMemcpyDeviceToHost,
                             ctx.stream));

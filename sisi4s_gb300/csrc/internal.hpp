@@ -56,6 +56,41 @@ struct Context {
   int emu_slices = 6;
   // GEMMs smaller than this many flops stay in FP64 in precision mode
   double emu_min_flops = 1e7;
+  // optional per-launch timing of the tensor-core GEMM kernel (CUDA events
+  // recorded on the context stream around each launch)
+  bool prof = false;
+  struct ProfRec {
+    cudaEvent_t a, b;
+    double tc_flops, fp64_flops;
+  };
+  std::vector<ProfRec> prof_recs;
+  std::vector<cudaEvent_t> prof_pool;
+  double prof_ms = 0, prof_tc_flops = 0, prof_fp64_flops = 0;
+  int64_t prof_launches = 0;
+  cudaEvent_t prof_event() {
+    if (!prof_pool.empty()) {
+      cudaEvent_t e = prof_pool.back();
+      prof_pool.pop_back();
+      return e;
+    }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+  }
+  void prof_harvest() {
+    for (auto &r : prof_recs) {
+      cudaEventSynchronize(r.b);
+      float ms = 0;
+      cudaEventElapsedTime(&ms, r.a, r.b);
+      prof_ms += ms;
+      prof_tc_flops += r.tc_flops;
+      prof_fp64_flops += r.fp64_flops;
+      prof_launches++;
+      prof_pool.push_back(r.a);
+      prof_pool.push_back(r.b);
+    }
+    prof_recs.clear();
+  }
 };
 
 // Stream-ordered device buffer (cudaMallocAsync on the context stream).

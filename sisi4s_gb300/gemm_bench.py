@@ -1,0 +1,61 @@
+"""Throughput of the library's GEMMs (FP64 and emulated FP64) on one GPU.
+
+  python -m sisi4s_gb300.gemm_bench M N K [--prec emu|fp64] [--slices S] [--reps R]
+
+Operands are random FP64 device buffers (column-major); timing uses CUDA
+events on the library stream after one warm-up launch.
+"""
+import argparse
+import json
+
+import numpy as np
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("M", type=int)
+    ap.add_argument("N", type=int)
+    ap.add_argument("K", type=int)
+    ap.add_argument("--prec", default="emu", choices=["emu", "fp64"])
+    ap.add_argument("--slices", type=int, default=6)
+    ap.add_argument("--reps", type=int, default=3)
+    args = ap.parse_args()
+    import torch
+    from . import capi
+    ctx = capi.Context(0)
+    ctx.set_emulation(args.slices, 0.0)
+    M, N, K = args.M, args.N, args.K
+    a = torch.randn(M * K, dtype=torch.float64, device="cuda")
+    b = torch.randn(K * N, dtype=torch.float64, device="cuda")
+    c = torch.zeros(M * N, dtype=torch.float64, device="cuda")
+    prec = capi.PREC_EMU if args.prec == "emu" else capi.PREC_FP64
+    torch.cuda.synchronize()
+
+    def run():
+        ctx.check(ctx.lib.gbcc_dgemm(ctx.h, 0, 0, M, N, K, 1.0, a.data_ptr(), M,
+                                     b.data_ptr(), K, 0.0, c.data_ptr(), M, prec))
+    run()
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    torch.cuda.synchronize()
+    ctx.profile(True)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.reps):
+        run()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.reps
+    st = ctx.gemm_stats()
+    out = {"M": M, "N": N, "K": K, "prec": args.prec, "slices": args.slices,
+           "ms_per_gemm": ms, "fp64_equiv_tflops": 2.0 * M * N * K / ms / 1e9}
+    if st["launches"]:
+        out["tensor_kernel_ms"] = st["ms"] / st["launches"]
+        out["tensor_kernel_bf16_tflops"] = st["tc_flops"] / st["ms"] / 1e9
+    print(json.dumps(out))
+    ctx.close()
+    del np
+
+
+if __name__ == "__main__":
+    main()

@@ -55,3 +55,16 @@ def column_major(a):
     of CTF dense storage and of the cc4s ``.elements`` files."""
     return np.ascontiguousarray(np.asarray(a, dtype=np.float64).transpose(
         tuple(range(a.ndim - 1, -1, -1)))).ravel()
+
+
+def mp2_amplitudes(system):
+    """MP2 amplitudes T2 = -V_abij / D_abij (T1 = 0) in the reference's index
+    order: the amplitudes the MP2-start iteration produces, used as given
+    starting amplitudes.  V_abij = sum_G Gamma_Gai Gamma_Gbj."""
+    No = system.No
+    gai = system.gamma[:, No:, :No]
+    v = np.einsum("Gai,Gbj->abij", gai, gai, optimize=True)
+    ep, eh = system.eps_p, system.eps_h
+    d = (((ep[:, None, None, None] - eh[None, None, :, None]) + ep[None, :, None, None])
+         - eh[None, None, None, :])
+    return np.zeros((system.Nv, No)), -v / d
