@@ -25,10 +25,13 @@
 // k-block of all S digit tiles of A and B into shared memory with 1-D bulk
 // copies (cp.async.bulk, the TMA engine) through a multi-stage mbarrier
 // pipeline.  Warp roles: warp 0 producer, warp 1 MMA issuer (one thread,
-// tcgen05.mma kind::f16, M=128 N=64 K=16), warps 2-9 epilogue (tcgen05.ld).
+// tcgen05.mma kind::f16, M=128, K=16, N up to 256: the B digits that pair
+// with one A digit are stacked along N), warps 2-9 epilogue (tcgen05.ld).
 // Every wait is bounded; on timeout the kernel records an error code, drains
 // what it issued (bounded) and frees its TMEM.
 #include <algorithm>
+#include <climits>
+#include <string>
 #include <vector>
 
 #include <cuda_bf16.h>
@@ -47,6 +50,10 @@ constexpr int FRAC = 29;       // fractional bits of the int64 total (g=0 units)
 constexpr int NUM_THREADS = 320;     // 10 warps
 constexpr int SMEM_BUDGET = 220 * 1024;
 constexpr long long WAIT_LIMIT = 1LL << 26;
+constexpr int GROUP_M = 16;    // m-tiles per rasterization group
+// exponents start at a large negative sentinel (all-zero rows keep it); any
+// value below EXP_FLOOR means "row is zero"
+constexpr int EXP_FLOOR = -1100;
 
 enum : int { ERR_NONE = 0, ERR_FULL = 1, ERR_EMPTY = 2, ERR_ACCF = 3,
              ERR_ACCE = 4, ERR_DRAIN = 5 };
@@ -181,7 +188,19 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) emu_gemm_kernel(EmuArgs a) {
   __shared__ volatile int abort_sh;
 
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-  const int tile_m = blockIdx.x, tile_n = blockIdx.y;
+  // grouped rasterization: consecutive CTAs walk GROUP_M m-tiles down one
+  // column of n-tiles, so that a wave of CTAs shares a compact set of A and B
+  // panels in L2
+  int tile_m, tile_n;
+  {
+    const int64_t t = blockIdx.x;
+    const int64_t gsz = (int64_t)GROUP_M * a.nt;
+    const int64_t g = t / gsz, r = t % gsz;
+    const int first = (int)(g * GROUP_M);
+    const int gm = min(GROUP_M, a.mt - first);
+    tile_m = first + (int)(r % gm);
+    tile_n = (int)(r / gm);
+  }
   const int nchunks = (a.kt + a.kc_blocks - 1) / a.kc_blocks;
 
   if (threadIdx.x == 0) {
@@ -246,7 +265,6 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) emu_gemm_kernel(EmuArgs a) {
   } else if (warp == 1) {
     // ------------------------------------------------------------ MMA issuer
     if (lane == 0) {
-      constexpr uint32_t idesc = instr_desc(TM, TN);
       int kb = 0;
       bool ok = true;
       for (int c = 0; c < nchunks && ok; ++c) {
@@ -257,7 +275,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) emu_gemm_kernel(EmuArgs a) {
         }
         tc_fence_after();
         const int kend = min(a.kt, (c + 1) * a.kc_blocks);
-        uint32_t started = 0;  // bit g: diagonal g initialised in this chunk
+        const int kfirst = kb;
         for (; kb < kend; ++kb) {
           const int st = kb % STAGES;
           if (!mbar_wait(smem_u32(&bar_full[st]), (kb / STAGES) & 1)) {
@@ -267,21 +285,26 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) emu_gemm_kernel(EmuArgs a) {
           }
           tc_fence_after();
           const uint32_t sbase = smem_base + st * STAGE_BYTES;
+          // Pairs (s, t) go to diagonal g = s + t at TMEM columns g*TN, so
+          // all pairs of one A digit s write the contiguous column range
+          // [s*TN, S*TN): one MMA per s (split at N = 256) whose B operand is
+          // the B digit tiles t = 0..S-1-s stacked along N (consecutive 4 KB
+          // tiles keep the 512 B row-group stride).  The first MMA of a chunk
+          // (s = 0, k16 = 0) overwrites every diagonal.
 #pragma unroll
           for (int k16 = 0; k16 < KB / 16; ++k16) {
 #pragma unroll
             for (int s = 0; s < S; ++s) {
               const uint64_t da = smem_desc(sbase + s * A_TILE + k16 * 256, 128,
                                             (KB / 8) * 128);
+              const uint32_t acc = (kb == kfirst && k16 == 0 && s == 0) ? 0u : 1u;
 #pragma unroll
-              for (int t = 0; t + s < S; ++t) {
-                const int g = s + t;
+              for (int off = 0; off < (S - s) * TN; off += 256) {
+                const int n = min(256, (S - s) * TN - off);
                 const uint64_t db =
-                    smem_desc(sbase + S * A_TILE + t * B_TILE + k16 * 256, 128,
-                              (KB / 8) * 128);
-                const uint32_t acc = (started >> g) & 1u;
-                mma_bf16(tmem + g * TN, da, db, idesc, acc);
-                started |= 1u << g;
+                    smem_desc(sbase + S * A_TILE + (off / TN) * B_TILE + k16 * 256,
+                              128, (KB / 8) * 128);
+                mma_bf16(tmem + s * TN + off, da, db, instr_desc(TM, n), acc);
               }
             }
           }
@@ -321,7 +344,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) emu_gemm_kernel(EmuArgs a) {
           tmem_ld16(lane_addr + g * TN + half * 32 + q * 16, v);
 #pragma unroll
           for (int j = 0; j < 16; ++j) {
-            const long long x = (long long)__float2ll_rn(v[j]);
+            const long long x = (long long)__float2int_rn(v[j]);  // exact, |v| <= 2^24
             long long y;
             if (sh >= 0) y = x << sh;
             else y = (x + (1LL << (-sh - 1))) >> (-sh);
@@ -335,12 +358,12 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) emu_gemm_kernel(EmuArgs a) {
     // write out: C[m + n ldc], m = tile_m*128 + row, n = tile_n*64 + half*32 + j
     const int64_t m = (int64_t)tile_m * TM + row;
     if (m < a.M && !abort_sh) {
-      const int ea = a.ea[m];
+      const int ea = max(a.ea[m], EXP_FLOOR);
 #pragma unroll
       for (int j = 0; j < 32; ++j) {
         const int64_t n = (int64_t)tile_n * TN + half * 32 + j;
         if (n >= a.N) continue;
-        const int e = ea + a.eb[n] - 14 - FRAC;
+        const int e = ea + max(a.eb[n], EXP_FLOOR) - 14 - FRAC;
         double v = ldexp((double)tot[j], e) * a.alpha;
         double *cp = a.C + m + n * a.ldc;
         if (a.beta != 0.0) v = fma(a.beta, *cp, v);
@@ -360,32 +383,44 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) emu_gemm_kernel(EmuArgs a) {
 // ---------------------------------------------------------------- splitting
 // exponent e with max|x| < 2^e over one row (rows of op(A) / columns of op(B)).
 // Element (r, k) of the operand lives at base[r*rs + k*ks].
-__global__ void row_exponent_kernel(const double *__restrict__ base, int64_t R,
-                                    int64_t K, int64_t rs, int64_t ks,
-                                    int *__restrict__ e) {
-  // one warp per row
-  const int64_t r = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
-  if (r >= R) return;
-  double m = 0.0;
-  for (int64_t k = threadIdx.x % 32; k < K; k += 32) m = fmax(m, fabs(base[r * rs + k * ks]));
-  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if (threadIdx.x % 32 == 0) {
-    int ex = 0;
-    if (m > 0.0) frexp(m, &ex);
-    e[r] = ex;
-  }
+// The row exponent is the largest frexp exponent over the row, so it is a
+// max of integers read from the IEEE exponent field: blocks over (rows,
+// K-chunks) combine with atomicMax, which is order-independent and therefore
+// deterministic.  e[] starts at a large negative sentinel (memset 0x80);
+// all-zero rows keep it.
+__device__ __forceinline__ int frexp_exponent(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int E = (int)((b >> 52) & 0x7FF);
+  return E == 0 ? INT_MIN : E - 1022;  // zero / subnormal: no contribution
 }
 
-// same, one thread per row, for operands whose row index is contiguous (rs == 1)
-__global__ void row_exponent_cols_kernel(const double *__restrict__ base, int64_t R,
-                                         int64_t K, int64_t ks, int *__restrict__ e) {
+// row index contiguous (rs == 1): one thread per row, one K-chunk per blockIdx.y
+__global__ void exponent_rows_contig_kernel(const double *__restrict__ base,
+                                            int64_t R, int64_t K, int64_t ks,
+                                            int64_t kchunk, int *__restrict__ e) {
   const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= R) return;
-  double m = 0.0;
-  for (int64_t k = 0; k < K; ++k) m = fmax(m, fabs(base[r + k * ks]));
-  int ex = 0;
-  if (m > 0.0) frexp(m, &ex);
-  e[r] = ex;
+  const int64_t k0 = (int64_t)blockIdx.y * kchunk;
+  const int64_t k1 = min(K, k0 + kchunk);
+  int m = INT_MIN;
+  for (int64_t k = k0; k < k1; ++k) m = max(m, frexp_exponent(base[r + k * ks]));
+  if (m != INT_MIN) atomicMax(&e[r], m);
+}
+
+// any strides: one warp per row, one K-chunk per blockIdx.y
+__global__ void exponent_rows_warp_kernel(const double *__restrict__ base,
+                                          int64_t R, int64_t K, int64_t rs,
+                                          int64_t ks, int64_t kchunk,
+                                          int *__restrict__ e) {
+  const int64_t r = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+  if (r >= R) return;
+  const int lane = threadIdx.x % 32;
+  const int64_t k0 = (int64_t)blockIdx.y * kchunk;
+  const int64_t k1 = min(K, k0 + kchunk);
+  int m = INT_MIN;
+  for (int64_t k = k0 + lane; k < k1; k += 32) m = max(m, frexp_exponent(base[r * rs + k * ks]));
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if (lane == 0 && m != INT_MIN) atomicMax(&e[r], m);
 }
 
 // fixed-point integer X = round(x 2^(F - e)) from the IEEE bits (integer ops)
@@ -422,12 +457,13 @@ __global__ void split_kernel(const double *__restrict__ base, int64_t R,
     const int64_t off = (tr * kt + tk) * tile_elems +
                         ((rr / 8) * (KB / 8) + kk) * 64 + (rr % 8) * 8;
     long long d[S][8];
-    const int er = (r < R) ? e[r] : 0;
+    const int er = (r < R) ? e[r] : EXP_FLOOR - 1;
+    const bool live = r < R && er >= EXP_FLOOR;  // rows below the floor are all zero
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
       const int64_t k = kg * 8 + j;
       long long X = 0;
-      if (r < R && k < K) X = to_fixed(base[r * rs + k * ks], er, 7 * S);
+      if (live && k < K) X = to_fixed(base[r * rs + k * ks], er, 7 * S);
 #pragma unroll
       for (int s = S - 1; s >= 1; --s) {
         const long long q = ((X + 64) & 127) - 64;
@@ -464,12 +500,16 @@ void run_emu(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
   DBuf err(ctx, sizeof(int));
   GBCC_CUDA(cudaMemsetAsync(err.as<int>(), 0, sizeof(int), ctx.stream));
   auto exponents = [&](const double *p, int64_t R, int64_t rs, int64_t ks, int *e) {
-    if (rs == 1 && R >= 4096)
-      row_exponent_cols_kernel<<<(unsigned)((R + 127) / 128), 128, 0, ctx.stream>>>(
-          p, R, K, ks, e);
-    else
-      row_exponent_kernel<<<(unsigned)((R + 7) / 8), 256, 0, ctx.stream>>>(p, R, K, rs,
-                                                                         ks, e);
+    GBCC_CUDA(cudaMemsetAsync(e, 0x80, sizeof(int) * R, ctx.stream));
+    if (rs == 1) {
+      const int64_t kchunk = std::max<int64_t>(64, (K + 4095) / 4096);
+      const dim3 grid((unsigned)((R + 127) / 128), (unsigned)((K + kchunk - 1) / kchunk));
+      exponent_rows_contig_kernel<<<grid, 128, 0, ctx.stream>>>(p, R, K, ks, kchunk, e);
+    } else {
+      const int64_t kchunk = std::max<int64_t>(1024, (K + 4095) / 4096);
+      const dim3 grid((unsigned)((R + 7) / 8), (unsigned)((K + kchunk - 1) / kchunk));
+      exponent_rows_warp_kernel<<<grid, 256, 0, ctx.stream>>>(p, R, K, rs, ks, kchunk, e);
+    }
     GBCC_CHECK_LAUNCH(ctx);
   };
   exponents(A, M, ars, aks, ea.as<int>());
@@ -512,7 +552,7 @@ void run_emu(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
     ev1 = ctx.prof_event();
     GBCC_CUDA(cudaEventRecord(ev0, ctx.stream));
   }
-  emu_gemm_kernel<S><<<dim3(mt, nt), NUM_THREADS, smem, ctx.stream>>>(args);
+  emu_gemm_kernel<S><<<(unsigned)((int64_t)mt * nt), NUM_THREADS, smem, ctx.stream>>>(args);
   GBCC_CHECK_LAUNCH(ctx);
   if (ctx.prof) {
     GBCC_CUDA(cudaEventRecord(ev1, ctx.stream));

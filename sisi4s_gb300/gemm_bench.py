@@ -8,8 +8,6 @@ events on the library stream after one warm-up launch.
 import argparse
 import json
 
-import numpy as np
-
 
 def main():
     ap = argparse.ArgumentParser()
@@ -54,7 +52,6 @@ def main():
         out["tensor_kernel_bf16_tflops"] = st["tc_flops"] / st["ms"] / 1e9
     print(json.dumps(out))
     ctx.close()
-    del np
 
 
 if __name__ == "__main__":

@@ -1,0 +1,200 @@
+"""The drop-in boundary without a GPU: the C ABI exports, the YAML step runner
+(parsing, data symbols, cc4s tensor files, fallible steps)."""
+import json
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB = os.path.join(ROOT, "sisi4s_gb300", "_lib", "libgbcc.so")
+RUNNER = os.path.join(ROOT, "sisi4s_gb300", "_lib", "sisi4s-gb300")
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    from sisi4s_gb300 import build
+    build.build()
+
+
+def declared_functions():
+    text = open(os.path.join(ROOT, "include", "gbcc.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(gbcc_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_function():
+    out = subprocess.run(["nm", "-D", "--defined-only", LIB], capture_output=True,
+                         text=True, check=True).stdout
+    exported = set(re.findall(r"\b(gbcc_[a-z0-9_]+)\b", out))
+    decl = declared_functions()
+    assert len(decl) >= 20
+    missing = [f for f in decl if f not in exported]
+    assert not missing, missing
+
+
+def test_library_loads_and_reports_no_device_without_gpu():
+    import ctypes
+    from sisi4s_gb300 import capi
+    lib = capi.load()
+    assert lib.gbcc_abi_version() == 1
+    assert lib.gbcc_status_string(capi.TIMEOUT) == b"TIMEOUT"
+    h = ctypes.c_void_p()
+    st = lib.gbcc_ctx_create(0, None, ctypes.byref(h))
+    try:
+        import torch
+        has_gpu = torch.cuda.is_available()
+    except Exception:
+        has_gpu = False
+    if not has_gpu:
+        assert st == capi.NO_DEVICE
+    else:
+        assert st == capi.OK
+        lib.gbcc_ctx_destroy(h)
+
+
+def _run(tmp_path, yaml_text, *extra):
+    inp = tmp_path / "in.yaml"
+    inp.write_text(yaml_text)
+    out = tmp_path / "out.yaml"
+    r = subprocess.run([RUNNER, "-i", str(inp), "-o", str(out), "-l",
+                        str(tmp_path / "log"), *extra], cwd=tmp_path,
+                       capture_output=True, text=True)
+    return r, json.loads(out.read_text())
+
+
+def _write_tensor(path, arr, binary=True):
+    flat = np.asarray(arr, dtype=np.float64).transpose(
+        tuple(range(arr.ndim - 1, -1, -1))).ravel()
+    dims = "".join("  - length: %d\n    type: State\n" % n for n in arr.shape)
+    path.write_text("version: 100\ntype: Tensor\ndimensions:\n%sscalarType: Real64\n"
+                    "elements:\n  type: %s\nunit: 1.0\n"
+                    % (dims, "IeeeBinaryFile" if binary else "TextFile"))
+    ep = str(path)[:-5] + ".elements"
+    if binary:
+        flat.tofile(ep)
+    else:
+        np.savetxt(ep, flat, fmt="%.17g")
+
+
+def test_read_write_roundtrip_and_symbols(tmp_path):
+    rng = np.random.default_rng(0)
+    a = rng.normal(size=(3, 4, 5))
+    _write_tensor(tmp_path / "A.yaml", a, binary=True)
+    _write_tensor(tmp_path / "B.yaml", a[0], binary=False)
+    r, out = _run(tmp_path, """
+- name: Nop    # anchors as in the reference's inputs
+  energyConvergence: &ec 1e-8
+  mixer: &mx DiisMixer
+- name: Read
+  in:
+    fileName: "A.yaml"
+  out:
+    destination: $A
+- name: Read
+  in: { fileName: B.yaml }
+  out: { destination: $B }
+- name: Write
+  in:
+    source: $A
+    fileName: "C.yaml"
+  out: {}
+- name: TensorWriter
+  in:  { Data: $B }
+  out:
+    {}
+- name: Nop
+  in:
+    a: *ec
+    b: *mx
+    c: 3
+    d: $Undefined
+""")
+    assert r.returncode == 0, r.stderr
+    back = np.fromfile(tmp_path / "C.elements").reshape(5, 4, 3).transpose(2, 1, 0)
+    assert np.array_equal(back, a)
+    txt = np.loadtxt(tmp_path / "B.dat")
+    assert np.allclose(txt, a[0].T.ravel(), rtol=0, atol=0)
+    last = out["steps"][-1]["in"]
+    assert last["a"] == 1e-8 and last["b"] == "DiisMixer" and last["c"] == 3
+    assert last["d"] == "Undefined"
+
+
+def test_define_holes_and_particles(tmp_path):
+    (tmp_path / "E.yaml").write_text(
+        "metaData:\n  fermiEnergy: -0.1\n  energies: [-1.0, -0.5, 0.3, 0.9, 1.7]\n")
+    r, out = _run(tmp_path, """
+- name: DefineHolesAndParticles
+  in:
+    fileName: "E.yaml"
+  out:
+    HoleEigenEnergies: $Eh
+    ParticleEigenEnergies: $Ep
+- name: Write
+  in: { source: $Eh, fileName: Eh.yaml }
+- name: Write
+  in: { source: $Ep, fileName: Ep.yaml }
+""")
+    assert r.returncode == 0, r.stderr
+    assert out["steps"][0]["No"] == 2 and out["steps"][0]["Nv"] == 3
+    assert np.array_equal(np.fromfile(tmp_path / "Eh.elements"), [-1.0, -0.5])
+    assert np.array_equal(np.fromfile(tmp_path / "Ep.elements"), [0.3, 0.9, 1.7])
+
+
+def test_dry_run_of_full_ccsd_t_input(tmp_path):
+    r, out = _run(tmp_path, """
+- name: Nop
+  maxIterations: &maxIterations 50
+- name: CcsdEnergyFromCoulombIntegrals
+  in:
+    mixer: DiisMixer
+    maxResidua: 4
+    maxIterations: *maxIterations
+    energyConvergence: 1e-8
+    CoulombVertex: $CoulombVertex
+    HoleEigenEnergies: $HoleEigenEnergies
+    ParticleEigenEnergies: $ParticleEigenEnergies
+  out:
+    CcsdEnergy: $CcsdEnergy
+    CcsdSinglesAmplitudes: $T1
+    CcsdDoublesAmplitudes: $T2
+- name: CcsdPerturbativeTriples
+  in:
+    CoulombVertex: $CoulombVertex
+    CcsdEnergy: $CcsdEnergy
+    CcsdSinglesAmplitudes: $T1
+    CcsdDoublesAmplitudes: $T2
+    HoleEigenEnergies: $HoleEigenEnergies
+    ParticleEigenEnergies: $ParticleEigenEnergies
+  out:
+    CcsdPerturbativeTriplesEnergy: $E
+""", "--dry")
+    assert r.returncode == 0, r.stderr
+    assert [s["name"] for s in out["steps"]] == [
+        "Nop", "CcsdEnergyFromCoulombIntegrals", "CcsdPerturbativeTriples"]
+    assert out["steps"][1]["in"]["maxIterations"] == 50
+
+
+def test_unknown_algorithm_and_fallible(tmp_path):
+    r, out = _run(tmp_path, "- name: NoSuchAlgorithm\n")
+    assert r.returncode == 1 and "unknown algorithm" in out["error"]
+    r, out = _run(tmp_path, """
+- name: Read
+  fallible: true
+  in: { fileName: missing.yaml }
+  out: { destination: $X }
+- name: Nop
+""")
+    assert r.returncode == 0
+    assert "failed" in out["steps"][0] and out["steps"][1]["name"] == "Nop"
+
+
+def test_list_algorithms():
+    r = subprocess.run([RUNNER, "--list"], capture_output=True, text=True, check=True)
+    names = r.stdout.split()
+    for n in ("CcsdEnergyFromCoulombIntegrals", "CcsdPerturbativeTriples",
+              "CoulombIntegralsFromVertex", "Read", "Write", "TensorWriter",
+              "DefineHolesAndParticles", "Nop"):
+        assert n in names
