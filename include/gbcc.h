@@ -192,6 +192,25 @@ gbcc_status gbcc_dgemm(gbcc_ctx *ctx, int transA, int transB, int64_t M,
                        int64_t lda, const double *B, int64_t ldb, double beta,
                        double *C, int64_t ldc, int precision);
 
+/* The emulated (GBCC_PREC_EMU) GEMM of gbcc_dgemm for callers that cannot let
+ * the library allocate device memory, e.g. a serving process whose arena
+ * already holds the whole HBM budget, or a host loop that must not enter the
+ * CUDA allocator.  It has no counterpart in the reference.  Its scratch (digit
+ * panels of both operands, exponents, error word) lives in one fixed 32 MiB
+ * device array that every GPU loading the library holds until exit; a GEMM
+ * whose scratch would exceed it (S digits x 2 bytes x (M padded to 128 +
+ * N padded to 64) x K padded to 32, plus 4 bytes per row and column) is
+ * rejected with GBCC_BAD_ARG.  Nothing is allocated or freed.  All calls on a
+ * device share the array, so calls whose work overlaps on the GPU race; order
+ * them.  The first call on a device looks up the array's device address; make
+ * it before any stream capture.  Device pointers, context stream, digits from
+ * gbcc_ctx_set_emulation. */
+gbcc_status gbcc_dgemm_emu_noalloc(gbcc_ctx *ctx, int transA, int transB,
+                                   int64_t M, int64_t N, int64_t K,
+                                   double alpha, const double *A, int64_t lda,
+                                   const double *B, int64_t ldb, double beta,
+                                   double *C, int64_t ldc);
+
 /* CCSD energy terms (direct, exchange) of device amplitudes, as
  * ClusterSinglesDoublesAlgorithm::getEnergy (.cxx:131-197). Device pointers. */
 gbcc_status gbcc_energy(gbcc_ctx *ctx, int No, int Nv, const double *T1,

@@ -88,6 +88,11 @@ _SIGS = {
                              C.c_int64, C.c_int64, C.c_double, C.c_void_p,
                              C.c_int64, C.c_void_p, C.c_int64, C.c_double,
                              C.c_void_p, C.c_int64, C.c_int]),
+    "gbcc_dgemm_emu_noalloc": (C.c_int, [C.c_void_p, C.c_int, C.c_int,
+                                         C.c_int64, C.c_int64, C.c_int64,
+                                         C.c_double, C.c_void_p, C.c_int64,
+                                         C.c_void_p, C.c_int64, C.c_double,
+                                         C.c_void_p, C.c_int64]),
     "gbcc_energy": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p,
                               C.c_void_p, C.c_void_p, _dp, _dp]),
 }

@@ -401,6 +401,19 @@ gbcc_status gbcc_dgemm(gbcc_ctx *ctx, int transA, int transB, int64_t M,
   });
 }
 
+gbcc_status gbcc_dgemm_emu_noalloc(gbcc_ctx *ctx, int transA, int transB,
+                                   int64_t M, int64_t N, int64_t K,
+                                   double alpha, const double *A, int64_t lda,
+                                   const double *B, int64_t ldb, double beta,
+                                   double *C, int64_t ldc) {
+  if (!ctx) return GBCC_BAD_ARG;
+  return guard(ctx, [&]() {
+    gbcc::gemm_emu_noalloc(ctx->c, transA != 0, transB != 0, M, N, K, alpha, A,
+                           lda, B, ldb, beta, C, ldc);
+    return GBCC_OK;
+  });
+}
+
 gbcc_status gbcc_energy(gbcc_ctx *ctx, int No, int Nv, const double *T1,
                         const double *T2, const double *Vabij, double *direct,
                         double *exchange) {

@@ -31,6 +31,7 @@
 // what it issued (bounded) and frees its TMEM.
 #include <algorithm>
 #include <climits>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -590,6 +591,153 @@ void gemm_emu(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
     }
     ctx.flops += 2.0 * (double)M * (double)N * (double)K;
   }
+}
+
+}  // namespace gbcc
+
+// ------------------------------------------------------------------------
+// Emulated GEMM that allocates nothing.
+//
+// Some callers of this library cannot let it allocate device memory: a
+// serving process that has reserved the whole HBM budget for its own arena,
+// or a host runtime whose hot loop must not enter the CUDA allocator (its
+// latency and fragmentation are outside the caller's control).  For them the
+// emulated GEMM can run with its scratch (row/column exponents, the digit
+// panels of both operands and the error word) in one file-scope device array
+// of fixed size instead of stream-ordered allocations.
+//
+// Limits and sharing: the array holds GBCC_NOALLOC_SCRATCH_BYTES (32 MiB);
+// every GPU that loads the library holds it until the process exits.  Every
+// call on a device uses the same array and it keeps the previous call's
+// contents; the error word is cleared at the start of each call and all
+// other scratch is fully rewritten before it is read.  Calls whose work
+// overlaps on the GPU (two streams, or two host threads) race on the array
+// and must be ordered by the caller.  The device address of the array is
+// looked up once per device, on the first call made with that device
+// current; that first call should therefore come before any stream capture.
+namespace gbcc {
+namespace {
+
+constexpr size_t NOALLOC_SCRATCH_BYTES = 32u << 20;
+__device__ __align__(256) uint8_t g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
+
+constexpr int MAX_DEVICES = 64;
+std::mutex g_noalloc_mu;
+uint8_t *g_noalloc_ptr[MAX_DEVICES] = {};
+
+uint8_t *noalloc_scratch(int device) {
+  require(device >= 0 && device < MAX_DEVICES, "device index out of range");
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_ptr[device]) {
+    void *p = nullptr;
+    // host code must not take the array's address directly: the name is a
+    // host-side stand-in; the device address comes from the runtime
+    GBCC_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    g_noalloc_ptr[device] = static_cast<uint8_t *>(p);
+  }
+  return g_noalloc_ptr[device];
+}
+
+size_t round256(size_t x) { return (x + 255) / 256 * 256; }
+
+template <int S>
+void run_emu_static(Context &ctx, bool ta, bool tb, int64_t M, int64_t N,
+                    int64_t K, double alpha, const double *A, int64_t lda,
+                    const double *B, int64_t ldb, double beta, double *C,
+                    int64_t ldc, uint8_t *scratch) {
+  const int mt = (int)((M + TM - 1) / TM);
+  const int nt = (int)((N + TN - 1) / TN);
+  const int kt = (int)((K + KB - 1) / KB);
+  require(nt <= 65535, "emu gemm: grid too large");
+  const size_t off_ea = 256;
+  const size_t off_eb = off_ea + round256(sizeof(int) * M);
+  const size_t off_a = off_eb + round256(sizeof(int) * N);
+  const size_t off_b = off_a + round256((size_t)S * mt * kt * A_TILE);
+  const size_t need = off_b + round256((size_t)S * nt * kt * B_TILE);
+  if (need > NOALLOC_SCRATCH_BYTES)
+    throw Error(GBCC_BAD_ARG,
+                "gbcc_dgemm_emu_noalloc: this GEMM needs " + std::to_string(need) +
+                    " bytes of scratch, more than the fixed " +
+                    std::to_string(NOALLOC_SCRATCH_BYTES) + " bytes");
+  int *err = reinterpret_cast<int *>(scratch);
+  int *ea = reinterpret_cast<int *>(scratch + off_ea);
+  int *eb = reinterpret_cast<int *>(scratch + off_eb);
+  __nv_bfloat16 *asl = reinterpret_cast<__nv_bfloat16 *>(scratch + off_a);
+  __nv_bfloat16 *bsl = reinterpret_cast<__nv_bfloat16 *>(scratch + off_b);
+  const int64_t ars = ta ? lda : 1, aks = ta ? 1 : lda;
+  const int64_t brs = tb ? 1 : ldb, bks = tb ? ldb : 1;
+  GBCC_CUDA(cudaMemsetAsync(err, 0, sizeof(int), ctx.stream));
+  auto exponents = [&](const double *p, int64_t R, int64_t rs, int64_t ks, int *e) {
+    GBCC_CUDA(cudaMemsetAsync(e, 0x80, sizeof(int) * R, ctx.stream));
+    if (rs == 1) {
+      const int64_t kchunk = std::max<int64_t>(64, (K + 4095) / 4096);
+      const dim3 grid((unsigned)((R + 127) / 128), (unsigned)((K + kchunk - 1) / kchunk));
+      exponent_rows_contig_kernel<<<grid, 128, 0, ctx.stream>>>(p, R, K, ks, kchunk, e);
+    } else {
+      const int64_t kchunk = std::max<int64_t>(1024, (K + 4095) / 4096);
+      const dim3 grid((unsigned)((R + 7) / 8), (unsigned)((K + kchunk - 1) / kchunk));
+      exponent_rows_warp_kernel<<<grid, 256, 0, ctx.stream>>>(p, R, K, rs, ks, kchunk, e);
+    }
+    GBCC_CHECK_LAUNCH(ctx);
+  };
+  exponents(A, M, ars, aks, ea);
+  exponents(B, N, brs, bks, eb);
+  auto grid_for = [&](int64_t segs) {
+    int64_t g = (segs + 255) / 256;
+    const int64_t cap = (int64_t)std::max(ctx.sm_count, 1) * 16;
+    return (unsigned)std::max<int64_t>(1, std::min(g, cap));
+  };
+  split_kernel<S, TM><<<grid_for((int64_t)mt * TM * kt * 4), 256, 0, ctx.stream>>>(
+      A, M, K, ars, aks, ea, mt, kt, asl);
+  GBCC_CHECK_LAUNCH(ctx);
+  split_kernel<S, TN><<<grid_for((int64_t)nt * TN * kt * 4), 256, 0, ctx.stream>>>(
+      B, N, K, brs, bks, eb, nt, kt, bsl);
+  GBCC_CHECK_LAUNCH(ctx);
+  constexpr int STAGE_BYTES = S * (A_TILE + B_TILE);
+  constexpr int STAGES = (SMEM_BUDGET / STAGE_BYTES) > 4 ? 4 : (SMEM_BUDGET / STAGE_BYTES);
+  const int smem = STAGES * STAGE_BYTES;
+  GBCC_CUDA(cudaFuncSetAttribute(emu_gemm_kernel<S>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  EmuArgs args{};
+  args.A = asl;
+  args.B = bsl;
+  args.ea = ea;
+  args.eb = eb;
+  args.C = C;
+  args.M = M; args.N = N; args.ldc = ldc;
+  args.mt = mt; args.nt = nt; args.kt = kt;
+  args.kc_blocks = (S <= 6 ? 512 : 256) / KB;
+  args.alpha = alpha;
+  args.beta = beta;
+  args.err = err;
+  emu_gemm_kernel<S><<<(unsigned)((int64_t)mt * nt), NUM_THREADS, smem, ctx.stream>>>(args);
+  GBCC_CHECK_LAUNCH(ctx);
+  int h = 0;
+  GBCC_CUDA(cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, ctx.stream));
+  GBCC_CUDA(cudaStreamSynchronize(ctx.stream));
+  if (h != ERR_NONE)
+    throw Error(GBCC_TIMEOUT, "emulated GEMM: a bounded device wait gave up (code " +
+                                  std::to_string(h) + ")");
+}
+
+}  // namespace
+
+void gemm_emu_noalloc(Context &ctx, bool ta, bool tb, int64_t M, int64_t N,
+                      int64_t K, double alpha, const double *A, int64_t lda,
+                      const double *B, int64_t ldb, double beta, double *C,
+                      int64_t ldc) {
+  require(M > 0 && N > 0 && K > 0, "gbcc_dgemm_emu_noalloc: sizes must be positive");
+  require(A && B && C, "gbcc_dgemm_emu_noalloc: null operand");
+  uint8_t *scratch = noalloc_scratch(ctx.device);
+  switch (ctx.emu_slices) {
+    case 4: run_emu_static<4>(ctx, ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, scratch); break;
+    case 5: run_emu_static<5>(ctx, ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, scratch); break;
+    case 6: run_emu_static<6>(ctx, ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, scratch); break;
+    case 7: run_emu_static<7>(ctx, ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, scratch); break;
+    case 8: run_emu_static<8>(ctx, ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, scratch); break;
+    default: throw Error(GBCC_BAD_ARG, "emu_slices must be in [4, 8]");
+  }
+  ctx.flops += 2.0 * (double)M * (double)N * (double)K;
 }
 
 }  // namespace gbcc

@@ -192,6 +192,12 @@ void gemm_emu(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
               double alpha, const double *A, int64_t lda, const double *B,
               int64_t ldb, double beta, double *C, int64_t ldc, int64_t batch,
               int64_t sA, int64_t sB, int64_t sC);
+// emulated GEMM with its scratch in a fixed file-scope device array
+void gemm_emu_noalloc(Context &ctx, bool ta, bool tb, int64_t M, int64_t N,
+                      int64_t K, double alpha, const double *A, int64_t lda,
+                      const double *B, int64_t ldb, double beta, double *C,
+                      int64_t ldc);
+
 // dst[perm-out] = alpha * src + beta * dst, where dst index d of the output
 // tensor corresponds to src dimension perm[d]. dst_lens[d] = src.lens[perm[d]].
 void permute(Context &ctx, const Ten &src, const int *perm, double alpha,
