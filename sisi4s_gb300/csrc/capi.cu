@@ -105,6 +105,14 @@ gbcc_status gbcc_ctx_create(int device, void *stream, gbcc_ctx **out) {
     GBCC_CUDA(cudaSetDevice(device));
     GBCC_CUDA(cudaDeviceGetAttribute(&ctx->c.sm_count,
                                      cudaDevAttrMultiProcessorCount, device));
+    // Temporaries are stream-ordered allocations from the device's default
+    // pool.  By default the pool hands freed memory back to the driver at
+    // every synchronisation, so each CCSD iteration would re-map its
+    // multi-GB working set; keep it in the pool instead.
+    cudaMemPool_t pool;
+    GBCC_CUDA(cudaDeviceGetDefaultMemPool(&pool, device));
+    uint64_t keep = UINT64_MAX;
+    GBCC_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
     if (stream) {
       ctx->c.stream = static_cast<cudaStream_t>(stream);
     } else {
@@ -125,6 +133,7 @@ void gbcc_ctx_destroy(gbcc_ctx *ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->c.device);
   cudaStreamSynchronize(ctx->c.stream);
+  if (ctx->c.dev_err) cudaFree(ctx->c.dev_err);
   ctx->c.prof_harvest();
   for (auto e : ctx->c.prof_pool) cudaEventDestroy(e);
   if (ctx->c.own_stream) cudaStreamDestroy(ctx->c.stream);
@@ -207,6 +216,7 @@ gbcc_status gbcc_ccsd_setup(gbcc_ctx *ctx, const gbcc_ccsd_in *in,
     s->opts = o;
     s->s = std::make_unique<gbcc::Ccsd>(ctx->c, std::move(inputs), o,
                                         in->init_T1, in->init_T2);
+    ctx->c.check_device_errors();
     *out = s.release();
     return GBCC_OK;
   });
@@ -312,7 +322,7 @@ gbcc_status gbcc_ccsd_residual(gbcc_ctx *ctx, const gbcc_ccsd_in *in,
                               cudaMemcpyDeviceToHost, ctx->c.stream));
     GBCC_CUDA(cudaMemcpyAsync(R2, R.as<double>() + L.off2, 8 * L.n2,
                               cudaMemcpyDeviceToHost, ctx->c.stream));
-    GBCC_CUDA(cudaStreamSynchronize(ctx->c.stream));
+    ctx->c.check_device_errors();
     return GBCC_OK;
   });
 }
@@ -397,6 +407,7 @@ gbcc_status gbcc_dgemm(gbcc_ctx *ctx, int transA, int transB, int64_t M,
     gbcc::require(M >= 0 && N >= 0 && K >= 0, "negative size");
     gbcc::gemm(ctx->c, transA != 0, transB != 0, M, N, K, alpha, A, lda, B,
                ldb, beta, C, ldc, 1, 0, 0, 0, precision);
+    ctx->c.check_device_errors();
     return GBCC_OK;
   });
 }

@@ -395,7 +395,7 @@ IterInfo Ccsd::iterate() {
                L_.No, partials_.as<double>(), sc + SC_EN);         // :102
   GBCC_CUDA(cudaMemcpyAsync(pinned_, sc, sizeof(double) * SC_N,
                             cudaMemcpyDeviceToHost, ctx.stream));
-  GBCC_CUDA(cudaStreamSynchronize(ctx.stream));
+  ctx.check_device_errors();  // the one host synchronisation per iteration
   const double *h = pinned_;
   const double spins = 2.0;
   double d = 0.5 * spins * spins * h[SC_EN + 0];                   // :170-172

@@ -170,6 +170,10 @@ struct EmuArgs {
   int64_t M, N, ldc;
   int mt, nt, kt;          // tile counts
   int kc_blocks;           // k-blocks per exact chunk
+  int kb_per_split;        // k-blocks per K-split (a multiple of kc_blocks)
+  int ksplit;              // number of K-splits (1: write C directly)
+  int frac;                // fractional bits of the int64 totals
+  long long *W;            // K-split totals [ksplit][N][M] (ksplit > 1)
   double alpha, beta;
   int *err;
 };
@@ -193,8 +197,10 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) emu_gemm_kernel(EmuArgs a) {
   // column of n-tiles, so that a wave of CTAs shares a compact set of A and B
   // panels in L2
   int tile_m, tile_n;
+  const int64_t ntiles = (int64_t)a.mt * a.nt;
+  const int split = (int)(blockIdx.x / ntiles);
   {
-    const int64_t t = blockIdx.x;
+    const int64_t t = blockIdx.x % ntiles;
     const int64_t gsz = (int64_t)GROUP_M * a.nt;
     const int64_t g = t / gsz, r = t % gsz;
     const int first = (int)(g * GROUP_M);
@@ -202,7 +208,10 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) emu_gemm_kernel(EmuArgs a) {
     tile_m = first + (int)(r % gm);
     tile_n = (int)(r / gm);
   }
-  const int nchunks = (a.kt + a.kc_blocks - 1) / a.kc_blocks;
+  // this CTA's k-blocks: [kb0, kb0 + nkb)
+  const int kb0 = split * a.kb_per_split;
+  const int nkb = max(0, min(a.kt, kb0 + a.kb_per_split) - kb0);
+  const int nchunks = (nkb + a.kc_blocks - 1) / a.kc_blocks;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -234,15 +243,16 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) emu_gemm_kernel(EmuArgs a) {
       const size_t a_slice = (size_t)a.mt * a.kt * (A_TILE / 2);
       const size_t b_slice = (size_t)a.nt * a.kt * (B_TILE / 2);
       int issued = 0;
-      for (int kb = 0; kb < a.kt; ++kb) {
-        const int st = kb % STAGES;
-        if (kb >= STAGES &&
-            !mbar_wait(smem_u32(&bar_empty[st]), ((kb / STAGES) - 1) & 1)) {
+      for (int kl = 0; kl < nkb; ++kl) {
+        const int st = kl % STAGES;
+        if (kl >= STAGES &&
+            !mbar_wait(smem_u32(&bar_empty[st]), ((kl / STAGES) - 1) & 1)) {
           atomicCAS(a.err, 0, ERR_EMPTY);
           abort_sh = 1;
           break;
         }
         if (abort_sh) break;
+        const int kb = kb0 + kl;
         const uint32_t full = smem_u32(&bar_full[st]);
         mbar_expect_tx(full, STAGE_BYTES);
         const uint32_t sbase = smem_base + st * STAGE_BYTES;
@@ -256,17 +266,17 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) emu_gemm_kernel(EmuArgs a) {
               a.B + s * b_slice + ((size_t)tile_n * a.kt + kb) * (B_TILE / 2);
           bulk_g2s(sbase + S * A_TILE + s * B_TILE, gb, B_TILE, full);
         }
-        issued = kb + 1;
+        issued = kl + 1;
       }
       // never leave a bulk copy in flight: wait (bounded) for the last
       // STAGES issued k-blocks to land
-      for (int kb = issued > STAGES ? issued - STAGES : 0; kb < issued; ++kb)
-        mbar_wait(smem_u32(&bar_full[kb % STAGES]), (kb / STAGES) & 1);
+      for (int kl = issued > STAGES ? issued - STAGES : 0; kl < issued; ++kl)
+        mbar_wait(smem_u32(&bar_full[kl % STAGES]), (kl / STAGES) & 1);
     }
   } else if (warp == 1) {
     // ------------------------------------------------------------ MMA issuer
     if (lane == 0) {
-      int kb = 0;
+      int kl = 0;
       bool ok = true;
       for (int c = 0; c < nchunks && ok; ++c) {
         if (c > 0 && !mbar_wait(smem_u32(&bar_acce), (c - 1) & 1)) {
@@ -275,11 +285,11 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) emu_gemm_kernel(EmuArgs a) {
           break;
         }
         tc_fence_after();
-        const int kend = min(a.kt, (c + 1) * a.kc_blocks);
-        const int kfirst = kb;
-        for (; kb < kend; ++kb) {
-          const int st = kb % STAGES;
-          if (!mbar_wait(smem_u32(&bar_full[st]), (kb / STAGES) & 1)) {
+        const int kend = min(nkb, (c + 1) * a.kc_blocks);
+        const int kfirst = kl;
+        for (; kl < kend; ++kl) {
+          const int st = kl % STAGES;
+          if (!mbar_wait(smem_u32(&bar_full[st]), (kl / STAGES) & 1)) {
             atomicCAS(a.err, 0, ERR_FULL);
             ok = false;
             break;
@@ -298,7 +308,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) emu_gemm_kernel(EmuArgs a) {
             for (int s = 0; s < S; ++s) {
               const uint64_t da = smem_desc(sbase + s * A_TILE + k16 * 256, 128,
                                             (KB / 8) * 128);
-              const uint32_t acc = (kb == kfirst && k16 == 0 && s == 0) ? 0u : 1u;
+              const uint32_t acc = (kl == kfirst && k16 == 0 && s == 0) ? 0u : 1u;
 #pragma unroll
               for (int off = 0; off < (S - s) * TN; off += 256) {
                 const int n = min(256, (S - s) * TN - off);
@@ -338,7 +348,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) emu_gemm_kernel(EmuArgs a) {
       tc_fence_after();
 #pragma unroll
       for (int g = 0; g < S; ++g) {
-        const int sh = FRAC - 7 * g;
+        const int sh = a.frac - 7 * g;
 #pragma unroll
         for (int q = 0; q < 2; ++q) {
           float v[16];
@@ -359,16 +369,26 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) emu_gemm_kernel(EmuArgs a) {
     // write out: C[m + n ldc], m = tile_m*128 + row, n = tile_n*64 + half*32 + j
     const int64_t m = (int64_t)tile_m * TM + row;
     if (m < a.M && !abort_sh) {
-      const int ea = max(a.ea[m], EXP_FLOOR);
+      if (a.ksplit == 1) {
+        const int ea = max(a.ea[m], EXP_FLOOR);
 #pragma unroll
-      for (int j = 0; j < 32; ++j) {
-        const int64_t n = (int64_t)tile_n * TN + half * 32 + j;
-        if (n >= a.N) continue;
-        const int e = ea + max(a.eb[n], EXP_FLOOR) - 14 - FRAC;
-        double v = ldexp((double)tot[j], e) * a.alpha;
-        double *cp = a.C + m + n * a.ldc;
-        if (a.beta != 0.0) v = fma(a.beta, *cp, v);
-        *cp = v;
+        for (int j = 0; j < 32; ++j) {
+          const int64_t n = (int64_t)tile_n * TN + half * 32 + j;
+          if (n >= a.N) continue;
+          const int e = ea + max(a.eb[n], EXP_FLOOR) - 14 - a.frac;
+          double v = ldexp((double)tot[j], e) * a.alpha;
+          double *cp = a.C + m + n * a.ldc;
+          if (a.beta != 0.0) v = fma(a.beta, *cp, v);
+          *cp = v;
+        }
+      } else {
+        // exact partial totals; emu_splitk_reduce adds them in split order
+        long long *w = a.W + (size_t)split * a.N * a.M + m;
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          const int64_t n = (int64_t)tile_n * TN + half * 32 + j;
+          if (n < a.N) w[n * a.M] = tot[j];
+        }
       }
     }
   }
@@ -485,21 +505,74 @@ __global__ void split_kernel(const double *__restrict__ base, int64_t R,
   }
 }
 
+// out = alpha * 2^(ea+eb-14-frac) * sum_s W[s] + beta * C, summing the exact
+// int64 split totals in split order (deterministic)
+__global__ void emu_splitk_reduce_kernel(const long long *__restrict__ W, int ks,
+                                         int64_t M, int64_t N,
+                                         const int *__restrict__ ea,
+                                         const int *__restrict__ eb, int frac,
+                                         double alpha, double beta,
+                                         double *__restrict__ C, int64_t ldc) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < M * N;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t m = i % M, n = i / M;
+    long long t = 0;
+    for (int s = 0; s < ks; ++s) t += W[((int64_t)s * N + n) * M + m];
+    const int e = max(ea[m], EXP_FLOOR) + max(eb[n], EXP_FLOOR) - 14 - frac;
+    double v = ldexp((double)t, e) * alpha;
+    double *cp = C + m + n * ldc;
+    if (beta != 0.0) v = fma(beta, *cp, v);
+    *cp = v;
+  }
+}
+
+struct EmuPlan {
+  int mt, nt, kt, kc_blocks, ksplit, kb_per_split, frac;
+};
+
+// Tiles, exact-chunk length, K-split and fixed-point width of one GEMM.
+// The int64 total of an output gathers nchunks chunk sums, each below
+// ~2^(23 + frac); frac = min(29, 38 - ceil(log2 nchunks)) keeps it below 2^62.
+// Small M x N with long K is split over K so that at least two CTAs per SM
+// have work; the split totals are exact, so the split does not change the
+// result.
+EmuPlan emu_plan(int S, int64_t M, int64_t N, int64_t K, int sm_count,
+                 bool allow_split) {
+  EmuPlan p{};
+  p.mt = (int)((M + TM - 1) / TM);
+  p.nt = (int)((N + TN - 1) / TN);
+  p.kt = (int)((K + KB - 1) / KB);
+  p.kc_blocks = (S <= 6 ? 512 : 256) / KB;
+  const int nchunks = (p.kt + p.kc_blocks - 1) / p.kc_blocks;
+  int lg = 0;
+  while ((1 << lg) < nchunks) ++lg;
+  p.frac = std::min(FRAC, 38 - lg);
+  const int64_t ctas = (int64_t)p.mt * p.nt;
+  const int64_t want = 2LL * std::max(sm_count, 1);
+  int ks = 1;
+  if (allow_split && ctas < want && nchunks > 1)
+    ks = (int)std::min<int64_t>({(want + ctas - 1) / ctas, (int64_t)nchunks, 64});
+  const int cps = (nchunks + ks - 1) / ks;  // chunks per split
+  p.kb_per_split = cps * p.kc_blocks;
+  p.ksplit = (p.kt + p.kb_per_split - 1) / p.kb_per_split;
+  return p;
+}
+
 template <int S>
 void run_emu(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
              double alpha, const double *A, int64_t lda, const double *B,
              int64_t ldb, double beta, double *C, int64_t ldc) {
-  const int mt = (int)((M + TM - 1) / TM);
-  const int nt = (int)((N + TN - 1) / TN);
-  const int kt = (int)((K + KB - 1) / KB);
-  require((int64_t)mt * nt < (1LL << 31) && nt <= 65535, "emu gemm: grid too large");
+  const EmuPlan P = emu_plan(S, M, N, K, ctx.sm_count, true);
+  const int mt = P.mt, nt = P.nt, kt = P.kt;
+  require((int64_t)mt * nt * P.ksplit < (1LL << 31), "emu gemm: grid too large");
   // strides of op(A)(m,k) and op(B)^T(n,k)
   const int64_t ars = ta ? lda : 1, aks = ta ? 1 : lda;
   const int64_t brs = tb ? 1 : ldb, bks = tb ? ldb : 1;
   DBuf ea(ctx, sizeof(int) * M), eb(ctx, sizeof(int) * N);
   DBuf asl(ctx, (size_t)S * mt * kt * A_TILE), bsl(ctx, (size_t)S * nt * kt * B_TILE);
-  DBuf err(ctx, sizeof(int));
-  GBCC_CUDA(cudaMemsetAsync(err.as<int>(), 0, sizeof(int), ctx.stream));
+  DBuf wsp;
+  if (P.ksplit > 1) wsp.alloc(ctx, sizeof(long long) * P.ksplit * M * N);
+  int *err = ctx.device_error_word();
   auto exponents = [&](const double *p, int64_t R, int64_t rs, int64_t ks, int *e) {
     GBCC_CUDA(cudaMemsetAsync(e, 0x80, sizeof(int) * R, ctx.stream));
     if (rs == 1) {
@@ -543,17 +616,22 @@ void run_emu(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
   args.C = C;
   args.M = M; args.N = N; args.ldc = ldc;
   args.mt = mt; args.nt = nt; args.kt = kt;
-  args.kc_blocks = (S <= 6 ? 512 : 256) / KB;
+  args.kc_blocks = P.kc_blocks;
+  args.kb_per_split = P.kb_per_split;
+  args.ksplit = P.ksplit;
+  args.frac = P.frac;
+  args.W = P.ksplit > 1 ? wsp.as<long long>() : nullptr;
   args.alpha = alpha;
   args.beta = beta;
-  args.err = err.as<int>();
+  args.err = err;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   if (ctx.prof) {
     ev0 = ctx.prof_event();
     ev1 = ctx.prof_event();
     GBCC_CUDA(cudaEventRecord(ev0, ctx.stream));
   }
-  emu_gemm_kernel<S><<<(unsigned)((int64_t)mt * nt), NUM_THREADS, smem, ctx.stream>>>(args);
+  emu_gemm_kernel<S><<<(unsigned)((int64_t)mt * nt * P.ksplit), NUM_THREADS, smem,
+                       ctx.stream>>>(args);
   GBCC_CHECK_LAUNCH(ctx);
   if (ctx.prof) {
     GBCC_CUDA(cudaEventRecord(ev1, ctx.stream));
@@ -562,13 +640,16 @@ void run_emu(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
     const double f = 2.0 * (double)M * (double)N * (double)K;
     ctx.prof_recs.push_back({ev0, ev1, f * S * (S + 1) / 2.0, f});
   }
-  int h = 0;
-  GBCC_CUDA(cudaMemcpyAsync(&h, err.as<int>(), sizeof(int), cudaMemcpyDeviceToHost,
-                            ctx.stream));
-  GBCC_CUDA(cudaStreamSynchronize(ctx.stream));
-  if (h != ERR_NONE)
-    throw Error(GBCC_TIMEOUT, "emulated GEMM: a bounded device wait gave up (code " +
-                                  std::to_string(h) + ")");
+  if (P.ksplit > 1) {
+    const int64_t n = M * N;
+    const int64_t g = std::min<int64_t>((n + 255) / 256, (int64_t)std::max(ctx.sm_count, 1) * 8);
+    emu_splitk_reduce_kernel<<<(unsigned)std::max<int64_t>(g, 1), 256, 0, ctx.stream>>>(
+        wsp.as<long long>(), P.ksplit, M, N, ea.as<int>(), eb.as<int>(), P.frac, alpha,
+        beta, C, ldc);
+    GBCC_CHECK_LAUNCH(ctx);
+  }
+  // a bounded wait that gave up sets the context's sticky error word; it is
+  // read at the next synchronisation point (check_device_errors)
 }
 
 }  // namespace
@@ -706,7 +787,14 @@ void run_emu_static(Context &ctx, bool ta, bool tb, int64_t M, int64_t N,
   args.C = C;
   args.M = M; args.N = N; args.ldc = ldc;
   args.mt = mt; args.nt = nt; args.kt = kt;
-  args.kc_blocks = (S <= 6 ? 512 : 256) / KB;
+  {
+    const EmuPlan P = emu_plan(S, M, N, K, ctx.sm_count, false);  // no K-split workspace
+    args.kc_blocks = P.kc_blocks;
+    args.kb_per_split = P.kb_per_split;
+    args.ksplit = 1;
+    args.frac = P.frac;
+    args.W = nullptr;
+  }
   args.alpha = alpha;
   args.beta = beta;
   args.err = err;

@@ -56,6 +56,32 @@ struct Context {
   int emu_slices = 6;
   // GEMMs smaller than this many flops stay in FP64 in precision mode
   double emu_min_flops = 1e7;
+  // sticky device error word: kernels whose bounded waits give up record a
+  // code here; read (and cleared) at synchronisation points
+  int *dev_err = nullptr;
+  int *device_error_word() {
+    if (!dev_err) {
+      if (cudaMalloc(&dev_err, sizeof(int)) != cudaSuccess)
+        throw Error(GBCC_OOM, "cannot allocate the device error word");
+      if (cudaMemsetAsync(dev_err, 0, sizeof(int), stream) != cudaSuccess)
+        throw Error(GBCC_CUDA_ERROR, "cannot clear the device error word");
+    }
+    return dev_err;
+  }
+  // synchronises the stream; throws GBCC_TIMEOUT if a kernel recorded an error
+  void check_device_errors() {
+    if (cudaStreamSynchronize(stream) != cudaSuccess)
+      throw Error(GBCC_CUDA_ERROR, "stream synchronisation failed");
+    if (!dev_err) return;
+    int h = 0;
+    if (cudaMemcpy(&h, dev_err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+      throw Error(GBCC_CUDA_ERROR, "cannot read the device error word");
+    if (h != 0) {
+      cudaMemset(dev_err, 0, sizeof(int));
+      throw Error(GBCC_TIMEOUT, "a bounded device wait gave up (code " +
+                                    std::to_string(h) + ")");
+    }
+  }
   // optional per-launch timing of the tensor-core GEMM kernel (CUDA events
   // recorded on the context stream around each launch)
   bool prof = false;

@@ -198,7 +198,7 @@ double triples_energy(Context &ctx, const CcsdInputs &I, const double *T1,
   std::vector<double> h(ntrip);
   GBCC_CUDA(cudaMemcpyAsync(h.data(), per_trip.as<double>(), 8 * ntrip,
                             cudaMemcpyDeviceToHost, ctx.stream));
-  GBCC_CUDA(cudaStreamSynchronize(ctx.stream));
+  ctx.check_device_errors();
   double e = 0.0;
   for (double v : h) e += v;  // fixed (triple) order
   return e;

@@ -62,3 +62,30 @@ def test_random_accuracy(ctx, ta, tb, M, N, K):
     bmax = np.abs(B.T if tb else B).max(axis=0)[None, :]
     bound = K * 2.0 ** -40 * amax * bmax + 1e-15 * np.abs(ref)
     assert np.all(np.abs(got - ref) <= bound)
+
+
+def test_split_k_is_exact(ctx):
+    # few output tiles and a long K: the product is split over K; the split
+    # totals are exact integers, so an exactly representable product must
+    # still come out exactly
+    rng = np.random.default_rng(7)
+    M, N, K = 40, 24, 20000
+    A = rng.integers(-(2 ** 10), 2 ** 10, size=(M, K)).astype(np.float64)
+    B = rng.integers(-(2 ** 10), 2 ** 10, size=(K, N)).astype(np.float64)
+    A[:, 0] = 2.0 ** 10
+    B[0, :] = 2.0 ** 10
+    got = _run(ctx, 0, 0, A, B, np.zeros((M, N)), 1.0, 0.0, 6)
+    assert np.array_equal(got, A @ B)
+
+
+def test_very_long_k_accuracy(ctx):
+    # 4096 exact chunks: the fixed-point width adapts so the int64 totals
+    # cannot overflow
+    rng = np.random.default_rng(8)
+    M, N, K = 32, 32, 1 << 21
+    A = rng.normal(size=(K, M))
+    B = rng.normal(size=(K, N))
+    ref = A.T @ B
+    got = _run(ctx, 1, 0, A, B, np.zeros((M, N)), 1.0, 0.0, 6)
+    bound = K * 2.0 ** -40 * np.abs(A).max(axis=0)[:, None] * np.abs(B).max(axis=0)[None, :]
+    assert np.all(np.abs(got - ref) <= bound)
