@@ -151,6 +151,42 @@ def cpu_iteration_time(sys_, threads):
     return time.perf_counter() - t0
 
 
+SERVE_OPTS = dict(mixer="DiisMixer", max_residua=5, max_iterations=100,
+                  energy_convergence=3e-11, amplitudes_convergence=1e-7)
+
+
+def serve_measure(args):
+    """CCSD(T) serving on samples of the request stream (No ~ U{4..16},
+    Nv log-uniform in [20, 160], NG = 4 Nv, request r seeded with r, the C1
+    convergence settings): one-at-a-time FP64 and mixed on the first
+    `serve_single` requests, and batched mixed with `serve_slots` concurrent
+    solves on the first `serve_requests`, all submitted at t = 0 (saturated)."""
+    from sisi4s_gb300 import serve
+    reqs = serve.make_requests(max(args.serve_requests, args.serve_single))
+    out = {"requests": args.serve_requests, "slots": args.serve_slots,
+           "solve": "RCCSD + (T), DIIS(5), energyConvergence 3e-11, "
+                    "amplitudesConvergence 1e-7, maxIterations 100"}
+    for prec in ("fp64", "emu"):
+        srv = serve.Server(slots=1)
+        recs, wall = serve.run_stream(srv, reqs[:args.serve_single], lam=None,
+                                      precision=prec, **SERVE_OPTS)
+        srv.close()
+        st = serve.latency_stats(recs, wall)
+        out["one_at_a_time_" + prec] = {"requests": args.serve_single,
+                                        "solves_per_s": st["solves_per_s"]}
+    srv = serve.Server(slots=args.serve_slots)
+    recs, wall = serve.run_stream(srv, reqs[:args.serve_requests], lam=None,
+                                  precision="emu", **SERVE_OPTS)
+    srv.close()
+    st = serve.latency_stats(recs, wall)
+    out["batched_emu"] = st
+    out["status_counts"] = {str(k): sum(1 for r in recs if r["status"] == k)
+                            for k in sorted(set(r["status"] for r in recs))}
+    out["batched_over_fp64_one_at_a_time"] = (
+        st["solves_per_s"] / out["one_at_a_time_fp64"]["solves_per_s"])
+    return out
+
+
 def run_reference(args, ws, rank, pg):
     """The reference's math on the host cores: the oracle restatement (the
     reference's CTF build cannot be built here), one C2 iteration per step."""
@@ -189,6 +225,10 @@ def main():
     ap.add_argument("--slices", type=int, default=6)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--serve-requests", type=int, default=32)
+    ap.add_argument("--serve-single", type=int, default=4)
+    ap.add_argument("--serve-slots", type=int, default=8)
     args = ap.parse_args()
     ws, rank, local, pg = dist_init()
     if args.impl == "reference":
@@ -212,14 +252,15 @@ def main():
               max_iterations=total_it + 1, energy_convergence=0.0,
               amplitudes_convergence=0.0)
 
-    # ---- mixed precision, inputs resident
-    sol = gpu.Solver(ctx, s.eps_h, s.eps_p, s.gamma, precision="emu", **kw)
+    # ---- mixed precision, inputs resident (steady-state iterations replay
+    # captured CUDA graphs)
+    sol = gpu.Solver(ctx, s.eps_h, s.eps_p, s.gamma, precision="emu",
+                     **dict(kw, max_iterations=total_it + 2))
     sol.step(args.warmup)
     barrier(pg)
     torch.cuda.synchronize()
     l0 = ctx.launches
     f0 = ctx.flops
-    ctx.profile(True)
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
@@ -227,12 +268,22 @@ def main():
         e_mixed, _ = sol.step(args.steps)
         e1.record(stream)
         torch.cuda.synchronize()
-    ctx.profile(False)
     ms = e0.elapsed_time(e1)
     barrier(pg)
     ms = max_over_ranks(pg, ms)
     launches = ctx.launches - l0
     fl = ctx.flops - f0
+    # roofline of the dominant kernel: two more (untimed) steps with CUDA
+    # events around every tensor-core GEMM launch (graphs off while profiling)
+    ctx.profile(True)
+    p0 = torch.cuda.Event(enable_timing=True)
+    p1 = torch.cuda.Event(enable_timing=True)
+    p0.record(stream)
+    sol.step(2)
+    p1.record(stream)
+    torch.cuda.synchronize()
+    ctx.profile(False)
+    prof_ms = p0.elapsed_time(p1)
     gs = ctx.gemm_stats()
     sol.close()
     value = ws * args.steps / (ms / 1e3)
@@ -288,8 +339,12 @@ def main():
             "launches": gs["launches"],
             "avg_launch_ms": gs["ms"] / max(gs["launches"], 1),
             "fp64_equiv_tflops": gs["fp64_flops"] / (gs["ms"] / 1e3) / 1e12 if gs["ms"] else None,
-            "gemm_share_of_step": gs["ms"] / ms if ms else None,
+            "gemm_share_of_step": gs["ms"] / prof_ms if prof_ms else None,
             "traffic": None}
+
+    serving = None
+    if not args.no_serve:
+        serving = serve_measure(args)
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
@@ -309,6 +364,7 @@ def main():
                                precision="emulated fp64, %d bf16 digits" % args.slices,
                                l2="inputs larger than L2 (T2, V, Gamma >= 0.5 GB)"),
                 "fp64": fp64, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
+                "serving": serving,
                 "gpu_launches": launches,
                 "fp64_equiv_tflops_per_step": fl / args.steps / (ms / args.steps / 1e3) / 1e12,
                 "clocks": clk.summary()}

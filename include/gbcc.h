@@ -65,6 +65,9 @@ void *gbcc_ctx_stream(const gbcc_ctx *ctx);
 gbcc_status gbcc_ctx_set_emulation(gbcc_ctx *ctx, int emu_slices,
                                    double emu_min_flops);
 
+/* Replay of steady-state CCSD iterations as captured CUDA graphs (default on;
+ * off runs every iteration eagerly).  Results are identical either way. */
+gbcc_status gbcc_ctx_set_graphs(gbcc_ctx *ctx, int enable);
 /* Timing of the tensor-core GEMM kernel: enable (1) / disable (0) CUDA-event
  * records around each of its launches on the context stream; stats returns
  * the accumulated device milliseconds, the launches, the bf16 tensor flops of
@@ -174,6 +177,45 @@ gbcc_status gbcc_triples(gbcc_ctx *ctx, const gbcc_triples_in *in,
 /* (T) from a device-resident CCSD solver (no amplitude round trip). */
 gbcc_status gbcc_triples_from_solver(gbcc_solver *s, int precision,
                                      double *e_total, double *e_t);
+
+/* --------------------------------------------------------------- serving */
+/* Continuous admission of many CCSD(T) solves of uneven size on one device
+ * (no counterpart in the reference, which runs one solve per process).
+ * `slots` workers each own a host thread and a CUDA stream; requests are
+ * admitted first-in first-out when a worker is free and their estimated device
+ * footprint fits in the remaining `hbm_budget_bytes`, so requests that arrive
+ * while others run start as slots and memory free up and their kernels run
+ * concurrently.  Results are bit-identical to a solve of the same request
+ * alone (every kernel is deterministic). */
+typedef struct {
+  int device;
+  int slots;                 /* concurrent solves, default 8 */
+  int64_t hbm_budget_bytes;  /* 0: 80 % of the free device memory */
+} gbcc_server_opts;
+
+typedef struct {
+  int64_t id;
+  int status;                /* gbcc_status of the solve */
+  double e_ccsd, e_t, e_total;
+  int iterations, converged;
+  double t_submit, t_admit, t_start, t_done;  /* seconds, monotonic clock */
+} gbcc_result;
+
+typedef struct gbcc_server gbcc_server;
+void gbcc_server_opts_default(gbcc_server_opts *opts);
+gbcc_status gbcc_server_create(const gbcc_server_opts *opts, gbcc_server **out);
+/* Copies the host inputs (vertex and eigenvalues only; the integrals are
+ * built on the device) and queues the solve; `triples` adds (T). */
+gbcc_status gbcc_server_submit(gbcc_server *s, const gbcc_ccsd_in *in,
+                               const gbcc_ccsd_opts *opts, int triples,
+                               int64_t *id);
+gbcc_status gbcc_server_poll(gbcc_server *s, int64_t id, gbcc_result *res,
+                             int *done);
+gbcc_status gbcc_server_wait(gbcc_server *s, int64_t id, gbcc_result *res);
+gbcc_status gbcc_server_stats(gbcc_server *s, int *pending, int *running,
+                              int64_t *bytes_in_use);
+/* Finishes every queued request, then stops the workers. */
+void gbcc_server_destroy(gbcc_server *s);
 
 /* ------------------------------------------------------ Coulomb integrals */
 /* Replaces CoulombIntegralsFromVertex::calculateRealIntegrals for the blocks

@@ -62,6 +62,7 @@ _SIGS = {
     "gbcc_ctx_stream": (C.c_void_p, [C.c_void_p]),
     "gbcc_ctx_set_emulation": (C.c_int, [C.c_void_p, C.c_int, C.c_double]),
     "gbcc_ctx_profile": (C.c_int, [C.c_void_p, C.c_int]),
+    "gbcc_ctx_set_graphs": (C.c_int, [C.c_void_p, C.c_int]),
     "gbcc_ctx_gemm_stats": (C.c_int, [C.c_void_p, _dp, C.POINTER(C.c_int64),
                                       _dp, _dp]),
     "gbcc_ccsd_opts_default": (None, [C.POINTER(CcsdOpts)]),
@@ -165,6 +166,9 @@ class Context:
     def set_emulation(self, slices=6, min_flops=1e7):
         self.check(self.lib.gbcc_ctx_set_emulation(self.h, int(slices),
                                                    float(min_flops)))
+
+    def set_graphs(self, enable=True):
+        self.check(self.lib.gbcc_ctx_set_graphs(self.h, 1 if enable else 0))
 
     def profile(self, enable=True):
         self.check(self.lib.gbcc_ctx_profile(self.h, 1 if enable else 0))

@@ -163,6 +163,12 @@ gbcc_status gbcc_ctx_set_emulation(gbcc_ctx *ctx, int emu_slices,
   return GBCC_OK;
 }
 
+gbcc_status gbcc_ctx_set_graphs(gbcc_ctx *ctx, int enable) {
+  if (!ctx) return GBCC_BAD_ARG;
+  ctx->c.use_graphs = enable != 0;
+  return GBCC_OK;
+}
+
 gbcc_status gbcc_ctx_profile(gbcc_ctx *ctx, int enable) {
   if (!ctx) return GBCC_BAD_ARG;
   ctx->c.prof = enable != 0;

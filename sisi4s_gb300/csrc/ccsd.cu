@@ -157,6 +157,8 @@ Ccsd::Ccsd(Context &ctx, std::unique_ptr<CcsdInputs> in,
 
 Ccsd::~Ccsd() {
   cudaStreamSynchronize(ctx_.stream);
+  for (auto &g : graphs_)
+    if (g.exec) cudaGraphExecDestroy(g.exec);
   if (pinned_) cudaFreeHost(pinned_);
 }
 
@@ -333,24 +335,23 @@ void Ccsd::residual(int it, const double *Tp, double *Rp) {
   }
 }
 
-IterInfo Ccsd::iterate() {
+// Device work of one iteration for the current host state (mixer position,
+// DIIS count, buffer parity); it only reads that state, so that it can be
+// captured into a CUDA graph and replayed for every later iteration that
+// starts from the same state.
+void Ccsd::iteration_body() {
   Context &ctx = ctx_;
   double *sc = scal_.as<double>();
   const int64_t n = L_.ntot;
   residual(it_, T_.as<double>(), R_.as<double>());                 // :95
-  IterInfo info;
   double *amp = nullptr;
   if (o_.mixer == 1) {                                             // DiisMixer
     const int N = o_.max_residua;
     const int k = next_;
-    if (!slotA_[k].bytes()) {
-      slotA_[k].alloc(ctx, 8 * n);
-      slotD_[k].alloc(ctx, 8 * n);
-    }
     std::vector<const double *> hist;
     std::vector<int> hslot;
     for (int i = 0; i < N; ++i)
-      if (i != k && slotD_[i].bytes() && (i < count_ || count_ == N)) {
+      if (i != k && slotD_[i].bytes()) {
         hist.push_back(slotD_[i].as<double>());
         hslot.push_back(i);
       }
@@ -359,20 +360,15 @@ IterInfo Ccsd::iterate() {
                   in_->eps_h.p(), in_->eps_p.p(), o_.level_shift,
                   (int)hist.size(), hist.data(), partials_.as<double>(),
                   sc + SC_UPD);                                    // :96-98
-    if (!hslot.empty())
-      GBCC_CUDA(cudaMemcpyAsync(hist_slot_.as<int>(), hslot.data(),
-                                sizeof(int) * hslot.size(),
-                                cudaMemcpyHostToDevice, ctx.stream));
-    if (count_ < N) ++count_;                                      // DiisMixer.cxx:141
+    const int count = std::min(count_ + 1, N);                     // DiisMixer.cxx:141
     // status as int in the double slot SC_STATUS (reinterpreted)
-    diis_solve(ctx, B_.as<double>(), N, k, count_, sc + SC_UPD,
-               (int)hslot.size(), hist_slot_.as<int>(), w_.as<double>(),
+    diis_solve(ctx, B_.as<double>(), N, k, count, sc + SC_UPD,
+               (int)hslot.size(), hslot.data(), w_.as<double>(),
                sc + SC_LAMBDA, reinterpret_cast<int *>(sc + SC_STATUS));
     std::vector<const double *> src;
-    for (int j = 0; j < count_; ++j) src.push_back(slotA_[(k + N - j) % N].as<double>());
-    diis_combine(ctx, count_, src.data(), w_.as<double>(), T_.as<double>(), n,
+    for (int j = 0; j < count; ++j) src.push_back(slotA_[(k + N - j) % N].as<double>());
+    diis_combine(ctx, count, src.data(), w_.as<double>(), T_.as<double>(), n,
                  partials_.as<double>(), sc + SC_TT);              // :160-174
-    next_ = (k + 1) % N;                                           // :179
     amp = T_.as<double>();
   } else {                                                         // LinearMixer
     jacobi_update(ctx, L_, R_.as<double>(), T_.as<double>(), E_.as<double>(),
@@ -386,15 +382,71 @@ IterInfo Ccsd::iterate() {
       // convergence sums come from the mixed vectors
       copy(ctx, sc + SC_UPD, sc + SC_LIN, 2);
     }
-    have_last_ = true;
-    std::swap(T_, E_);                                             // amplitudes = last
-    std::swap(Lres_, D_);
-    amp = T_.as<double>();
+    amp = E_.as<double>();                                         // becomes T below
   }
   energy_terms(ctx, amp, amp + L_.off2, in_->Vabij.p(), in_->Vx.p(), L_.Nv,
                L_.No, partials_.as<double>(), sc + SC_EN);         // :102
   GBCC_CUDA(cudaMemcpyAsync(pinned_, sc, sizeof(double) * SC_N,
                             cudaMemcpyDeviceToHost, ctx.stream));
+}
+
+IterInfo Ccsd::iterate() {
+  Context &ctx = ctx_;
+  const int64_t n = L_.ntot;
+  IterInfo info;
+  // graph key of the state this iteration starts from (-1: run eagerly)
+  int key = -1;
+  if (o_.mixer == 1) {
+    const int k = next_;
+    if (!slotA_[k].bytes()) {
+      slotA_[k].alloc(ctx, 8 * n);
+      slotD_[k].alloc(ctx, 8 * n);
+    }
+    if (count_ == o_.max_residua && it_ >= 1) key = k;
+  } else if (have_last_ && it_ >= 1) {
+    key = (int)(swaps_ & 1);
+  }
+  if (key >= 0 && ctx.use_graphs && !ctx.prof) {
+    if ((int)graphs_.size() <= key) graphs_.resize(key + 1);
+    Graph &g = graphs_[key];
+    if (!g.exec) {
+      const uint64_t l0 = ctx.launches;
+      const double f0 = ctx.flops;
+      GBCC_CUDA(cudaStreamBeginCapture(ctx.stream, cudaStreamCaptureModeThreadLocal));
+      try {
+        iteration_body();
+      } catch (...) {
+        cudaGraph_t bad = nullptr;
+        cudaStreamEndCapture(ctx.stream, &bad);
+        if (bad) cudaGraphDestroy(bad);
+        throw;
+      }
+      cudaGraph_t graph = nullptr;
+      GBCC_CUDA(cudaStreamEndCapture(ctx.stream, &graph));
+      const cudaError_t ie = cudaGraphInstantiate(&g.exec, graph, 0);
+      cudaGraphDestroy(graph);
+      GBCC_CUDA(ie);
+      g.launches = ctx.launches - l0;
+      g.flops = ctx.flops - f0;
+      ctx.launches = l0;
+      ctx.flops = f0;
+    }
+    GBCC_CUDA(cudaGraphLaunch(g.exec, ctx.stream));
+    ctx.launches += g.launches;
+    ctx.flops += g.flops;
+  } else {
+    iteration_body();
+  }
+  // host state after the iteration
+  if (o_.mixer == 1) {
+    if (count_ < o_.max_residua) ++count_;                         // DiisMixer.cxx:141
+    next_ = (next_ + 1) % o_.max_residua;                          // :179
+  } else {
+    have_last_ = true;
+    std::swap(T_, E_);                                             // amplitudes = last
+    std::swap(Lres_, D_);
+    ++swaps_;
+  }
   ctx.check_device_errors();  // the one host synchronisation per iteration
   const double *h = pinned_;
   const double spins = 2.0;

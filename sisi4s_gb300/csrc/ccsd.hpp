@@ -69,6 +69,16 @@ class Ccsd {
   double e_ = 0, prev_ = 0, dir_ = 0, exc_ = 0;
   std::vector<double> hist_;
   double *pinned_ = nullptr;
+  // steady-state iterations replayed as CUDA graphs, one per starting state
+  // (DIIS ring position, or linear-mixer buffer parity)
+  struct Graph {
+    cudaGraphExec_t exec = nullptr;
+    uint64_t launches = 0;
+    double flops = 0;
+  };
+  std::vector<Graph> graphs_;
+  uint64_t swaps_ = 0;
+  void iteration_body();
 };
 
 }  // namespace gbcc

@@ -173,22 +173,25 @@ __global__ void pair_energy_kernel(const double *__restrict__ T1,
 // DIIS: write 2<dT_i, dT> into row/column k+1 of B, solve the leading
 // (count+1) block B c = (-1,0,...,0) by Gaussian elimination with partial
 // pivoting, and emit the weights w_j = c[i_j + 1], i_j = (k + N - j) % N.
+struct HistSlots {
+  int n;
+  int slot[GBCC_MAX_DIIS];
+};
+
 __global__ void diis_solve_kernel(double *B, int N, int k, int count,
-                                  const int *slot_valid,
-                                  const double *__restrict__ sums, int nhist,
-                                  const int *hist_slot, double *weights,
+                                  const double *__restrict__ sums,
+                                  HistSlots hs, double *weights,
                                   double *lambda, int *status) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   const int ld = N + 1;
-  // sums: [0] dT.dT (own slot), [2+q] dT.hist[q] (slot hist_slot[q])
+  // sums: [0] dT.dT (own slot), [2+q] dT.hist[q] (slot hs.slot[q])
   B[(k + 1) + ld * (k + 1)] = 2.0 * sums[0];
-  for (int q = 0; q < nhist; ++q) {
-    const int i = hist_slot[q];
+  for (int q = 0; q < hs.n; ++q) {
+    const int i = hs.slot[q];
     const double ov = 2.0 * sums[2 + q];
     B[(k + 1) + ld * (i + 1)] = ov;
     B[(i + 1) + ld * (k + 1)] = ov;
   }
-  (void)slot_valid;
   const int dim = count + 1;
   double M[(GBCC_MAX_DIIS + 1) * (GBCC_MAX_DIIS + 1)];
   double x[GBCC_MAX_DIIS + 1];
@@ -418,10 +421,13 @@ void pair_energy(Context &ctx, const double *T1, const double *T2,
 }
 
 void diis_solve(Context &ctx, double *B, int N, int k, int count,
-                const double *sums, int nhist, const int *hist_slot_dev,
+                const double *sums, int nhist, const int *hist_slot,
                 double *weights, double *lambda, int *status) {
-  diis_solve_kernel<<<1, 32, 0, ctx.stream>>>(B, N, k, count, nullptr, sums,
-                                              nhist, hist_slot_dev, weights,
+  require(nhist <= GBCC_MAX_DIIS, "too many DIIS vectors");
+  HistSlots hs{};
+  hs.n = nhist;
+  for (int q = 0; q < nhist; ++q) hs.slot[q] = hist_slot[q];
+  diis_solve_kernel<<<1, 32, 0, ctx.stream>>>(B, N, k, count, sums, hs, weights,
                                               lambda, status);
   GBCC_CHECK_LAUNCH(ctx);
 }

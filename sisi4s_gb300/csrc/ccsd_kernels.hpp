@@ -37,8 +37,9 @@ void energy_terms(Context &ctx, const double *T1, const double *T2,
 void pair_energy(Context &ctx, const double *T1, const double *T2,
                  const double *V, const double *Vx, int64_t Nv, int64_t No,
                  double *out);
+// hist_slot: host array of the nhist history slots (passed as kernel arguments)
 void diis_solve(Context &ctx, double *B, int N, int k, int count,
-                const double *sums, int nhist, const int *hist_slot_dev,
+                const double *sums, int nhist, const int *hist_slot,
                 double *weights, double *lambda, int *status);
 void diis_combine(Context &ctx, int count, const double *const *src,
                   const double *w, double *out, int64_t n, double *partials,

@@ -56,6 +56,8 @@ struct Context {
   int emu_slices = 6;
   // GEMMs smaller than this many flops stay in FP64 in precision mode
   double emu_min_flops = 1e7;
+  // replay steady-state CCSD iterations as captured CUDA graphs
+  bool use_graphs = true;
   // sticky device error word: kernels whose bounded waits give up record a
   // code here; read (and cleared) at synchronisation points
   int *dev_err = nullptr;

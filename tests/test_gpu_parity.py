@@ -179,3 +179,23 @@ def test_deterministic_bits(ctx):
     a = gpu.ccsd_solve(ctx, s.eps_h, s.eps_p, s.gamma, **kw)
     b = gpu.ccsd_solve(ctx, s.eps_h, s.eps_p, s.gamma, **kw)
     assert a["energy"] == b["energy"] and np.array_equal(a["T2"], b["T2"])
+
+
+@pytest.mark.parametrize("mixer,precision", [("DiisMixer", "fp64"),
+                                             ("DiisMixer", "emu"),
+                                             ("LinearMixer", "fp64")])
+def test_graph_replay_equals_eager(ctx, mixer, precision):
+    """Steady-state iterations replayed from captured CUDA graphs give the
+    same bits as eager execution."""
+    s = make_system(4, 20, 60, seed=9)
+    kw = dict(mixer=mixer, max_residua=3, mixing_ratio=0.8, max_iterations=10,
+              energy_convergence=0.0, amplitudes_convergence=0.0,
+              precision=precision)
+    ctx.set_emulation(6, 1e4)
+    ctx.set_graphs(False)
+    eager = gpu.ccsd_solve(ctx, s.eps_h, s.eps_p, s.gamma, **kw)
+    ctx.set_graphs(True)
+    graph = gpu.ccsd_solve(ctx, s.eps_h, s.eps_p, s.gamma, **kw)
+    ctx.set_emulation(6, 1e7)
+    assert np.array_equal(eager["history"], graph["history"])
+    assert np.array_equal(eager["T2"], graph["T2"])
