@@ -654,6 +654,143 @@ void run_emu(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
 
 }  // namespace
 
+// ------------------------------------------------------------ pre-split panels
+// A family of `count` operands with the same shape, operand p at base +
+// p*pstride, each R x K with element (r, k) at r*rs + k*ks, split once into
+// digit panels (A role: 128-row tiles, B role: 64-row tiles) and reused by
+// many GEMMs.
+namespace {
+template <int S>
+void split_batch(Context &ctx, EmuPanels &P, const double *base, int64_t pstride) {
+  const int TR = P.role_a ? TM : TN;
+  const int64_t plane = (int64_t)P.rt * P.kt * TR * KB;  // elements per digit plane
+  const int64_t K = P.K;
+  auto grid_for = [&](int64_t segs) {
+    int64_t g = (segs + 255) / 256;
+    const int64_t cap = (int64_t)std::max(ctx.sm_count, 1) * 16;
+    return (unsigned)std::max<int64_t>(1, std::min(g, cap));
+  };
+  for (int p = 0; p < P.count; ++p) {
+    const double *b = base + p * pstride;
+    int *e = P.exps.as<int>() + (int64_t)p * P.rows;
+    GBCC_CUDA(cudaMemsetAsync(e, 0x80, sizeof(int) * P.rows, ctx.stream));
+    if (P.rs == 1) {
+      const int64_t kchunk = std::max<int64_t>(64, (K + 4095) / 4096);
+      const dim3 grid((unsigned)((P.rows + 127) / 128), (unsigned)((K + kchunk - 1) / kchunk));
+      exponent_rows_contig_kernel<<<grid, 128, 0, ctx.stream>>>(b, P.rows, K, P.ks, kchunk, e);
+    } else {
+      const int64_t kchunk = std::max<int64_t>(1024, (K + 4095) / 4096);
+      const dim3 grid((unsigned)((P.rows + 7) / 8), (unsigned)((K + kchunk - 1) / kchunk));
+      exponent_rows_warp_kernel<<<grid, 256, 0, ctx.stream>>>(b, P.rows, K, P.rs, P.ks, kchunk, e);
+    }
+    GBCC_CHECK_LAUNCH(ctx);
+    __nv_bfloat16 *out = P.panels.as<__nv_bfloat16>() + (int64_t)p * S * plane;
+    if (P.role_a)
+      split_kernel<S, TM><<<grid_for((int64_t)P.rt * TM * P.kt * 4), 256, 0, ctx.stream>>>(
+          b, P.rows, K, P.rs, P.ks, e, P.rt, P.kt, out);
+    else
+      split_kernel<S, TN><<<grid_for((int64_t)P.rt * TN * P.kt * 4), 256, 0, ctx.stream>>>(
+          b, P.rows, K, P.rs, P.ks, e, P.rt, P.kt, out);
+    GBCC_CHECK_LAUNCH(ctx);
+  }
+}
+
+template <int S>
+void gemm_panels(Context &ctx, const EmuPanels &A, int ia, const EmuPanels &B, int ib,
+                 double alpha, double beta, double *C, int64_t ldc) {
+  const int64_t M = A.rows, N = B.rows, K = A.K;
+  const EmuPlan P = emu_plan(S, M, N, K, ctx.sm_count, true);
+  const int64_t aplane = (int64_t)A.rt * A.kt * TM * KB;
+  const int64_t bplane = (int64_t)B.rt * B.kt * TN * KB;
+  DBuf wsp;
+  if (P.ksplit > 1) wsp.alloc(ctx, sizeof(long long) * P.ksplit * M * N);
+  constexpr int STAGE_BYTES = S * (A_TILE + B_TILE);
+  constexpr int STAGES = (SMEM_BUDGET / STAGE_BYTES) > 4 ? 4 : (SMEM_BUDGET / STAGE_BYTES);
+  const int smem = STAGES * STAGE_BYTES;
+  GBCC_CUDA(cudaFuncSetAttribute(emu_gemm_kernel<S>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  EmuArgs args{};
+  args.A = A.panels.as<__nv_bfloat16>() + (int64_t)ia * S * aplane;
+  args.B = B.panels.as<__nv_bfloat16>() + (int64_t)ib * S * bplane;
+  args.ea = A.exps.as<int>() + (int64_t)ia * M;
+  args.eb = B.exps.as<int>() + (int64_t)ib * N;
+  args.C = C;
+  args.M = M; args.N = N; args.ldc = ldc;
+  args.mt = P.mt; args.nt = P.nt; args.kt = P.kt;
+  args.kc_blocks = P.kc_blocks;
+  args.kb_per_split = P.kb_per_split;
+  args.ksplit = P.ksplit;
+  args.frac = P.frac;
+  args.W = P.ksplit > 1 ? wsp.as<long long>() : nullptr;
+  args.alpha = alpha;
+  args.beta = beta;
+  args.err = ctx.device_error_word();
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  if (ctx.prof) {
+    ev0 = ctx.prof_event();
+    ev1 = ctx.prof_event();
+    GBCC_CUDA(cudaEventRecord(ev0, ctx.stream));
+  }
+  emu_gemm_kernel<S><<<(unsigned)((int64_t)P.mt * P.nt * P.ksplit), NUM_THREADS, smem,
+                       ctx.stream>>>(args);
+  GBCC_CHECK_LAUNCH(ctx);
+  if (ctx.prof) {
+    GBCC_CUDA(cudaEventRecord(ev1, ctx.stream));
+    const double f = 2.0 * (double)M * (double)N * (double)K;
+    ctx.prof_recs.push_back({ev0, ev1, f * S * (S + 1) / 2.0, f});
+  }
+  if (P.ksplit > 1) {
+    const int64_t n = M * N;
+    const int64_t g = std::min<int64_t>((n + 255) / 256, (int64_t)std::max(ctx.sm_count, 1) * 8);
+    emu_splitk_reduce_kernel<<<(unsigned)std::max<int64_t>(g, 1), 256, 0, ctx.stream>>>(
+        wsp.as<long long>(), P.ksplit, M, N, args.ea, args.eb, P.frac, alpha, beta, C, ldc);
+    GBCC_CHECK_LAUNCH(ctx);
+  }
+  ctx.flops += 2.0 * (double)M * (double)N * (double)K;
+}
+}  // namespace
+
+EmuPanels emu_split(Context &ctx, bool role_a, const double *base, int64_t R,
+                    int64_t K, int64_t rs, int64_t ks, int count, int64_t pstride) {
+  require(R > 0 && K > 0 && count > 0, "emu_split: empty operand");
+  EmuPanels P;
+  P.role_a = role_a;
+  P.S = ctx.emu_slices;
+  P.rows = R;
+  P.K = K;
+  P.rs = rs;
+  P.ks = ks;
+  P.count = count;
+  P.rt = (int)((R + (role_a ? TM : TN) - 1) / (role_a ? TM : TN));
+  P.kt = (int)((K + KB - 1) / KB);
+  const size_t tile = role_a ? A_TILE : B_TILE;
+  P.panels.alloc(ctx, (size_t)count * P.S * P.rt * P.kt * tile);
+  P.exps.alloc(ctx, sizeof(int) * (size_t)count * R);
+  switch (P.S) {
+    case 4: split_batch<4>(ctx, P, base, pstride); break;
+    case 5: split_batch<5>(ctx, P, base, pstride); break;
+    case 6: split_batch<6>(ctx, P, base, pstride); break;
+    case 7: split_batch<7>(ctx, P, base, pstride); break;
+    case 8: split_batch<8>(ctx, P, base, pstride); break;
+    default: throw Error(GBCC_BAD_ARG, "emu_slices must be in [4, 8]");
+  }
+  return P;
+}
+
+void emu_gemm_panels(Context &ctx, const EmuPanels &A, int ia, const EmuPanels &B,
+                     int ib, double alpha, double beta, double *C, int64_t ldc) {
+  require(A.role_a && !B.role_a && A.K == B.K && A.S == B.S, "emu_gemm_panels: operand mismatch");
+  require(ia >= 0 && ia < A.count && ib >= 0 && ib < B.count, "emu_gemm_panels: index");
+  switch (A.S) {
+    case 4: gemm_panels<4>(ctx, A, ia, B, ib, alpha, beta, C, ldc); break;
+    case 5: gemm_panels<5>(ctx, A, ia, B, ib, alpha, beta, C, ldc); break;
+    case 6: gemm_panels<6>(ctx, A, ia, B, ib, alpha, beta, C, ldc); break;
+    case 7: gemm_panels<7>(ctx, A, ia, B, ib, alpha, beta, C, ldc); break;
+    case 8: gemm_panels<8>(ctx, A, ia, B, ib, alpha, beta, C, ldc); break;
+    default: throw Error(GBCC_BAD_ARG, "emu_slices must be in [4, 8]");
+  }
+}
+
 void gemm_emu(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
               double alpha, const double *A, int64_t lda, const double *B,
               int64_t ldb, double beta, double *C, int64_t ldc, int64_t batch,

@@ -220,6 +220,20 @@ void gemm_emu(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
               double alpha, const double *A, int64_t lda, const double *B,
               int64_t ldb, double beta, double *C, int64_t ldc, int64_t batch,
               int64_t sA, int64_t sB, int64_t sC);
+// Digit panels of a family of `count` same-shape operands (operand p at
+// base + p*pstride, element (r, k) at r*rs + k*ks), split once and reused by
+// many emulated GEMMs.  role_a: A operand (rows = M), else B (rows = N).
+struct EmuPanels {
+  DBuf panels, exps;
+  bool role_a = true;
+  int S = 6, count = 0, rt = 0, kt = 0;
+  int64_t rows = 0, K = 0, rs = 0, ks = 0;
+};
+EmuPanels emu_split(Context &ctx, bool role_a, const double *base, int64_t R,
+                    int64_t K, int64_t rs, int64_t ks, int count, int64_t pstride);
+// C[M,N] = alpha A_ia B_ib^T + beta C with M = A.rows, N = B.rows, K = A.K
+void emu_gemm_panels(Context &ctx, const EmuPanels &A, int ia, const EmuPanels &B,
+                     int ib, double alpha, double beta, double *C, int64_t ldc);
 // emulated GEMM with its scratch in a fixed file-scope device array
 void gemm_emu_noalloc(Context &ctx, bool ta, bool tb, int64_t M, int64_t N,
                       int64_t K, double alpha, const double *A, int64_t lda,

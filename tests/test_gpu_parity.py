@@ -199,3 +199,15 @@ def test_graph_replay_equals_eager(ctx, mixer, precision):
     ctx.set_emulation(6, 1e7)
     assert np.array_equal(eager["history"], graph["history"])
     assert np.array_equal(eager["T2"], graph["T2"])
+
+
+@pytest.mark.parametrize("No,Nv,NG", [(3, 8, 20), (4, 40, 90)])
+def test_triples_emulated_matches_oracle(ctx, No, Nv, NG):
+    s = make_system(No, Nv, NG, seed=No + Nv)
+    ints = oracle_ints(s.gamma, No)
+    T1, T2 = _rand_amplitudes(Nv, No, seed=3, scale=0.05)
+    ref = triples_dense(s.eps_h, s.eps_p, T1, T2, ints["PPHH"], ints["HHHP"],
+                        s.gamma)
+    et, _ = gpu.triples(ctx, s.eps_h, s.eps_p, s.gamma, T1, T2, precision="emu")
+    # six bf16 digits: ~2^-40 relative per contraction
+    assert abs(et - ref) < 1e-10 * max(1.0, abs(ref))
