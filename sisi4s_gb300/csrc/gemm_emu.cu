@@ -31,6 +31,7 @@
 // what it issued (bounded) and frees its TMEM.
 #include <algorithm>
 #include <climits>
+#include <cmath>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -162,6 +163,60 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
   for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
 }
 
+// Output scaling alpha: (-1)^neg 2^shift when pow2, else a general multiplier.
+struct OutScale {
+  double alpha;
+  int pow2, shift, neg;
+};
+
+OutScale out_scale(double alpha) {
+  OutScale o{alpha, 0, 0, 0};
+  int x = 0;
+  const double m = std::frexp(alpha, &x);
+  if (m == 0.5 || m == -0.5) {
+    o.pow2 = 1;
+    o.shift = x - 1;
+    o.neg = alpha < 0.0 ? 1 : 0;
+  }
+  return o;
+}
+
+// rare route of fixed_to_double (subnormal or overflowing results)
+__device__ __noinline__ double fixed_to_double_slow(long long t, int e) {
+  return ldexp(__ll2double_rn(t), e);
+}
+
+// t * 2^e rounded once to the nearest double (ties to even): the value of
+// ldexp((double)t, e) whenever the result is a normal number, built with
+// integer instructions only (leading-zero count, 53-bit round, exponent
+// field), because the FP64 pipe of this GPU issues a few instructions per
+// clock per SM and the GEMM epilogue converts every output element.
+// Subnormal or overflowing results take the FP64 route.
+__device__ __forceinline__ double fixed_to_double(long long t, int e) {
+  if (t == 0) return 0.0;
+  const unsigned long long sgn = (unsigned long long)t & 0x8000000000000000ull;
+  unsigned long long mag = t < 0 ? 0ull - (unsigned long long)t : (unsigned long long)t;
+  const int lz = __clzll((long long)mag);
+  mag <<= lz;                                // leading one at bit 63
+  unsigned long long mant = mag >> 11;       // 53 significant bits
+  const unsigned rem = (unsigned)(mag & 0x7FFull);
+  mant += (rem > 0x400u || (rem == 0x400u && (mant & 1ull))) ? 1ull : 0ull;
+  int be = 63 - lz + e + 1023;               // biased exponent of the leading one
+  if (mant >> 53) {
+    mant >>= 1;
+    ++be;
+  }
+  if (be <= 0 || be >= 2047) return fixed_to_double_slow(t, e);
+  return __longlong_as_double(
+      (long long)(sgn | ((unsigned long long)be << 52) | (mant & 0xFFFFFFFFFFFFFull)));
+}
+
+// alpha * t * 2^e; a power-of-two alpha costs no FP64 instruction
+__device__ __forceinline__ double scaled_total(long long t, int e, const OutScale &o) {
+  if (o.pow2) return fixed_to_double(o.neg ? -t : t, e + o.shift);
+  return fixed_to_double(t, e) * o.alpha;
+}
+
 struct EmuArgs {
   const __nv_bfloat16 *A;  // [S][mt][kt] tiles
   const __nv_bfloat16 *B;  // [S][nt][kt] tiles
@@ -174,7 +229,8 @@ struct EmuArgs {
   int ksplit;              // number of K-splits (1: write C directly)
   int frac;                // fractional bits of the int64 totals
   long long *W;            // K-split totals [ksplit][N][M] (ksplit > 1)
-  double alpha, beta;
+  OutScale os;             // alpha
+  double beta;
   int *err;
 };
 
@@ -366,27 +422,39 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) emu_gemm_kernel(EmuArgs a) {
       tc_fence_before();
       mbar_arrive(smem_u32(&bar_acce));
     }
-    // write out: C[m + n ldc], m = tile_m*128 + row, n = tile_n*64 + half*32 + j
+    // write out: C[m + n ldc], m = tile_m*128 + row, n = n0 + j.  The 32
+    // column exponents are loaded once (one per lane) and broadcast by
+    // shuffles, and C is read in batches of 8 columns, so the write-out waits
+    // on a few memory latencies instead of one per column.
     const int64_t m = (int64_t)tile_m * TM + row;
-    if (m < a.M && !abort_sh) {
+    const int64_t n0 = (int64_t)tile_n * TN + half * 32;
+    if (!abort_sh) {
       if (a.ksplit == 1) {
-        const int ea = max(a.ea[m], EXP_FLOOR);
+        const int ebl = (n0 + lane < a.N) ? max(a.eb[n0 + lane], EXP_FLOOR) : 0;
+        const bool mrow = m < a.M;
+        const int ea = mrow ? max(a.ea[m], EXP_FLOOR) - 14 - a.frac : 0;
+        double *cp = a.C + m + n0 * a.ldc;
 #pragma unroll
-        for (int j = 0; j < 32; ++j) {
-          const int64_t n = (int64_t)tile_n * TN + half * 32 + j;
-          if (n >= a.N) continue;
-          const int e = ea + max(a.eb[n], EXP_FLOOR) - 14 - a.frac;
-          double v = ldexp((double)tot[j], e) * a.alpha;
-          double *cp = a.C + m + n * a.ldc;
-          if (a.beta != 0.0) v = fma(a.beta, *cp, v);
-          *cp = v;
+        for (int j0 = 0; j0 < 32; j0 += 8) {
+          double c[8];
+#pragma unroll
+          for (int j = 0; j < 8; ++j)
+            c[j] = (a.beta != 0.0 && mrow && n0 + j0 + j < a.N) ? cp[(j0 + j) * a.ldc] : 0.0;
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            const int eb = __shfl_sync(0xffffffffu, ebl, j0 + j);
+            if (!mrow || n0 + j0 + j >= a.N) continue;
+            double v = scaled_total(tot[j0 + j], ea + eb, a.os);
+            if (a.beta != 0.0) v = fma(a.beta, c[j], v);
+            cp[(j0 + j) * a.ldc] = v;
+          }
         }
-      } else {
+      } else if (m < a.M) {
         // exact partial totals; emu_splitk_reduce adds them in split order
         long long *w = a.W + (size_t)split * a.N * a.M + m;
 #pragma unroll
         for (int j = 0; j < 32; ++j) {
-          const int64_t n = (int64_t)tile_n * TN + half * 32 + j;
+          const int64_t n = n0 + j;
           if (n < a.N) w[n * a.M] = tot[j];
         }
       }
@@ -511,7 +579,7 @@ __global__ void emu_splitk_reduce_kernel(const long long *__restrict__ W, int ks
                                          int64_t M, int64_t N,
                                          const int *__restrict__ ea,
                                          const int *__restrict__ eb, int frac,
-                                         double alpha, double beta,
+                                         OutScale os, double beta,
                                          double *__restrict__ C, int64_t ldc) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < M * N;
        i += (int64_t)gridDim.x * blockDim.x) {
@@ -519,7 +587,7 @@ __global__ void emu_splitk_reduce_kernel(const long long *__restrict__ W, int ks
     long long t = 0;
     for (int s = 0; s < ks; ++s) t += W[((int64_t)s * N + n) * M + m];
     const int e = max(ea[m], EXP_FLOOR) + max(eb[n], EXP_FLOOR) - 14 - frac;
-    double v = ldexp((double)t, e) * alpha;
+    double v = scaled_total(t, e, os);
     double *cp = C + m + n * ldc;
     if (beta != 0.0) v = fma(beta, *cp, v);
     *cp = v;
@@ -621,7 +689,7 @@ void run_emu(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
   args.ksplit = P.ksplit;
   args.frac = P.frac;
   args.W = P.ksplit > 1 ? wsp.as<long long>() : nullptr;
-  args.alpha = alpha;
+  args.os = out_scale(alpha);
   args.beta = beta;
   args.err = err;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -644,7 +712,7 @@ void run_emu(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
     const int64_t n = M * N;
     const int64_t g = std::min<int64_t>((n + 255) / 256, (int64_t)std::max(ctx.sm_count, 1) * 8);
     emu_splitk_reduce_kernel<<<(unsigned)std::max<int64_t>(g, 1), 256, 0, ctx.stream>>>(
-        wsp.as<long long>(), P.ksplit, M, N, ea.as<int>(), eb.as<int>(), P.frac, alpha,
+        wsp.as<long long>(), P.ksplit, M, N, ea.as<int>(), eb.as<int>(), P.frac, args.os,
         beta, C, ldc);
     GBCC_CHECK_LAUNCH(ctx);
   }
@@ -722,7 +790,7 @@ void gemm_panels(Context &ctx, const EmuPanels &A, int ia, const EmuPanels &B, i
   args.ksplit = P.ksplit;
   args.frac = P.frac;
   args.W = P.ksplit > 1 ? wsp.as<long long>() : nullptr;
-  args.alpha = alpha;
+  args.os = out_scale(alpha);
   args.beta = beta;
   args.err = ctx.device_error_word();
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -743,7 +811,7 @@ void gemm_panels(Context &ctx, const EmuPanels &A, int ia, const EmuPanels &B, i
     const int64_t n = M * N;
     const int64_t g = std::min<int64_t>((n + 255) / 256, (int64_t)std::max(ctx.sm_count, 1) * 8);
     emu_splitk_reduce_kernel<<<(unsigned)std::max<int64_t>(g, 1), 256, 0, ctx.stream>>>(
-        wsp.as<long long>(), P.ksplit, M, N, args.ea, args.eb, P.frac, alpha, beta, C, ldc);
+        wsp.as<long long>(), P.ksplit, M, N, args.ea, args.eb, P.frac, args.os, beta, C, ldc);
     GBCC_CHECK_LAUNCH(ctx);
   }
   ctx.flops += 2.0 * (double)M * (double)N * (double)K;
@@ -932,7 +1000,7 @@ void run_emu_static(Context &ctx, bool ta, bool tb, int64_t M, int64_t N,
     args.frac = P.frac;
     args.W = nullptr;
   }
-  args.alpha = alpha;
+  args.os = out_scale(alpha);
   args.beta = beta;
   args.err = err;
   emu_gemm_kernel<S><<<(unsigned)((int64_t)mt * nt), NUM_THREADS, smem, ctx.stream>>>(args);

@@ -89,3 +89,23 @@ def test_very_long_k_accuracy(ctx):
     got = _run(ctx, 1, 0, A, B, np.zeros((M, N)), 1.0, 0.0, 6)
     bound = K * 2.0 ** -40 * np.abs(A).max(axis=0)[:, None] * np.abs(B).max(axis=0)[None, :]
     assert np.all(np.abs(got - ref) <= bound)
+
+
+@pytest.mark.parametrize("alpha", [1.0, -2.0, 0.7])
+def test_wide_totals_round_to_nearest(ctx, alpha):
+    # 21-bit integers are exactly three 7-bit digits, so with 8 slices every
+    # digit product is kept and the int64 totals are exact; the exact products
+    # need more than 53 significant bits, so the conversion of the totals to
+    # double must round to nearest (ties to even) like numpy's int64 -> float64
+    rng = np.random.default_rng(11)
+    M, N, K = 64, 48, 16384
+    A = rng.integers(2 ** 19, 2 ** 20, size=(M, K))
+    B = rng.integers(2 ** 19, 2 ** 20, size=(K, N))
+    A[:, 0] = 2 ** 20
+    B[0, :] = 2 ** 20
+    exact = A @ B                      # int64, 2^52 < . < 2^55
+    assert (exact > 2 ** 53).mean() > 0.5
+    want = exact.astype(np.float64) * alpha
+    got = _run(ctx, 0, 0, A.astype(np.float64), B.astype(np.float64),
+               np.zeros((M, N)), alpha, 0.0, 8)
+    assert np.array_equal(got, want)
