@@ -26,9 +26,12 @@
 // copies (cp.async.bulk, the TMA engine) through a multi-stage mbarrier
 // pipeline.  Warp roles: warp 0 producer, warp 1 MMA issuer (one thread,
 // tcgen05.mma kind::f16, M=128, K=16, N up to 256: the B digits that pair
-// with one A digit are stacked along N), warps 2-9 epilogue (tcgen05.ld).
-// Every wait is bounded; on timeout the kernel records an error code, drains
-// what it issued (bounded) and frees its TMEM.
+// with one A digit are stacked along N), warps 2-17 epilogue (tcgen05.ld).
+// The kernel is persistent: one CTA per SM walks its share of the output
+// tiles, and the epilogue hands TMEM back to the MMA issuer as soon as it has
+// folded a chunk, so the conversion and store of one tile overlap the MMAs
+// of the next.  Every wait is bounded; on timeout the kernel records an error
+// code, drains what it issued (bounded) and frees its TMEM.
 #include <algorithm>
 #include <climits>
 #include <cmath>
@@ -38,6 +41,7 @@
 
 #include <cuda_bf16.h>
 
+#include "df32.hpp"
 #include "internal.hpp"
 
 namespace gbcc {
@@ -49,7 +53,9 @@ constexpr int KB = 32;         // k per tile
 constexpr int A_TILE = TM * KB * 2;  // bytes
 constexpr int B_TILE = TN * KB * 2;
 constexpr int FRAC = 29;       // fractional bits of the int64 total (g=0 units)
-constexpr int NUM_THREADS = 320;     // 10 warps
+constexpr int EPI_WARPS = 16;        // epilogue warps (4 per TMEM lane quarter)
+constexpr int EPI_COLS = TN / (EPI_WARPS / 4);  // output columns per epilogue thread
+constexpr int NUM_THREADS = 64 + 32 * EPI_WARPS;
 constexpr int SMEM_BUDGET = 220 * 1024;
 constexpr long long WAIT_LIMIT = 1LL << 26;
 constexpr int GROUP_M = 16;    // m-tiles per rasterization group
@@ -222,6 +228,7 @@ struct EmuArgs {
   const __nv_bfloat16 *B;  // [S][nt][kt] tiles
   const int *ea, *eb;      // row / column exponents
   double *C;
+  df32 *Cdf;               // float-float output instead of C when not null
   int64_t M, N, ldc;
   int mt, nt, kt;          // tile counts
   int kc_blocks;           // k-blocks per exact chunk
@@ -234,7 +241,50 @@ struct EmuArgs {
   int *err;
 };
 
-template <int S>
+// work unit u (a K-split of one output tile) -> split index and tile.
+// Grouped rasterization: consecutive units walk GROUP_M m-tiles down one
+// column of n-tiles, so that the CTAs working at the same time share a
+// compact set of A and B panels in L2.
+// (32-bit arithmetic: the host keeps mt * nt * ksplit below 2^31; 64-bit
+// integer division would cost FP64-pipe instructions on this GPU)
+__device__ __forceinline__ void unit_coords(const EmuArgs &a, int u, int &split,
+                                            int &tile_m, int &tile_n) {
+  const int ntiles = a.mt * a.nt;
+  split = u / ntiles;
+  const int t = u - split * ntiles;
+  const int gsz = GROUP_M * a.nt;
+  const int g = t / gsz, r = t - g * gsz;
+  const int first = g * GROUP_M;
+  const int gm = min(GROUP_M, a.mt - first);
+  tile_m = first + r % gm;
+  tile_n = r / gm;
+}
+
+// a * 2^k for a float-float a (exact unless the result leaves the FP32 range)
+__device__ __forceinline__ df32 df_ldexp(df32 v, int k) {
+  while (k > 127 || k < -126) {
+    const int step = k > 0 ? 127 : -126;
+    const float f = __int_as_float((step + 127) << 23);
+    v = df_make(v.hi * f, v.lo * f);
+    k -= step;
+    if (v.hi == 0.0f) return v;
+  }
+  const float f = __int_as_float((k + 127) << 23);
+  return df_make(v.hi * f, v.lo * f);
+}
+
+// a + b for an FP32 b (TwoSum of the leading parts, then Fast2Sum)
+__device__ __forceinline__ df32 df_add_f(df32 a, float b) {
+  const float s = a.hi + b;
+  const float bb = s - a.hi;
+  const float e = ((a.hi - (s - bb)) + (b - bb)) + a.lo;
+  return df_fast2sum(s, e);
+}
+
+// DF: float-float output (a.Cdf).  The exact FP32 diagonal sums are then
+// added straight into a float-float accumulator, smallest diagonal first, on
+// the FP32 pipe; otherwise they fold into an exact int64 total.
+template <int S, bool DF>
 __global__ void __launch_bounds__(NUM_THREADS, 1) emu_gemm_kernel(EmuArgs a) {
   constexpr int STAGE_BYTES = S * (A_TILE + B_TILE);
   constexpr int STAGES = (SMEM_BUDGET / STAGE_BYTES) > 4 ? 4 : (SMEM_BUDGET / STAGE_BYTES);
@@ -249,25 +299,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) emu_gemm_kernel(EmuArgs a) {
   __shared__ volatile int abort_sh;
 
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-  // grouped rasterization: consecutive CTAs walk GROUP_M m-tiles down one
-  // column of n-tiles, so that a wave of CTAs shares a compact set of A and B
-  // panels in L2
-  int tile_m, tile_n;
-  const int64_t ntiles = (int64_t)a.mt * a.nt;
-  const int split = (int)(blockIdx.x / ntiles);
-  {
-    const int64_t t = blockIdx.x % ntiles;
-    const int64_t gsz = (int64_t)GROUP_M * a.nt;
-    const int64_t g = t / gsz, r = t % gsz;
-    const int first = (int)(g * GROUP_M);
-    const int gm = min(GROUP_M, a.mt - first);
-    tile_m = first + (int)(r % gm);
-    tile_n = (int)(r / gm);
-  }
-  // this CTA's k-blocks: [kb0, kb0 + nkb)
-  const int kb0 = split * a.kb_per_split;
-  const int nkb = max(0, min(a.kt, kb0 + a.kb_per_split) - kb0);
-  const int nchunks = (nkb + a.kc_blocks - 1) / a.kc_blocks;
+  const int nunits = a.mt * a.nt * a.ksplit;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -275,7 +307,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) emu_gemm_kernel(EmuArgs a) {
       mbar_init(smem_u32(&bar_empty[s]), 1);
     }
     mbar_init(smem_u32(&bar_accf), 1);
-    mbar_init(smem_u32(&bar_acce), 256);
+    mbar_init(smem_u32(&bar_acce), 32 * EPI_WARPS);
     mbar_init(smem_u32(&bar_drain), 1);
     abort_sh = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -298,164 +330,241 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) emu_gemm_kernel(EmuArgs a) {
     if (lane == 0) {
       const size_t a_slice = (size_t)a.mt * a.kt * (A_TILE / 2);
       const size_t b_slice = (size_t)a.nt * a.kt * (B_TILE / 2);
-      int issued = 0;
-      for (int kl = 0; kl < nkb; ++kl) {
-        const int st = kl % STAGES;
-        if (kl >= STAGES &&
-            !mbar_wait(smem_u32(&bar_empty[st]), ((kl / STAGES) - 1) & 1)) {
-          atomicCAS(a.err, 0, ERR_EMPTY);
-          abort_sh = 1;
-          break;
+      long long g = 0;  // k-blocks issued by this CTA
+      bool ok = true;
+      for (int u = blockIdx.x; u < nunits && ok; u += gridDim.x) {
+        int split, tile_m, tile_n;
+        unit_coords(a, u, split, tile_m, tile_n);
+        const int kb0 = split * a.kb_per_split;
+        const int nkb = max(0, min(a.kt, kb0 + a.kb_per_split) - kb0);
+        for (int kl = 0; kl < nkb; ++kl) {
+          const int st = (int)(g % STAGES);
+          if (g >= STAGES &&
+              !mbar_wait(smem_u32(&bar_empty[st]), (int)((g / STAGES) - 1) & 1)) {
+            atomicCAS(a.err, 0, ERR_EMPTY);
+            abort_sh = 1;
+            ok = false;
+            break;
+          }
+          if (abort_sh) {
+            ok = false;
+            break;
+          }
+          const int kb = kb0 + kl;
+          const uint32_t full = smem_u32(&bar_full[st]);
+          mbar_expect_tx(full, STAGE_BYTES);
+          const uint32_t sbase = smem_base + st * STAGE_BYTES;
+          for (int s = 0; s < S; ++s) {
+            const __nv_bfloat16 *ga =
+                a.A + s * a_slice + ((size_t)tile_m * a.kt + kb) * (A_TILE / 2);
+            bulk_g2s(sbase + s * A_TILE, ga, A_TILE, full);
+          }
+          for (int s = 0; s < S; ++s) {
+            const __nv_bfloat16 *gb =
+                a.B + s * b_slice + ((size_t)tile_n * a.kt + kb) * (B_TILE / 2);
+            bulk_g2s(sbase + S * A_TILE + s * B_TILE, gb, B_TILE, full);
+          }
+          ++g;
         }
-        if (abort_sh) break;
-        const int kb = kb0 + kl;
-        const uint32_t full = smem_u32(&bar_full[st]);
-        mbar_expect_tx(full, STAGE_BYTES);
-        const uint32_t sbase = smem_base + st * STAGE_BYTES;
-        for (int s = 0; s < S; ++s) {
-          const __nv_bfloat16 *ga =
-              a.A + s * a_slice + ((size_t)tile_m * a.kt + kb) * (A_TILE / 2);
-          bulk_g2s(sbase + s * A_TILE, ga, A_TILE, full);
-        }
-        for (int s = 0; s < S; ++s) {
-          const __nv_bfloat16 *gb =
-              a.B + s * b_slice + ((size_t)tile_n * a.kt + kb) * (B_TILE / 2);
-          bulk_g2s(sbase + S * A_TILE + s * B_TILE, gb, B_TILE, full);
-        }
-        issued = kl + 1;
       }
       // never leave a bulk copy in flight: wait (bounded) for the last
       // STAGES issued k-blocks to land
-      for (int kl = issued > STAGES ? issued - STAGES : 0; kl < issued; ++kl)
-        mbar_wait(smem_u32(&bar_full[kl % STAGES]), (kl / STAGES) & 1);
+      for (long long k = g > STAGES ? g - STAGES : 0; k < g; ++k)
+        mbar_wait(smem_u32(&bar_full[k % STAGES]), (int)(k / STAGES) & 1);
     }
+    __syncwarp();
   } else if (warp == 1) {
     // ------------------------------------------------------------ MMA issuer
     if (lane == 0) {
-      int kl = 0;
+      long long g = 0;   // k-blocks consumed
+      long long cg = 0;  // chunks issued
       bool ok = true;
-      for (int c = 0; c < nchunks && ok; ++c) {
-        if (c > 0 && !mbar_wait(smem_u32(&bar_acce), (c - 1) & 1)) {
-          atomicCAS(a.err, 0, ERR_ACCE);
-          ok = false;
-          break;
-        }
-        tc_fence_after();
-        const int kend = min(nkb, (c + 1) * a.kc_blocks);
-        const int kfirst = kl;
-        for (; kl < kend; ++kl) {
-          const int st = kl % STAGES;
-          if (!mbar_wait(smem_u32(&bar_full[st]), (kl / STAGES) & 1)) {
-            atomicCAS(a.err, 0, ERR_FULL);
+      for (int u = blockIdx.x; u < nunits && ok; u += gridDim.x) {
+        int split, tile_m, tile_n;
+        unit_coords(a, u, split, tile_m, tile_n);
+        const int kb0 = split * a.kb_per_split;
+        const int nkb = max(0, min(a.kt, kb0 + a.kb_per_split) - kb0);
+        const int nchunks = (nkb + a.kc_blocks - 1) / a.kc_blocks;
+        int kl = 0;
+        for (int c = 0; c < nchunks; ++c) {
+          // TMEM is free once the epilogue has folded the previous chunk
+          if (cg > 0 && !mbar_wait(smem_u32(&bar_acce), (int)(cg - 1) & 1)) {
+            atomicCAS(a.err, 0, ERR_ACCE);
             ok = false;
             break;
           }
           tc_fence_after();
-          const uint32_t sbase = smem_base + st * STAGE_BYTES;
-          // Pairs (s, t) go to diagonal g = s + t at TMEM columns g*TN, so
-          // all pairs of one A digit s write the contiguous column range
-          // [s*TN, S*TN): one MMA per s (split at N = 256) whose B operand is
-          // the B digit tiles t = 0..S-1-s stacked along N (consecutive 4 KB
-          // tiles keep the 512 B row-group stride).  The first MMA of a chunk
-          // (s = 0, k16 = 0) overwrites every diagonal.
+          const int kend = min(nkb, (c + 1) * a.kc_blocks);
+          const int kfirst = kl;
+          for (; kl < kend; ++kl) {
+            const int st = (int)(g % STAGES);
+            if (!mbar_wait(smem_u32(&bar_full[st]), (int)(g / STAGES) & 1)) {
+              atomicCAS(a.err, 0, ERR_FULL);
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+            const uint32_t sbase = smem_base + st * STAGE_BYTES;
+            // Pairs (s, t) go to diagonal g = s + t at TMEM columns g*TN, so
+            // all pairs of one A digit s write the contiguous column range
+            // [s*TN, S*TN): one MMA per s (split at N = 256) whose B operand is
+            // the B digit tiles t = 0..S-1-s stacked along N (consecutive 4 KB
+            // tiles keep the 512 B row-group stride).  The first MMA of a chunk
+            // (s = 0, k16 = 0) overwrites every diagonal.
 #pragma unroll
-          for (int k16 = 0; k16 < KB / 16; ++k16) {
+            for (int k16 = 0; k16 < KB / 16; ++k16) {
 #pragma unroll
-            for (int s = 0; s < S; ++s) {
-              const uint64_t da = smem_desc(sbase + s * A_TILE + k16 * 256, 128,
-                                            (KB / 8) * 128);
-              const uint32_t acc = (kl == kfirst && k16 == 0 && s == 0) ? 0u : 1u;
+              for (int s = 0; s < S; ++s) {
+                const uint64_t da = smem_desc(sbase + s * A_TILE + k16 * 256, 128,
+                                              (KB / 8) * 128);
+                const uint32_t acc = (kl == kfirst && k16 == 0 && s == 0) ? 0u : 1u;
 #pragma unroll
-              for (int off = 0; off < (S - s) * TN; off += 256) {
-                const int n = min(256, (S - s) * TN - off);
-                const uint64_t db =
-                    smem_desc(sbase + S * A_TILE + (off / TN) * B_TILE + k16 * 256,
-                              128, (KB / 8) * 128);
-                mma_bf16(tmem + s * TN + off, da, db, instr_desc(TM, n), acc);
+                for (int off = 0; off < (S - s) * TN; off += 256) {
+                  const int n = min(256, (S - s) * TN - off);
+                  const uint64_t db =
+                      smem_desc(sbase + S * A_TILE + (off / TN) * B_TILE + k16 * 256,
+                                128, (KB / 8) * 128);
+                  mma_bf16(tmem + s * TN + off, da, db, instr_desc(TM, n), acc);
+                }
               }
             }
+            mma_commit(smem_u32(&bar_empty[st]));
+            ++g;
           }
-          mma_commit(smem_u32(&bar_empty[st]));
+          if (!ok) break;
+          mma_commit(smem_u32(&bar_accf));
+          ++cg;
         }
-        if (!ok) break;
-        mma_commit(smem_u32(&bar_accf));
       }
       // make sure every issued MMA finished before TMEM is released
       mma_commit(smem_u32(&bar_drain));
       if (!mbar_wait(smem_u32(&bar_drain), 0)) atomicCAS(a.err, 0, ERR_DRAIN);
       if (!ok) abort_sh = 1;
     }
+    __syncwarp();
   } else {
     // ------------------------------------------------------------ epilogue
-    const int ew = warp - 2;             // 0..7
+    const int ew = warp - 2;             // 0..EPI_WARPS-1
     const int quarter = warp & 3;        // TMEM lane quarter this warp may access
-    const int half = ew >> 2;            // column half
+    const int cgrp = ew >> 2;            // column group of EPI_COLS columns
     const int row = quarter * 32 + lane; // row within the tile
     const uint32_t lane_addr = tmem + ((uint32_t)(quarter * 32) << 16);
-    long long tot[32];
+    long long cg = 0;  // chunks consumed
+    for (int u = blockIdx.x; u < nunits; u += gridDim.x) {
+      int split, tile_m, tile_n;
+      unit_coords(a, u, split, tile_m, tile_n);
+      const int kb0 = split * a.kb_per_split;
+      const int nkb = max(0, min(a.kt, kb0 + a.kb_per_split) - kb0);
+      const int nchunks = (nkb + a.kc_blocks - 1) / a.kc_blocks;
+      long long tot[DF ? 1 : EPI_COLS];
+      df32 acc[DF ? EPI_COLS : 1];
 #pragma unroll
-    for (int j = 0; j < 32; ++j) tot[j] = 0;
-    for (int c = 0; c < nchunks; ++c) {
-      if (!mbar_wait(smem_u32(&bar_accf), c & 1)) {
-        atomicCAS(a.err, 0, ERR_ACCF);
-        break;
-      }
-      if (abort_sh) break;
-      tc_fence_after();
+      for (int j = 0; j < (DF ? 1 : EPI_COLS); ++j) tot[j] = 0;
 #pragma unroll
-      for (int g = 0; g < S; ++g) {
-        const int sh = a.frac - 7 * g;
+      for (int j = 0; j < (DF ? EPI_COLS : 1); ++j) acc[j] = df_make(0.0f, 0.0f);
+      bool ok = true;
+      for (int c = 0; c < nchunks; ++c) {
+        if (!mbar_wait(smem_u32(&bar_accf), (int)(cg & 1))) {
+          atomicCAS(a.err, 0, ERR_ACCF);
+          ok = false;
+          break;
+        }
+        if (abort_sh) {
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        if constexpr (DF) {
+          // acc += sum_g x_g 2^(-7g), units of the g = 0 digit product
 #pragma unroll
-        for (int q = 0; q < 2; ++q) {
-          float v[16];
-          tmem_ld16(lane_addr + g * TN + half * 32 + q * 16, v);
+          for (int g = S - 1; g >= 0; --g) {
+            const float w = __int_as_float((127 - 7 * g) << 23);  // 2^(-7g), exact scaling
+            float v[16];
+            tmem_ld16(lane_addr + g * TN + cgrp * EPI_COLS, v);
 #pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            const long long x = (long long)__float2int_rn(v[j]);  // exact, |v| <= 2^24
-            long long y;
-            if (sh >= 0) y = x << sh;
-            else y = (x + (1LL << (-sh - 1))) >> (-sh);
-            tot[q * 16 + j] += y;
+            for (int j = 0; j < EPI_COLS; ++j) acc[j] = df_add_f(acc[j], v[j] * w);
+          }
+        } else {
+#pragma unroll
+          for (int g = 0; g < S; ++g) {
+            const int sh = a.frac - 7 * g;
+            float v[16];
+            tmem_ld16(lane_addr + g * TN + cgrp * EPI_COLS, v);
+#pragma unroll
+            for (int j = 0; j < EPI_COLS; ++j) {
+              const long long x = (long long)__float2int_rn(v[j]);  // exact, |v| <= 2^24
+              long long y;
+              if (sh >= 0) y = x << sh;
+              else y = (x + (1LL << (-sh - 1))) >> (-sh);
+              tot[j] += y;
+            }
           }
         }
+        tc_fence_before();
+        mbar_arrive(smem_u32(&bar_acce));
+        ++cg;
       }
-      tc_fence_before();
-      mbar_arrive(smem_u32(&bar_acce));
-    }
-    // write out: C[m + n ldc], m = tile_m*128 + row, n = n0 + j.  The 32
-    // column exponents are loaded once (one per lane) and broadcast by
-    // shuffles, and C is read in batches of 8 columns, so the write-out waits
-    // on a few memory latencies instead of one per column.
-    const int64_t m = (int64_t)tile_m * TM + row;
-    const int64_t n0 = (int64_t)tile_n * TN + half * 32;
-    if (!abort_sh) {
+      if (!ok || abort_sh) break;
+      // write out: C[m + n ldc], m = tile_m*128 + row, n = n0 + j.  The column
+      // exponents are loaded once (one per lane) and broadcast by shuffles,
+      // and C is read in batches of 8 columns, so the write-out waits on a
+      // few memory latencies instead of one per column.
+      const int64_t m = (int64_t)tile_m * TM + row;
+      const int64_t n0 = (int64_t)tile_n * TN + cgrp * EPI_COLS;
       if (a.ksplit == 1) {
-        const int ebl = (n0 + lane < a.N) ? max(a.eb[n0 + lane], EXP_FLOOR) : 0;
+        const int ebl =
+            (lane < EPI_COLS && n0 + lane < a.N) ? max(a.eb[n0 + lane], EXP_FLOOR) : 0;
         const bool mrow = m < a.M;
         const int ea = mrow ? max(a.ea[m], EXP_FLOOR) - 14 - a.frac : 0;
+        const bool accumulate = a.beta != 0.0;
+        if constexpr (DF) {
+          // float-float output; alpha = +-2^k and beta in {0, 1} (host-checked)
+          const int ea_df = mrow ? max(a.ea[m], EXP_FLOOR) - 14 + a.os.shift : 0;
+          df32 *cp = a.Cdf + m + n0 * a.ldc;
+#pragma unroll
+          for (int j0 = 0; j0 < EPI_COLS; j0 += 8) {
+            df32 c[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+              c[j] = (accumulate && mrow && n0 + j0 + j < a.N) ? cp[(j0 + j) * a.ldc]
+                                                              : df_make(0.0f, 0.0f);
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+              const int eb = __shfl_sync(0xffffffffu, ebl, j0 + j);
+              if (!mrow || n0 + j0 + j >= a.N) continue;
+              df32 v = df_ldexp(acc[j0 + j], ea_df + eb);
+              if (a.os.neg) v = df_neg(v);
+              if (accumulate) v = df_add(v, c[j]);
+              cp[(j0 + j) * a.ldc] = v;
+            }
+          }
+        } else {
         double *cp = a.C + m + n0 * a.ldc;
 #pragma unroll
-        for (int j0 = 0; j0 < 32; j0 += 8) {
+        for (int j0 = 0; j0 < EPI_COLS; j0 += 8) {
           double c[8];
 #pragma unroll
           for (int j = 0; j < 8; ++j)
-            c[j] = (a.beta != 0.0 && mrow && n0 + j0 + j < a.N) ? cp[(j0 + j) * a.ldc] : 0.0;
+            c[j] = (accumulate && mrow && n0 + j0 + j < a.N) ? cp[(j0 + j) * a.ldc] : 0.0;
 #pragma unroll
           for (int j = 0; j < 8; ++j) {
             const int eb = __shfl_sync(0xffffffffu, ebl, j0 + j);
             if (!mrow || n0 + j0 + j >= a.N) continue;
             double v = scaled_total(tot[j0 + j], ea + eb, a.os);
-            if (a.beta != 0.0) v = fma(a.beta, c[j], v);
+            if (accumulate) v = fma(a.beta, c[j], v);
             cp[(j0 + j) * a.ldc] = v;
           }
         }
+        }
       } else if (m < a.M) {
         // exact partial totals; emu_splitk_reduce adds them in split order
-        long long *w = a.W + (size_t)split * a.N * a.M + m;
+        if constexpr (!DF) {
+          long long *w = a.W + (size_t)split * a.N * a.M + m;
 #pragma unroll
-        for (int j = 0; j < 32; ++j) {
-          const int64_t n = n0 + j;
-          if (n < a.N) w[n * a.M] = tot[j];
+          for (int j = 0; j < EPI_COLS; ++j) {
+            const int64_t n = n0 + j;
+            if (n < a.N) w[n * a.M] = tot[j];
+          }
         }
       }
     }
@@ -594,6 +703,11 @@ __global__ void emu_splitk_reduce_kernel(const long long *__restrict__ W, int ks
   }
 }
 
+// persistent grid: one CTA per SM (shared memory and TMEM allow no more)
+unsigned emu_grid(const Context &ctx, int64_t units) {
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>(units, std::max(ctx.sm_count, 1)));
+}
+
 struct EmuPlan {
   int mt, nt, kt, kc_blocks, ksplit, kb_per_split, frac;
 };
@@ -672,7 +786,7 @@ void run_emu(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
   const int smem = STAGES * STAGE_BYTES;
   static bool attr_set = false;
   if (!attr_set) {
-    GBCC_CUDA(cudaFuncSetAttribute(emu_gemm_kernel<S>,
+    GBCC_CUDA(cudaFuncSetAttribute(emu_gemm_kernel<S, false>,
                                    cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     attr_set = true;
   }
@@ -698,7 +812,7 @@ void run_emu(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
     ev1 = ctx.prof_event();
     GBCC_CUDA(cudaEventRecord(ev0, ctx.stream));
   }
-  emu_gemm_kernel<S><<<(unsigned)((int64_t)mt * nt * P.ksplit), NUM_THREADS, smem,
+  emu_gemm_kernel<S, false><<<emu_grid(ctx, (int64_t)mt * nt * P.ksplit), NUM_THREADS, smem,
                        ctx.stream>>>(args);
   GBCC_CHECK_LAUNCH(ctx);
   if (ctx.prof) {
@@ -765,9 +879,10 @@ void split_batch(Context &ctx, EmuPanels &P, const double *base, int64_t pstride
 
 template <int S>
 void gemm_panels(Context &ctx, const EmuPanels &A, int ia, const EmuPanels &B, int ib,
-                 double alpha, double beta, double *C, int64_t ldc) {
+                 double alpha, double beta, double *C, df32 *Cdf, int64_t ldc) {
   const int64_t M = A.rows, N = B.rows, K = A.K;
-  const EmuPlan P = emu_plan(S, M, N, K, ctx.sm_count, true);
+  // float-float output is written directly (no K-split workspace)
+  const EmuPlan P = emu_plan(S, M, N, K, ctx.sm_count, Cdf == nullptr);
   const int64_t aplane = (int64_t)A.rt * A.kt * TM * KB;
   const int64_t bplane = (int64_t)B.rt * B.kt * TN * KB;
   DBuf wsp;
@@ -775,7 +890,8 @@ void gemm_panels(Context &ctx, const EmuPanels &A, int ia, const EmuPanels &B, i
   constexpr int STAGE_BYTES = S * (A_TILE + B_TILE);
   constexpr int STAGES = (SMEM_BUDGET / STAGE_BYTES) > 4 ? 4 : (SMEM_BUDGET / STAGE_BYTES);
   const int smem = STAGES * STAGE_BYTES;
-  GBCC_CUDA(cudaFuncSetAttribute(emu_gemm_kernel<S>,
+  void (*kern)(EmuArgs) = Cdf ? emu_gemm_kernel<S, true> : emu_gemm_kernel<S, false>;
+  GBCC_CUDA(cudaFuncSetAttribute(kern,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
   EmuArgs args{};
   args.A = A.panels.as<__nv_bfloat16>() + (int64_t)ia * S * aplane;
@@ -783,6 +899,7 @@ void gemm_panels(Context &ctx, const EmuPanels &A, int ia, const EmuPanels &B, i
   args.ea = A.exps.as<int>() + (int64_t)ia * M;
   args.eb = B.exps.as<int>() + (int64_t)ib * N;
   args.C = C;
+  args.Cdf = Cdf;
   args.M = M; args.N = N; args.ldc = ldc;
   args.mt = P.mt; args.nt = P.nt; args.kt = P.kt;
   args.kc_blocks = P.kc_blocks;
@@ -799,7 +916,7 @@ void gemm_panels(Context &ctx, const EmuPanels &A, int ia, const EmuPanels &B, i
     ev1 = ctx.prof_event();
     GBCC_CUDA(cudaEventRecord(ev0, ctx.stream));
   }
-  emu_gemm_kernel<S><<<(unsigned)((int64_t)P.mt * P.nt * P.ksplit), NUM_THREADS, smem,
+  kern<<<emu_grid(ctx, (int64_t)P.mt * P.nt * P.ksplit), NUM_THREADS, smem,
                        ctx.stream>>>(args);
   GBCC_CHECK_LAUNCH(ctx);
   if (ctx.prof) {
@@ -846,15 +963,20 @@ EmuPanels emu_split(Context &ctx, bool role_a, const double *base, int64_t R,
 }
 
 void emu_gemm_panels(Context &ctx, const EmuPanels &A, int ia, const EmuPanels &B,
-                     int ib, double alpha, double beta, double *C, int64_t ldc) {
+                     int ib, double alpha, double beta, double *C, int64_t ldc,
+                     df32 *Cdf) {
   require(A.role_a && !B.role_a && A.K == B.K && A.S == B.S, "emu_gemm_panels: operand mismatch");
   require(ia >= 0 && ia < A.count && ib >= 0 && ib < B.count, "emu_gemm_panels: index");
+  if (Cdf) {
+    require(out_scale(alpha).pow2 && (beta == 0.0 || beta == 1.0),
+            "emu_gemm_panels: float-float output needs alpha = +-2^k and beta in {0, 1}");
+  }
   switch (A.S) {
-    case 4: gemm_panels<4>(ctx, A, ia, B, ib, alpha, beta, C, ldc); break;
-    case 5: gemm_panels<5>(ctx, A, ia, B, ib, alpha, beta, C, ldc); break;
-    case 6: gemm_panels<6>(ctx, A, ia, B, ib, alpha, beta, C, ldc); break;
-    case 7: gemm_panels<7>(ctx, A, ia, B, ib, alpha, beta, C, ldc); break;
-    case 8: gemm_panels<8>(ctx, A, ia, B, ib, alpha, beta, C, ldc); break;
+    case 4: gemm_panels<4>(ctx, A, ia, B, ib, alpha, beta, C, Cdf, ldc); break;
+    case 5: gemm_panels<5>(ctx, A, ia, B, ib, alpha, beta, C, Cdf, ldc); break;
+    case 6: gemm_panels<6>(ctx, A, ia, B, ib, alpha, beta, C, Cdf, ldc); break;
+    case 7: gemm_panels<7>(ctx, A, ia, B, ib, alpha, beta, C, Cdf, ldc); break;
+    case 8: gemm_panels<8>(ctx, A, ia, B, ib, alpha, beta, C, Cdf, ldc); break;
     default: throw Error(GBCC_BAD_ARG, "emu_slices must be in [4, 8]");
   }
 }
@@ -982,7 +1104,7 @@ void run_emu_static(Context &ctx, bool ta, bool tb, int64_t M, int64_t N,
   constexpr int STAGE_BYTES = S * (A_TILE + B_TILE);
   constexpr int STAGES = (SMEM_BUDGET / STAGE_BYTES) > 4 ? 4 : (SMEM_BUDGET / STAGE_BYTES);
   const int smem = STAGES * STAGE_BYTES;
-  GBCC_CUDA(cudaFuncSetAttribute(emu_gemm_kernel<S>,
+  GBCC_CUDA(cudaFuncSetAttribute(emu_gemm_kernel<S, false>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
   EmuArgs args{};
   args.A = asl;
@@ -1003,7 +1125,7 @@ void run_emu_static(Context &ctx, bool ta, bool tb, int64_t M, int64_t N,
   args.os = out_scale(alpha);
   args.beta = beta;
   args.err = err;
-  emu_gemm_kernel<S><<<(unsigned)((int64_t)mt * nt), NUM_THREADS, smem, ctx.stream>>>(args);
+  emu_gemm_kernel<S, false><<<emu_grid(ctx, (int64_t)mt * nt), NUM_THREADS, smem, ctx.stream>>>(args);
   GBCC_CHECK_LAUNCH(ctx);
   int h = 0;
   GBCC_CUDA(cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, ctx.stream));

@@ -231,9 +231,13 @@ struct EmuPanels {
 };
 EmuPanels emu_split(Context &ctx, bool role_a, const double *base, int64_t R,
                     int64_t K, int64_t rs, int64_t ks, int count, int64_t pstride);
-// C[M,N] = alpha A_ia B_ib^T + beta C with M = A.rows, N = B.rows, K = A.K
+// C[M,N] = alpha A_ia B_ib^T + beta C with M = A.rows, N = B.rows, K = A.K.
+// With Cdf given, C is a float-float array instead (hi and lo rounded from
+// the exact fixed-point totals; alpha = +-2^k, beta in {0, 1}).
+struct df32;
 void emu_gemm_panels(Context &ctx, const EmuPanels &A, int ia, const EmuPanels &B,
-                     int ib, double alpha, double beta, double *C, int64_t ldc);
+                     int ib, double alpha, double beta, double *C, int64_t ldc,
+                     df32 *Cdf = nullptr);
 // emulated GEMM with its scratch in a fixed file-scope device array
 void gemm_emu_noalloc(Context &ctx, bool ta, bool tb, int64_t M, int64_t N,
                       int64_t K, double alpha, const double *A, int64_t lda,

@@ -12,17 +12,20 @@
 // one fused epilogue kernel per triple with a deterministic reduction.
 //
 // Precision mode: the two W products of every image are emulated-FP64 GEMMs
-// on digit panels split once per (T) call.  The epilogue stays in FP64 in
-// both modes: its terms cancel strongly, and rounding W or the epilogue
-// arithmetic to FP32 moved E_(T) by ~1e-9 relative at No=32, Nv=256.  The FP64
-// pipe of this GPU issues a few operations per clock per SM, so the epilogue
-// is written to need few of them (cycle-type regrouping of the spin/Fermi
-// weights, one division per element).
+// on digit panels split once per (T) call, written as float-float pairs
+// (hi + lo, ~48 bits) rounded from their exact fixed-point totals, and the
+// epilogue computes in float-float.  Its terms cancel strongly: rounding W or
+// the epilogue arithmetic to plain FP32 moved E_(T) by ~1e-9 relative at
+// No=32, Nv=256, far above 1 uHa.  Float-float keeps FP64-level accuracy
+// while running on the FP32 pipe; the FP64 pipe of this GPU issues a few
+// operations per clock per SM, so an FP64 epilogue costs as much as the
+// GEMMs.  FP64 mode runs the same kernel in double.
 
 #include <algorithm>
 #include <vector>
 
 #include "ccsd.hpp"
+#include "df32.hpp"
 
 namespace gbcc {
 namespace {
@@ -70,11 +73,35 @@ __device__ __forceinline__ int find_tile(const int (*tl)[3], int n, int c0, int 
   return j;
 }
 
-// per-thread sum of products (FMA chain)
+// Arithmetic of the epilogue type R: double in FP64 mode, float-float
+// (df32) in precision mode, where the FP32 pipe does the work.
+__device__ __forceinline__ double ar_add(double a, double b) { return a + b; }
+__device__ __forceinline__ double ar_sub(double a, double b) { return a - b; }
+__device__ __forceinline__ double ar_madd(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ double ar_scale(double a, float k) { return (double)k * a; }
+__device__ __forceinline__ double ar_div(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ double ar_to_double(double a) { return a; }
+__device__ __forceinline__ void ar_set(double &r, double x) { r = x; }
+__device__ __forceinline__ df32 ar_add(df32 a, df32 b) { return df_add(a, b); }
+__device__ __forceinline__ df32 ar_sub(df32 a, df32 b) { return df_sub(a, b); }
+__device__ __forceinline__ df32 ar_madd(df32 a, df32 b, df32 c) { return df_add(df_mul(a, b), c); }
+__device__ __forceinline__ df32 ar_scale(df32 a, float k) { return df_mulf(a, k); }
+__device__ __forceinline__ df32 ar_div(df32 a, df32 b) { return df_div(a, b); }
+__device__ __forceinline__ double ar_to_double(df32 a) { return df_to_double(a); }
+__device__ __forceinline__ void ar_set(df32 &r, double x) { r = df_from_double(x); }
+
+template <typename R>
+__device__ __forceinline__ R ar_zero() {
+  R r;
+  ar_set(r, 0.0);
+  return r;
+}
+
+// per-thread sum of products
 template <typename R> struct ProductSum {
-  R s = R(0);
-  __device__ void add(R x, R z) { s = fma(x, z, s); }
-  __device__ double value() const { return (double)s; }
+  R s = ar_zero<R>();
+  __device__ void add(R x, R z) { s = ar_madd(x, z, s); }
+  __device__ double value() const { return ar_to_double(s); }
 };
 
 // One CTA per orbit of 8^3 tiles under the six coordinate permutations.
@@ -87,110 +114,137 @@ template <typename R> struct ProductSum {
 // depends only on the cycle type: 8 for the identity (r = p), -4 for a
 // transposition (r of the other parity), 2 for a 3-cycle, so
 //   Z_p = 6 G_p + 2 G_same(p) - 4 G_other(p),   G_r = DV[x_r(y)],
-// where G_even / G_odd sum G_r over even / odd r: two FMAs per (p, y).
+// where G_even / G_odd sum G_r over even / odd r.
 // DV lives only in shared memory.  W_p tiles are read in natural order
 // (coalesced) and scattered into the permuted D.V positions; for a fixed p
-// the scatter is a bijection of the orbit onto itself.  R is the arithmetic
-// type (double).
+// the scatter is a bijection of the orbit onto itself.  Both permuted
+// shared-memory accesses (the scatter by pi_p and the read of x_r(y)) put
+// local coordinate z_k at stride OP^img[p][k], and move tile j to the orbit
+// tile jt[p][j]; these tables are built once per CTA.  R is the arithmetic
+// type: double, or float-float in precision mode.
 template <typename R>
 __global__ void __launch_bounds__(EPI_THREADS, 3) triples_orbit_kernel(EpiArgs a) {
   __shared__ R DV[6 * OT_WORDS];
   __shared__ double red[EPI_THREADS / 32];
+  __shared__ int s_jt[6][6];         // [p][j]: orbit tile of tile j moved by image p
+  __shared__ int s_ps[6][3];         // [p][k]: shared-memory stride of z_k under image p
+  __shared__ int s_org[6][3];        // first global coordinate of tile j
+  __shared__ int s_lim[6][3];        // valid extent of tile j per dimension
+  __shared__ int s_n;
   const int64_t Nv = a.Nv, No = a.No;
   const R *__restrict__ eps_p = static_cast<const R *>(a.eps_p);
   const R *__restrict__ T1h = static_cast<const R *>(a.T1h);
   const R *__restrict__ Vabij = static_cast<const R *>(a.Vabij);
-  const int rep[3] = {a.orbits[3 * blockIdx.x], a.orbits[3 * blockIdx.x + 1],
-                      a.orbits[3 * blockIdx.x + 2]};
-  int tl[6][3];
-  int n = 0;
-  for (int s = 0; s < 6; ++s) {
-    const int c0 = rep[a.img[s][0]], c1 = rep[a.img[s][1]], c2 = rep[a.img[s][2]];
-    bool seen = false;
-    for (int j = 0; j < n; ++j) seen |= (tl[j][0] == c0 && tl[j][1] == c1 && tl[j][2] == c2);
-    if (!seen) { tl[n][0] = c0; tl[n][1] = c1; tl[n][2] = c2; ++n; }
+  if (threadIdx.x == 0) {
+    const int rep[3] = {a.orbits[3 * blockIdx.x], a.orbits[3 * blockIdx.x + 1],
+                        a.orbits[3 * blockIdx.x + 2]};
+    int tl[6][3];
+    int n = 0;
+    for (int q = 0; q < 6; ++q) {
+      const int c0 = rep[a.img[q][0]], c1 = rep[a.img[q][1]], c2 = rep[a.img[q][2]];
+      bool seen = false;
+      for (int j = 0; j < n; ++j) seen |= (tl[j][0] == c0 && tl[j][1] == c1 && tl[j][2] == c2);
+      if (!seen) { tl[n][0] = c0; tl[n][1] = c1; tl[n][2] = c2; ++n; }
+    }
+    for (int j = 0; j < n; ++j)
+      for (int k = 0; k < 3; ++k) {
+        s_org[j][k] = tl[j][k] * OT;
+        const int64_t rest = Nv - (int64_t)tl[j][k] * OT;
+        s_lim[j][k] = rest < OT ? (int)rest : OT;
+      }
+    for (int q = 0; q < 6; ++q) {
+      for (int k = 0; k < 3; ++k) s_ps[q][k] = a.img[q][k] == 0 ? 1 : (a.img[q][k] == 1 ? OP : OP * OP);
+      for (int j = 0; j < n; ++j)
+        s_jt[q][j] = find_tile(tl, n, tl[j][a.dinv[q][0]], tl[j][a.dinv[q][1]], tl[j][a.dinv[q][2]]);
+    }
+    s_n = n;
   }
-  for (int i = threadIdx.x; i < 6 * OT_WORDS; i += EPI_THREADS) DV[i] = R(0);
+  for (int i = threadIdx.x; i < 6 * OT_WORDS; i += EPI_THREADS) DV[i] = ar_zero<R>();
   __syncthreads();
+  const int n = s_n;
+  // this thread's local coordinates: e = tid + 256 h, z0 fastest
+  int z0[EPI_PER], z1[EPI_PER], z2[EPI_PER];
+  int64_t zoff[EPI_PER];
+#pragma unroll
+  for (int h = 0; h < EPI_PER; ++h) {
+    const int e = threadIdx.x + EPI_THREADS * h;
+    z0[h] = e % OT;
+    z1[h] = (e / OT) % OT;
+    z2[h] = e / (OT * OT);
+    zoff[h] = z0[h] + Nv * (z1[h] + Nv * z2[h]);
+  }
   // pass 1: permuted sum of the six W_p
+#pragma unroll
   for (int p = 0; p < 6; ++p) {
     const R *__restrict__ W = static_cast<const R *>(a.W[p]);
-    const int d0 = a.dinv[p][0], d1 = a.dinv[p][1], d2 = a.dinv[p][2];
     R v[6][EPI_PER];
 #pragma unroll
     for (int j = 0; j < 6; ++j)
 #pragma unroll
       for (int h = 0; h < EPI_PER; ++h) {
-        v[j][h] = R(0);
-        if (j < n) {
-          const int e = threadIdx.x + EPI_THREADS * h;
-          const int64_t g0 = tl[j][0] * OT + e % OT, g1 = tl[j][1] * OT + (e / OT) % OT,
-                        g2 = tl[j][2] * OT + e / (OT * OT);
-          if (g0 < Nv && g1 < Nv && g2 < Nv) v[j][h] = W[g0 + Nv * (g1 + Nv * g2)];
-        }
+        v[j][h] = ar_zero<R>();
+        if (j < n && z0[h] < s_lim[j][0] && z1[h] < s_lim[j][1] && z2[h] < s_lim[j][2])
+          v[j][h] = W[s_org[j][0] + Nv * (s_org[j][1] + Nv * (int64_t)s_org[j][2]) + zoff[h]];
       }
+    const int ps0 = s_ps[p][0], ps1 = s_ps[p][1], ps2 = s_ps[p][2];
 #pragma unroll
     for (int j = 0; j < 6; ++j) {
       if (j >= n) break;
-      const int jt = find_tile(tl, n, tl[j][d0], tl[j][d1], tl[j][d2]);
+      const int base = s_jt[p][j] * OT_WORDS;
 #pragma unroll
       for (int h = 0; h < EPI_PER; ++h) {
-        const int e = threadIdx.x + EPI_THREADS * h;
-        const int z[3] = {e % OT, (e / OT) % OT, e / (OT * OT)};
-        R &t = DV[jt * OT_WORDS + z[d0] + OP * (z[d1] + OP * z[d2])];
-        t = t + v[j][h];
+        R &t = DV[base + z0[h] * ps0 + z1[h] * ps1 + z2[h] * ps2];
+        t = ar_add(t, v[j][h]);
       }
     }
     __syncthreads();
   }
-  const R ehs = (R)__dadd_rn(__dadd_rn(a.eps_h[a.i3[0]], a.eps_h[a.i3[1]]), a.eps_h[a.i3[2]]);
+  R ehs;
+  ar_set(ehs, __dadd_rn(__dadd_rn(a.eps_h[a.i3[0]], a.eps_h[a.i3[1]]), a.eps_h[a.i3[2]]));
   for (int j = 0; j < n; ++j)
-    for (int e = threadIdx.x; e < OT_ELEMS; e += EPI_THREADS) {
-      const int u0 = e % OT, u1 = (e / OT) % OT, u2 = e / (OT * OT);
-      const int64_t g0 = tl[j][0] * OT + u0, g1 = tl[j][1] * OT + u1, g2 = tl[j][2] * OT + u2;
-      R &t = DV[j * OT_WORDS + u0 + OP * (u1 + OP * u2)];
-      if (g0 < Nv && g1 < Nv && g2 < Nv) {
-        R den = ehs - eps_p[g0];
-        den = den - eps_p[g1];
-        den = den - eps_p[g2];
-        t = __ddiv_rn(t, den);
+#pragma unroll
+    for (int h = 0; h < EPI_PER; ++h) {
+      R &t = DV[j * OT_WORDS + z0[h] + OP * (z1[h] + OP * z2[h])];
+      if (z0[h] < s_lim[j][0] && z1[h] < s_lim[j][1] && z2[h] < s_lim[j][2]) {
+        R den = ar_sub(ehs, eps_p[s_org[j][0] + z0[h]]);
+        den = ar_sub(den, eps_p[s_org[j][1] + z1[h]]);
+        den = ar_sub(den, eps_p[s_org[j][2] + z2[h]]);
+        t = ar_div(t, den);
       } else {
-        t = R(0);
+        t = ar_zero<R>();
       }
     }
   __syncthreads();
   // pass 2: contraction with the spin/Fermi-weighted permutations of DV
   ProductSum<R> acc;
+#pragma unroll 1
   for (int j = 0; j < n; ++j) {
-    int jr[6];
-#pragma unroll
-    for (int r = 0; r < 6; ++r)
-      jr[r] = find_tile(tl, n, tl[j][a.rinv[r][0]], tl[j][a.rinv[r][1]], tl[j][a.rinv[r][2]]);
+    const int64_t gbase = s_org[j][0] + Nv * (s_org[j][1] + Nv * (int64_t)s_org[j][2]);
 #pragma unroll
     for (int h = 0; h < EPI_PER; ++h) {
-      const int e = threadIdx.x + EPI_THREADS * h;
-      const int z[3] = {e % OT, (e / OT) % OT, e / (OT * OT)};
-      const int64_t y0 = tl[j][0] * OT + z[0], y1 = tl[j][1] * OT + z[1], y2 = tl[j][2] * OT + z[2];
-      if (y0 >= Nv || y1 >= Nv || y2 >= Nv) continue;
-      const int64_t off = y0 + Nv * (y1 + Nv * y2);
+      if (z0[h] >= s_lim[j][0] || z1[h] >= s_lim[j][1] || z2[h] >= s_lim[j][2]) continue;
+      const int64_t y0 = s_org[j][0] + z0[h], y1 = s_org[j][1] + z1[h], y2 = s_org[j][2] + z2[h];
+      const int64_t off = gbase + zoff[h];
       R w[6];
 #pragma unroll
       for (int p = 0; p < 6; ++p)
-        w[p] = a.distinct[p] ? static_cast<const R *>(a.W[p])[off] : R(0);
-      R G[6], ge = R(0), go = R(0);
+        w[p] = a.distinct[p] ? static_cast<const R *>(a.W[p])[off] : ar_zero<R>();
+      R G[6], ge = ar_zero<R>(), go = ar_zero<R>();
 #pragma unroll
       for (int r = 0; r < 6; ++r) {
-        G[r] = DV[jr[r] * OT_WORDS + z[a.rinv[r][0]] + OP * (z[a.rinv[r][1]] + OP * z[a.rinv[r][2]])];
-        if (a.odd[r]) go = go + G[r];
-        else ge = ge + G[r];
+        G[r] = DV[s_jt[r][j] * OT_WORDS + z0[h] * s_ps[r][0] + z1[h] * s_ps[r][1] +
+                  z2[h] * s_ps[r][2]];
+        if (a.odd[r]) go = ar_add(go, G[r]);
+        else ge = ar_add(ge, G[r]);
       }
-      const R ze = R(2) * ge - R(4) * go, zo = R(2) * go - R(4) * ge;
+      const R ze = ar_sub(ar_scale(ge, 2.0f), ar_scale(go, 4.0f));
+      const R zo = ar_sub(ar_scale(go, 2.0f), ar_scale(ge, 4.0f));
 #pragma unroll
       for (int p = 0; p < 6; ++p) {
         if (!a.distinct[p]) continue;
-        const R x = fma(T1h[y0 + Nv * a.m[p][0]],
-                        Vabij[y1 + Nv * (y2 + Nv * (a.m[p][1] + No * a.m[p][2]))], w[p]);
-        const R zz = fma(R(6), G[p], a.odd[p] ? zo : ze);
+        const R x = ar_madd(T1h[y0 + Nv * a.m[p][0]],
+                            Vabij[y1 + Nv * (y2 + Nv * (a.m[p][1] + No * a.m[p][2]))], w[p]);
+        const R zz = ar_add(ar_scale(G[p], 6.0f), a.odd[p] ? zo : ze);
         acc.add(x, zz);
       }
     }
@@ -207,13 +261,13 @@ __global__ void __launch_bounds__(EPI_THREADS, 3) triples_orbit_kernel(EpiArgs a
   }
 }
 
-// dst[i] = (R)(scale * src[i])
+// dst[i] = scale * src[i] in the epilogue type (scale a power of two)
 template <typename R>
 __global__ void scaled_copy_kernel(const double *__restrict__ src, int64_t n, double scale,
                                    R *__restrict__ dst) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
-    dst[i] = (R)(scale * src[i]);
+    ar_set(dst[i], scale * src[i]);
 }
 
 // out[t] = sum of partials[t][0..nb) ; one block per triple slot
@@ -239,8 +293,11 @@ __global__ void sum_rows_kernel(const double *__restrict__ partials, int nb,
 double triples_energy(Context &ctx, const CcsdInputs &I, const double *T1,
                       const double *T2, int precision) {
   const int64_t No = I.No, Nv = I.Nv;
+  // Precision mode: W is produced as float-float by the emulated GEMMs and the
+  // epilogue computes in float-float; FP64 mode computes in double.  Both
+  // element types are 8 bytes.
   const bool emu = precision == GBCC_PREC_EMU;
-  using R = double;  // epilogue arithmetic type
+  static_assert(sizeof(df32) == sizeof(double), "epilogue element size");
   // Wvv[d,b,c,k] = sum_F Gab[F,b,d] Gai[F,c,k]
   OTen Wvv(ctx, {Nv, Nv, Nv, No});
   contract(ctx, 1.0, I.Gab, "Fbd", I.Gai, "Fck", 0.0, Wvv, "dbck", precision);
@@ -249,12 +306,27 @@ double triples_energy(Context &ctx, const CcsdInputs &I, const double *T1,
   assign(ctx, 1.0, I.Vijka, "jklc", 0.0, Vt, "lcjk");
   const int64_t n3 = Nv * Nv * Nv;
   std::vector<DBuf> Wb(6);
-  for (auto &b : Wb) b.alloc(ctx, sizeof(R) * n3);
-  // T1 / 2 (exact scaling)
-  DBuf t1h(ctx, sizeof(R) * Nv * No);
-  scaled_copy_kernel<R><<<(unsigned)((Nv * No + 255) / 256), 256, 0, ctx.stream>>>(
-      T1, Nv * No, 0.5, t1h.as<R>());
-  GBCC_CHECK_LAUNCH(ctx);
+  for (auto &b : Wb) b.alloc(ctx, 8 * n3);
+  // epilogue operands in the epilogue type: T1 / 2 (exact scaling), and in
+  // precision mode float-float copies of eps_p and Vabij
+  const int64_t nv4 = Nv * Nv * No * No;
+  auto convert = [&](const double *src, int64_t n, double scale, void *dst) {
+    const unsigned g = (unsigned)std::min<int64_t>((n + 255) / 256, 8192);
+    if (emu)
+      scaled_copy_kernel<df32><<<g, 256, 0, ctx.stream>>>(src, n, scale, static_cast<df32 *>(dst));
+    else
+      scaled_copy_kernel<double><<<g, 256, 0, ctx.stream>>>(src, n, scale,
+                                                            static_cast<double *>(dst));
+    GBCC_CHECK_LAUNCH(ctx);
+  };
+  DBuf t1h(ctx, 8 * Nv * No), epsr, vr;
+  convert(T1, Nv * No, 0.5, t1h.as<void>());
+  if (emu) {
+    epsr.alloc(ctx, 8 * Nv);
+    vr.alloc(ctx, 8 * nv4);
+    convert(I.eps_p.p(), Nv, 1.0, epsr.as<void>());
+    convert(I.Vabij.p(), nv4, 1.0, vr.as<void>());
+  }
   int img[6][3];
   for (int p = 0; p < 6; ++p) perm3(p, img[p]);
   EpiArgs base{};
@@ -269,9 +341,9 @@ double triples_energy(Context &ctx, const CcsdInputs &I, const double *T1,
     base.odd[p] = inversions & 1;
   }
   base.eps_h = I.eps_h.p();
-  base.eps_p = I.eps_p.p();
+  base.eps_p = emu ? epsr.as<void>() : static_cast<const void *>(I.eps_p.p());
   base.T1h = t1h.as<void>();
-  base.Vabij = I.Vabij.p();
+  base.Vabij = emu ? vr.as<void>() : static_cast<const void *>(I.Vabij.p());
   base.Nv = Nv;
   base.No = No;
   // orbit representatives A <= B <= C of the 8^3 tiles
@@ -327,13 +399,17 @@ double triples_energy(Context &ctx, const CcsdInputs &I, const double *T1,
           }
           a.distinct[p] = 1;
           a.W[p] = Wb[p].as<void>();
-          double *Wp = Wb[p].as<double>();
           if (emu) {
-            emu_gemm_panels(ctx, At, (int)(m[0] + No * m[1]), Bw, m[2], 1.0, 0.0, Wp, Nv);
-            emu_gemm_panels(ctx, Ah, m[0], Bh, (int)(m[1] + No * m[2]), -1.0, 1.0, Wp,
-                            Nv * Nv);
+            // the short-K hole product first (beta = 0: no read of W), then the
+            // particle product accumulates, its C reads hidden behind K = Nv
+            df32 *Wp = Wb[p].as<df32>();
+            emu_gemm_panels(ctx, Ah, m[0], Bh, (int)(m[1] + No * m[2]), -1.0, 0.0, nullptr,
+                            Nv * Nv, Wp);
+            emu_gemm_panels(ctx, At, (int)(m[0] + No * m[1]), Bw, m[2], 1.0, 1.0, nullptr, Nv,
+                            Wp);
             continue;
           }
+          double *Wp = Wb[p].as<double>();
           // W[a,(b,c)] = sum_d T2[a,d,m0,m1] Wvv[d,(b,c),m2]
           gemm(ctx, false, false, Nv, Nv * Nv, Nv, 1.0,
                T2 + Nv * Nv * (m[0] + No * m[1]), Nv, Wvv.p() + n3 * m[2], Nv,
@@ -345,7 +421,10 @@ double triples_energy(Context &ctx, const CcsdInputs &I, const double *T1,
                0, 0, 0, precision);
         }
         a.partials = partials.as<double>() + (int64_t)nb * t;
-        triples_orbit_kernel<R><<<nb, EPI_THREADS, 0, ctx.stream>>>(a);
+        if (emu)
+          triples_orbit_kernel<df32><<<nb, EPI_THREADS, 0, ctx.stream>>>(a);
+        else
+          triples_orbit_kernel<double><<<nb, EPI_THREADS, 0, ctx.stream>>>(a);
         GBCC_CHECK_LAUNCH(ctx);
       }
   sum_rows_kernel<<<(unsigned)ntrip, 256, 0, ctx.stream>>>(partials.as<double>(), nb,
