@@ -90,6 +90,13 @@ __device__ __forceinline__ df32 ar_div(df32 a, df32 b) { return df_div(a, b); }
 __device__ __forceinline__ double ar_to_double(df32 a) { return df_to_double(a); }
 __device__ __forceinline__ void ar_set(df32 &r, double x) { r = df_from_double(x); }
 
+__device__ __forceinline__ double ar_shfl_down(double v, int o) {
+  return __shfl_down_sync(0xffffffffu, v, o);
+}
+__device__ __forceinline__ df32 ar_shfl_down(df32 v, int o) {
+  return df_make(__shfl_down_sync(0xffffffffu, v.hi, o), __shfl_down_sync(0xffffffffu, v.lo, o));
+}
+
 template <typename R>
 __device__ __forceinline__ R ar_zero() {
   R r;
@@ -123,14 +130,17 @@ template <typename R> struct ProductSum {
 // tile jt[p][j]; these tables are built once per CTA.  R is the arithmetic
 // type: double, or float-float in precision mode.
 template <typename R>
-__global__ void __launch_bounds__(EPI_THREADS, 3) triples_orbit_kernel(EpiArgs a) {
+__global__ void __launch_bounds__(EPI_THREADS, 4) triples_orbit_kernel(EpiArgs a) {
   __shared__ R DV[6 * OT_WORDS];
-  __shared__ double red[EPI_THREADS / 32];
   __shared__ int s_jt[6][6];         // [p][j]: orbit tile of tile j moved by image p
   __shared__ int s_ps[6][3];         // [p][k]: shared-memory stride of z_k under image p
   __shared__ int s_org[6][3];        // first global coordinate of tile j
   __shared__ int s_lim[6][3];        // valid extent of tile j per dimension
-  __shared__ int s_n;
+  __shared__ int64_t s_gbase[6];     // global offset of the first element of tile j
+  __shared__ const R *s_W[6];        // W_p
+  __shared__ int64_t s_t1[6], s_v[6];  // offsets of T1h[:, m0] and Vabij[:, :, m1, m2]
+  __shared__ int s_dist[6], s_odd[6], s_n;
+  __shared__ R s_ehs;                // eps_i + eps_j + eps_k
   const int64_t Nv = a.Nv, No = a.No;
   const R *__restrict__ eps_p = static_cast<const R *>(a.eps_p);
   const R *__restrict__ T1h = static_cast<const R *>(a.T1h);
@@ -146,45 +156,45 @@ __global__ void __launch_bounds__(EPI_THREADS, 3) triples_orbit_kernel(EpiArgs a
       for (int j = 0; j < n; ++j) seen |= (tl[j][0] == c0 && tl[j][1] == c1 && tl[j][2] == c2);
       if (!seen) { tl[n][0] = c0; tl[n][1] = c1; tl[n][2] = c2; ++n; }
     }
-    for (int j = 0; j < n; ++j)
+    for (int j = 0; j < n; ++j) {
       for (int k = 0; k < 3; ++k) {
         s_org[j][k] = tl[j][k] * OT;
         const int64_t rest = Nv - (int64_t)tl[j][k] * OT;
         s_lim[j][k] = rest < OT ? (int)rest : OT;
       }
+      s_gbase[j] = s_org[j][0] + Nv * (s_org[j][1] + Nv * (int64_t)s_org[j][2]);
+    }
     for (int q = 0; q < 6; ++q) {
       for (int k = 0; k < 3; ++k) s_ps[q][k] = a.img[q][k] == 0 ? 1 : (a.img[q][k] == 1 ? OP : OP * OP);
       for (int j = 0; j < n; ++j)
         s_jt[q][j] = find_tile(tl, n, tl[j][a.dinv[q][0]], tl[j][a.dinv[q][1]], tl[j][a.dinv[q][2]]);
+      s_W[q] = static_cast<const R *>(a.W[q]);
+      s_t1[q] = Nv * a.m[q][0];
+      s_v[q] = Nv * Nv * (a.m[q][1] + No * a.m[q][2]);
+      s_dist[q] = a.distinct[q];
+      s_odd[q] = a.odd[q];
     }
     s_n = n;
+    ar_set(s_ehs, __dadd_rn(__dadd_rn(a.eps_h[a.i3[0]], a.eps_h[a.i3[1]]), a.eps_h[a.i3[2]]));
   }
   for (int i = threadIdx.x; i < 6 * OT_WORDS; i += EPI_THREADS) DV[i] = ar_zero<R>();
   __syncthreads();
   const int n = s_n;
-  // this thread's local coordinates: e = tid + 256 h, z0 fastest
-  int z0[EPI_PER], z1[EPI_PER], z2[EPI_PER];
-  int64_t zoff[EPI_PER];
-#pragma unroll
-  for (int h = 0; h < EPI_PER; ++h) {
-    const int e = threadIdx.x + EPI_THREADS * h;
-    z0[h] = e % OT;
-    z1[h] = (e / OT) % OT;
-    z2[h] = e / (OT * OT);
-    zoff[h] = z0[h] + Nv * (z1[h] + Nv * z2[h]);
-  }
-  // pass 1: permuted sum of the six W_p
-#pragma unroll
+  // pass 1: permuted sum of the six W_p; this thread's local coordinates are
+  // e = tid + 256 h, z0 fastest
+#pragma unroll 1
   for (int p = 0; p < 6; ++p) {
-    const R *__restrict__ W = static_cast<const R *>(a.W[p]);
+    const R *__restrict__ W = s_W[p];
     R v[6][EPI_PER];
 #pragma unroll
     for (int j = 0; j < 6; ++j)
 #pragma unroll
       for (int h = 0; h < EPI_PER; ++h) {
+        const int e = threadIdx.x + EPI_THREADS * h;
+        const int z0 = e % OT, z1 = (e / OT) % OT, z2 = e / (OT * OT);
         v[j][h] = ar_zero<R>();
-        if (j < n && z0[h] < s_lim[j][0] && z1[h] < s_lim[j][1] && z2[h] < s_lim[j][2])
-          v[j][h] = W[s_org[j][0] + Nv * (s_org[j][1] + Nv * (int64_t)s_org[j][2]) + zoff[h]];
+        if (j < n && z0 < s_lim[j][0] && z1 < s_lim[j][1] && z2 < s_lim[j][2])
+          v[j][h] = W[s_gbase[j] + z0 + Nv * (z1 + Nv * z2)];
       }
     const int ps0 = s_ps[p][0], ps1 = s_ps[p][1], ps2 = s_ps[p][2];
 #pragma unroll
@@ -193,22 +203,24 @@ __global__ void __launch_bounds__(EPI_THREADS, 3) triples_orbit_kernel(EpiArgs a
       const int base = s_jt[p][j] * OT_WORDS;
 #pragma unroll
       for (int h = 0; h < EPI_PER; ++h) {
-        R &t = DV[base + z0[h] * ps0 + z1[h] * ps1 + z2[h] * ps2];
+        const int e = threadIdx.x + EPI_THREADS * h;
+        R &t = DV[base + (e % OT) * ps0 + ((e / OT) % OT) * ps1 + (e / (OT * OT)) * ps2];
         t = ar_add(t, v[j][h]);
       }
     }
     __syncthreads();
   }
-  R ehs;
-  ar_set(ehs, __dadd_rn(__dadd_rn(a.eps_h[a.i3[0]], a.eps_h[a.i3[1]]), a.eps_h[a.i3[2]]));
+  const R ehs = s_ehs;
   for (int j = 0; j < n; ++j)
 #pragma unroll
     for (int h = 0; h < EPI_PER; ++h) {
-      R &t = DV[j * OT_WORDS + z0[h] + OP * (z1[h] + OP * z2[h])];
-      if (z0[h] < s_lim[j][0] && z1[h] < s_lim[j][1] && z2[h] < s_lim[j][2]) {
-        R den = ar_sub(ehs, eps_p[s_org[j][0] + z0[h]]);
-        den = ar_sub(den, eps_p[s_org[j][1] + z1[h]]);
-        den = ar_sub(den, eps_p[s_org[j][2] + z2[h]]);
+      const int e = threadIdx.x + EPI_THREADS * h;
+      const int z0 = e % OT, z1 = (e / OT) % OT, z2 = e / (OT * OT);
+      R &t = DV[j * OT_WORDS + z0 + OP * (z1 + OP * z2)];
+      if (z0 < s_lim[j][0] && z1 < s_lim[j][1] && z2 < s_lim[j][2]) {
+        R den = ar_sub(ehs, eps_p[s_org[j][0] + z0]);
+        den = ar_sub(den, eps_p[s_org[j][1] + z1]);
+        den = ar_sub(den, eps_p[s_org[j][2] + z2]);
         t = ar_div(t, den);
       } else {
         t = ar_zero<R>();
@@ -218,46 +230,41 @@ __global__ void __launch_bounds__(EPI_THREADS, 3) triples_orbit_kernel(EpiArgs a
   // pass 2: contraction with the spin/Fermi-weighted permutations of DV
   ProductSum<R> acc;
 #pragma unroll 1
-  for (int j = 0; j < n; ++j) {
-    const int64_t gbase = s_org[j][0] + Nv * (s_org[j][1] + Nv * (int64_t)s_org[j][2]);
+  for (int jh = 0; jh < n * EPI_PER; ++jh) {
+    const int j = jh / EPI_PER, e = threadIdx.x + EPI_THREADS * (jh % EPI_PER);
+    const int z0 = e % OT, z1 = (e / OT) % OT, z2 = e / (OT * OT);
+    if (z0 >= s_lim[j][0] || z1 >= s_lim[j][1] || z2 >= s_lim[j][2]) continue;
+    const int64_t y0 = s_org[j][0] + z0;
+    const int64_t y12 = (s_org[j][1] + z1) + Nv * (int64_t)(s_org[j][2] + z2);
+    const int64_t off = s_gbase[j] + z0 + Nv * (z1 + Nv * z2);
+    R G[6], ge = ar_zero<R>(), go = ar_zero<R>();
 #pragma unroll
-    for (int h = 0; h < EPI_PER; ++h) {
-      if (z0[h] >= s_lim[j][0] || z1[h] >= s_lim[j][1] || z2[h] >= s_lim[j][2]) continue;
-      const int64_t y0 = s_org[j][0] + z0[h], y1 = s_org[j][1] + z1[h], y2 = s_org[j][2] + z2[h];
-      const int64_t off = gbase + zoff[h];
-      R w[6];
+    for (int r = 0; r < 6; ++r) {
+      G[r] = DV[s_jt[r][j] * OT_WORDS + z0 * s_ps[r][0] + z1 * s_ps[r][1] + z2 * s_ps[r][2]];
+      if (s_odd[r]) go = ar_add(go, G[r]);
+      else ge = ar_add(ge, G[r]);
+    }
+    const R ze = ar_sub(ar_scale(ge, 2.0f), ar_scale(go, 4.0f));
+    const R zo = ar_sub(ar_scale(go, 2.0f), ar_scale(ge, 4.0f));
 #pragma unroll
-      for (int p = 0; p < 6; ++p)
-        w[p] = a.distinct[p] ? static_cast<const R *>(a.W[p])[off] : ar_zero<R>();
-      R G[6], ge = ar_zero<R>(), go = ar_zero<R>();
-#pragma unroll
-      for (int r = 0; r < 6; ++r) {
-        G[r] = DV[s_jt[r][j] * OT_WORDS + z0[h] * s_ps[r][0] + z1[h] * s_ps[r][1] +
-                  z2[h] * s_ps[r][2]];
-        if (a.odd[r]) go = ar_add(go, G[r]);
-        else ge = ar_add(ge, G[r]);
-      }
-      const R ze = ar_sub(ar_scale(ge, 2.0f), ar_scale(go, 4.0f));
-      const R zo = ar_sub(ar_scale(go, 2.0f), ar_scale(ge, 4.0f));
-#pragma unroll
-      for (int p = 0; p < 6; ++p) {
-        if (!a.distinct[p]) continue;
-        const R x = ar_madd(T1h[y0 + Nv * a.m[p][0]],
-                            Vabij[y1 + Nv * (y2 + Nv * (a.m[p][1] + No * a.m[p][2]))], w[p]);
-        const R zz = ar_add(ar_scale(G[p], 6.0f), a.odd[p] ? zo : ze);
-        acc.add(x, zz);
-      }
+    for (int p = 0; p < 6; ++p) {
+      if (!s_dist[p]) continue;
+      const R x = ar_madd(T1h[y0 + s_t1[p]], Vabij[y12 + s_v[p]], s_W[p][off]);
+      const R zz = ar_add(ar_scale(G[p], 6.0f), s_odd[p] ? zo : ze);
+      acc.add(x, zz);
     }
   }
-  double sum = acc.value();
-  for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
+  // block sum in the epilogue type; one conversion to double per CTA
+  __shared__ R red[EPI_THREADS / 32];
+  R sum = acc.s;
+  for (int o = 16; o > 0; o >>= 1) sum = ar_add(sum, ar_shfl_down(sum, o));
   const int wi = threadIdx.x / 32, ln = threadIdx.x % 32;
   if (ln == 0) red[wi] = sum;
   __syncthreads();
   if (threadIdx.x < 32) {
-    double r = (threadIdx.x < EPI_THREADS / 32) ? red[threadIdx.x] : 0.0;
-    for (int o = 16; o > 0; o >>= 1) r += __shfl_down_sync(0xffffffffu, r, o);
-    if (threadIdx.x == 0) a.partials[blockIdx.x] = r;
+    R r = (threadIdx.x < EPI_THREADS / 32) ? red[threadIdx.x] : ar_zero<R>();
+    for (int o = 16; o > 0; o >>= 1) r = ar_add(r, ar_shfl_down(r, o));
+    if (threadIdx.x == 0) a.partials[blockIdx.x] = ar_to_double(r);
   }
 }
 
