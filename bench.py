@@ -229,6 +229,10 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=32)
     ap.add_argument("--serve-single", type=int, default=4)
     ap.add_argument("--serve-slots", type=int, default=8)
+    ap.add_argument("--no-triples", action="store_true",
+                    help="skip the (T) correction on the final amplitudes")
+    ap.add_argument("--triples-fp64", action="store_true",
+                    help="also run the FP64 (T) for dE_(T) (minutes at the default size)")
     args = ap.parse_args()
     ws, rank, local, pg = dist_init()
     if args.impl == "reference":
@@ -285,6 +289,25 @@ def main():
     ctx.profile(False)
     prof_ms = p0.elapsed_time(p1)
     gs = ctx.gemm_stats()
+
+    # ---- (T) on the final amplitudes: precision mode, optionally FP64
+    triples = None
+    if not args.no_triples:
+        No = W["No"]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e_t, _ = sol.triples("emu")
+        t_emu = time.perf_counter() - t0
+        triples = {"seconds": t_emu, "e_t": e_t,
+                   "hole_triples": No * (No + 1) * (No + 2) // 6,
+                   "precision": "emulated fp64 GEMMs, float-float epilogue",
+                   "amplitudes": "after %d iterations" % (total_it + 2)}
+        if args.triples_fp64:
+            t0 = time.perf_counter()
+            e_t64, _ = sol.triples("fp64")
+            t64 = time.perf_counter() - t0
+            triples.update(fp64_seconds=t64, e_t_fp64=e_t64, dE_t_ha=e_t - e_t64,
+                           speedup=t64 / t_emu)
     sol.close()
     value = ws * args.steps / (ms / 1e3)
 
@@ -364,7 +387,7 @@ def main():
                                precision="emulated fp64, %d bf16 digits" % args.slices,
                                l2="inputs larger than L2 (T2, V, Gamma >= 0.5 GB)"),
                 "fp64": fp64, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
-                "serving": serving,
+                "serving": serving, "triples": triples,
                 "gpu_launches": launches,
                 "fp64_equiv_tflops_per_step": fl / args.steps / (ms / args.steps / 1e3) / 1e12,
                 "clocks": clk.summary()}

@@ -635,50 +635,63 @@ __device__ __forceinline__ long long to_fixed(double x, int e, int F) {
   return (bits >> 63) ? -X : X;
 }
 
+// bf16 bits of a small integer v (|v| <= 2^8: exact in bf16), FP32-pipe
+// and integer instructions only: the magic-number add makes the float v
+// exactly, and its upper 16 bits are the bf16 encoding.
+__device__ __forceinline__ uint32_t small_int_bf16_bits(int v) {
+  const float f = __int_as_float(0x4B400000 + v) - 12582912.0f;  // 1.5 * 2^23
+  return __float_as_uint(f) >> 16;
+}
+
 // digits of one operand into tiles [S][rt][kt] of TR rows x 32 k.
 // One thread writes one 16-byte core-matrix row (8 consecutive k) per digit.
+// The balanced digits come straight from Y = X + B, B = sum_{s>=1} 64 *
+// 128^(S-1-s): d_s = ((Y >> 7(S-1-s)) & 127) - 64 for s >= 1 and
+// d_0 = Y >> 7(S-1), the unique representation with d_s in [-64, 63].
+// Index arithmetic is 32-bit (the host checks the segment count).
 template <int S, int TR>
 __global__ void split_kernel(const double *__restrict__ base, int64_t R,
                              int64_t K, int64_t rs, int64_t ks,
                              const int *__restrict__ e, int rt, int kt,
                              __nv_bfloat16 *__restrict__ out) {
-  const int64_t segs = (int64_t)rt * TR * kt * (KB / 8);  // 16-byte segments per digit
-  const int64_t tile_elems = (int64_t)TR * KB;
-  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < segs;
-       idx += (int64_t)gridDim.x * blockDim.x) {
+  const unsigned rows = (unsigned)rt * TR;
+  const unsigned segs = rows * (unsigned)kt * (KB / 8);  // 16-byte segments per digit
+  constexpr unsigned tile_elems = TR * KB;
+  const int64_t plane = (int64_t)rt * kt * tile_elems;
+  long long bias = 0;
+#pragma unroll
+  for (int s = 1; s < S; ++s) bias += 64LL << (7 * (S - 1 - s));
+  for (unsigned idx = blockIdx.x * blockDim.x + threadIdx.x; idx < segs;
+       idx += gridDim.x * blockDim.x) {
     // idx -> (row r in [0, rt*TR), k-group kg in [0, kt*4)) with r fastest
-    const int64_t r = idx % ((int64_t)rt * TR);
-    const int64_t kg = idx / ((int64_t)rt * TR);
-    const int64_t tr = r / TR, rr = r % TR;
-    const int64_t tk = kg / (KB / 8), kk = kg % (KB / 8);
+    const unsigned kg = idx / rows, r = idx - kg * rows;
+    const unsigned tr = r / TR, rr = r % TR;
+    const unsigned tk = kg / (KB / 8), kk = kg % (KB / 8);
     // destination offset (elements) inside the digit plane
-    const int64_t off = (tr * kt + tk) * tile_elems +
+    const int64_t off = ((int64_t)tr * kt + tk) * tile_elems +
                         ((rr / 8) * (KB / 8) + kk) * 64 + (rr % 8) * 8;
-    long long d[S][8];
     const int er = (r < R) ? e[r] : EXP_FLOOR - 1;
     const bool live = r < R && er >= EXP_FLOOR;  // rows below the floor are all zero
+    uint32_t packed[S][4];
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
-      const int64_t k = kg * 8 + j;
+      const int64_t k = (int64_t)kg * 8 + j;
       long long X = 0;
       if (live && k < K) X = to_fixed(base[r * rs + k * ks], er, 7 * S);
+      const long long Y = X + bias;
 #pragma unroll
-      for (int s = S - 1; s >= 1; --s) {
-        const long long q = ((X + 64) & 127) - 64;
-        d[s][j] = q;
-        X = (X - q) >> 7;
+      for (int s = 0; s < S; ++s) {
+        const int d = s == 0 ? (int)(Y >> (7 * (S - 1)))
+                             : (int)((Y >> (7 * (S - 1 - s))) & 127) - 64;
+        const uint32_t bits = small_int_bf16_bits(d);
+        if (j % 2 == 0) packed[s][j / 2] = bits;
+        else packed[s][j / 2] |= bits << 16;
       }
-      d[0][j] = X;
     }
-    const int64_t plane = (int64_t)rt * kt * tile_elems;
 #pragma unroll
-    for (int s = 0; s < S; ++s) {
-      __align__(16) __nv_bfloat16 v[8];
-#pragma unroll
-      for (int j = 0; j < 8; ++j) v[j] = __float2bfloat16_rn((float)d[s][j]);
+    for (int s = 0; s < S; ++s)
       *reinterpret_cast<uint4 *>(out + s * plane + off) =
-          *reinterpret_cast<const uint4 *>(v);
-    }
+          make_uint4(packed[s][0], packed[s][1], packed[s][2], packed[s][3]);
   }
 }
 
@@ -771,6 +784,7 @@ void run_emu(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
   exponents(A, M, ars, aks, ea.as<int>());
   exponents(B, N, brs, bks, eb.as<int>());
   auto grid_for = [&](int64_t segs) {
+    require(segs < (1LL << 31), "emulated GEMM: operand too large to split");
     int64_t g = (segs + 255) / 256;
     const int64_t cap = (int64_t)std::max(ctx.sm_count, 1) * 16;
     return (unsigned)std::max<int64_t>(1, std::min(g, cap));
@@ -848,6 +862,7 @@ void split_batch(Context &ctx, EmuPanels &P, const double *base, int64_t pstride
   const int64_t plane = (int64_t)P.rt * P.kt * TR * KB;  // elements per digit plane
   const int64_t K = P.K;
   auto grid_for = [&](int64_t segs) {
+    require(segs < (1LL << 31), "emulated GEMM: operand too large to split");
     int64_t g = (segs + 255) / 256;
     const int64_t cap = (int64_t)std::max(ctx.sm_count, 1) * 16;
     return (unsigned)std::max<int64_t>(1, std::min(g, cap));
@@ -1091,6 +1106,7 @@ void run_emu_static(Context &ctx, bool ta, bool tb, int64_t M, int64_t N,
   exponents(A, M, ars, aks, ea);
   exponents(B, N, brs, bks, eb);
   auto grid_for = [&](int64_t segs) {
+    require(segs < (1LL << 31), "emulated GEMM: operand too large to split");
     int64_t g = (segs + 255) / 256;
     const int64_t cap = (int64_t)std::max(ctx.sm_count, 1) * 16;
     return (unsigned)std::max<int64_t>(1, std::min(g, cap));
