@@ -11,80 +11,115 @@ namespace {
 
 constexpr int MAXD = 6;
 
+// dims of a permutation that are walked by block index (all but the one or
+// two handled inside a block); lengths and run counts fit 32 bits (checked)
 struct PermDesc {
   int nrest;
-  int64_t rlen[MAXD];
+  unsigned rlen[MAXD];
   int64_t rss[MAXD];  // src stride of rest dim
   int64_t rsd[MAXD];  // dst stride of rest dim
 };
 
-__device__ __forceinline__ void decompose(const PermDesc &d, int64_t r,
-                                          int64_t &so, int64_t &dof) {
+// dst = alpha src + beta dst with alpha / beta classified on the host, so
+// that only a real scaling or accumulation issues FP64 instructions
+enum : int { ALPHA_ONE = 0, ALPHA_NEG = 1, ALPHA_GEN = 2 };
+enum : int { BETA_ZERO = 0, BETA_ONE = 1, BETA_GEN = 2 };
+struct Scale {
+  int am, bm;
+  double alpha, beta;
+};
+
+Scale make_scale(double alpha, double beta) {
+  Scale s{};
+  s.alpha = alpha;
+  s.beta = beta;
+  s.am = alpha == 1.0 ? ALPHA_ONE : (alpha == -1.0 ? ALPHA_NEG : ALPHA_GEN);
+  s.bm = beta == 0.0 ? BETA_ZERO : (beta == 1.0 ? BETA_ONE : BETA_GEN);
+  return s;
+}
+
+// same roundings as alpha * s (+ beta * d) with __dmul_rn / __dadd_rn;
+// -s is the sign flip that __dmul_rn(-1, s) gives
+__device__ __forceinline__ double apply(const Scale &sc, double s, const double *dptr) {
+  double v;
+  if (sc.am == ALPHA_ONE) v = s;
+  else if (sc.am == ALPHA_NEG)
+    v = __longlong_as_double(__double_as_longlong(s) ^ (long long)0x8000000000000000ull);
+  else v = __dmul_rn(sc.alpha, s);
+  if (sc.bm == BETA_ZERO) return v;
+  const double o = (sc.bm == BETA_ONE) ? *dptr : __dmul_rn(sc.beta, *dptr);
+  return __dadd_rn(v, o);
+}
+
+// 32-bit decomposition of a block's rest index (64-bit integer division
+// costs FP64-pipe instructions on this GPU)
+__device__ __forceinline__ void decompose(const PermDesc &d, unsigned r, int64_t &so,
+                                          int64_t &dof) {
   so = 0;
   dof = 0;
   for (int k = 0; k < d.nrest; ++k) {
-    const int64_t q = r / d.rlen[k];
-    const int64_t c = r - q * d.rlen[k];
-    so += c * d.rss[k];
-    dof += c * d.rsd[k];
+    const unsigned q = r / d.rlen[k];
+    const unsigned c = r - q * d.rlen[k];
+    so += (int64_t)c * d.rss[k];
+    dof += (int64_t)c * d.rsd[k];
     r = q;
   }
 }
 
-__device__ __forceinline__ double combine(double alpha, double s, double beta,
-                                          const double *dptr) {
-  const double v = (alpha == 1.0) ? s : __dmul_rn(alpha, s);
-  if (beta == 0.0) return v;
-  const double o = (beta == 1.0) ? *dptr : __dmul_rn(beta, *dptr);
-  return __dadd_rn(v, o);
-}
-
 // src dim 0 is also dst dim 0: contiguous runs of length L0 on both sides.
-__global__ void perm_runs_kernel(const double *__restrict__ src,
-                                 double *__restrict__ dst, int64_t L0,
-                                 PermDesc d, double alpha, double beta) {
+// A block moves an X x Y tile: X elements of the run (threadIdx.x) times Y
+// consecutive indices of dim 1 (threadIdx.y; strides ss1 / sd1), with one
+// decomposition of the remaining dims per block.
+__global__ void perm_runs_kernel(const double *__restrict__ src, double *__restrict__ dst,
+                                 int L0, int X, int nx, int L1, int Y, int ny,
+                                 int64_t ss1, int64_t sd1, PermDesc d, Scale sc) {
   __shared__ int64_t base[2];
-  if (threadIdx.x == 0) decompose(d, blockIdx.x, base[0], base[1]);
+  unsigned b = blockIdx.x;
+  const unsigned xt = b % nx;
+  b /= nx;
+  const unsigned yt = b % ny;
+  const unsigned r = b / ny;
+  if (threadIdx.x == 0 && threadIdx.y == 0) decompose(d, r, base[0], base[1]);
   __syncthreads();
-  const int64_t so = base[0], dof = base[1];
-  for (int64_t x = (int64_t)blockIdx.y * blockDim.x + threadIdx.x; x < L0;
-       x += (int64_t)gridDim.y * blockDim.x) {
-    double *dp = dst + dof + x;
-    *dp = combine(alpha, src[so + x], beta, dp);
+  const int x0 = xt * X, x1 = min(L0, x0 + X);
+  const int y0 = yt * Y, y1 = min(L1, y0 + Y);
+  for (int y = y0 + threadIdx.y; y < y1; y += blockDim.y) {
+    const double *sp = src + base[0] + (int64_t)y * ss1;
+    double *dp = dst + base[1] + (int64_t)y * sd1;
+    for (int x = x0 + threadIdx.x; x < x1; x += blockDim.x) dp[x] = apply(sc, sp[x], dp + x);
   }
 }
 
 // src dim 0 (x) goes to dst stride sd0; src dim p (y, src stride ssp) becomes
-// the dst fastest dim.
+// the dst fastest dim: 32x32 shared tile, coalesced on both sides.
 __global__ void perm_tile_kernel(const double *__restrict__ src,
-                                 double *__restrict__ dst, int64_t L0,
-                                 int64_t Lp, int64_t ssp, int64_t sd0,
-                                 int64_t tiles_x, int64_t tiles_y, PermDesc d,
-                                 double alpha, double beta) {
+                                 double *__restrict__ dst, int L0,
+                                 int Lp, int64_t ssp, int64_t sd0,
+                                 int tiles_x, int tiles_y, PermDesc d, Scale sc) {
   __shared__ double tile[32][33];
   __shared__ int64_t base[2];
-  int64_t b = blockIdx.x;
-  const int64_t tx_ = b % tiles_x;
+  unsigned b = blockIdx.x;
+  const unsigned tx_ = b % tiles_x;
   b /= tiles_x;
-  const int64_t ty_ = b % tiles_y;
-  const int64_t r = b / tiles_y;
+  const unsigned ty_ = b % tiles_y;
+  const unsigned r = b / tiles_y;
   if (threadIdx.x == 0 && threadIdx.y == 0) decompose(d, r, base[0], base[1]);
   __syncthreads();
   const int64_t so = base[0], dof = base[1];
-  const int64_t x0 = tx_ * 32, y0 = ty_ * 32;
+  const int x0 = tx_ * 32, y0 = ty_ * 32;
   const int tx = threadIdx.x, ty = threadIdx.y;
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
-    const int64_t y = y0 + ty + 8 * k, x = x0 + tx;
-    if (x < L0 && y < Lp) tile[ty + 8 * k][tx] = src[so + x + y * ssp];
+    const int y = y0 + ty + 8 * k, x = x0 + tx;
+    if (x < L0 && y < Lp) tile[ty + 8 * k][tx] = src[so + x + (int64_t)y * ssp];
   }
   __syncthreads();
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
-    const int64_t x = x0 + ty + 8 * k, y = y0 + tx;
+    const int x = x0 + ty + 8 * k, y = y0 + tx;
     if (x < L0 && y < Lp) {
-      double *dp = dst + dof + y + x * sd0;
-      *dp = combine(alpha, tile[tx][ty + 8 * k], beta, dp);
+      double *dp = dst + dof + y + (int64_t)x * sd0;
+      *dp = apply(sc, tile[tx][ty + 8 * k], dp);
     }
   }
 }
@@ -167,43 +202,42 @@ void permute(Context &ctx, const Ten &src, const int *perm, double alpha,
   int pfast = 0;
   for (size_t k = 0; k < dims.size(); ++k)
     if (dims[k].sd < dims[pfast].sd) pfast = (int)k;
+  for (const Dim &dm : dims) require(dm.len < (1LL << 31), "permute: dimension too long");
+  const Scale sc = make_scale(alpha, beta);
   PermDesc d{};
+  auto add_rest = [&](const Dim &dm) {
+    d.rlen[d.nrest] = (unsigned)dm.len;
+    d.rss[d.nrest] = dm.ss;
+    d.rsd[d.nrest] = dm.sd;
+    d.nrest++;
+    return dm.len;
+  };
   if (pfast == 0 && dims[0].ss == 1 && dims[0].sd == 1) {
-    const int64_t L0 = dims[0].len;
+    const int L0 = (int)dims[0].len;
+    const Dim d1 = dims.size() > 1 ? dims[1] : Dim{1, 0, 0};
     int64_t R = 1;
-    d.nrest = 0;
-    for (size_t k = 1; k < dims.size(); ++k) {
-      d.rlen[d.nrest] = dims[k].len;
-      d.rss[d.nrest] = dims[k].ss;
-      d.rsd[d.nrest] = dims[k].sd;
-      d.nrest++;
-      R *= dims[k].len;
-    }
-    require(R < (1LL << 31), "permute: too many runs");
-    const int threads = L0 >= 256 ? 256 : (L0 >= 128 ? 128 : (L0 >= 64 ? 64 : 32));
-    int64_t gy = (L0 + threads - 1) / threads;
-    if (gy > 65535) gy = 65535;
-    dim3 grid((unsigned)R, (unsigned)gy);
-    perm_runs_kernel<<<grid, threads, 0, ctx.stream>>>(src.p, dst.p, L0, d,
-                                                       alpha, beta);
+    for (size_t k = 2; k < dims.size(); ++k) R *= add_rest(dims[k]);
+    // tile of X x Y elements per block, about 4096 elements
+    const int X = std::min(L0, 4096);
+    const int nx = (L0 + X - 1) / X;
+    const int L1 = (int)d1.len;
+    const int Y = (int)std::min<int64_t>(L1, std::max<int64_t>(1, 4096 / X));
+    const int ny = (L1 + Y - 1) / Y;
+    const int bx = X >= 256 ? 256 : (X >= 128 ? 128 : (X >= 64 ? 64 : 32));
+    const int by = 256 / bx;
+    require(R * nx * ny < (1LL << 31), "permute: too many blocks");
+    perm_runs_kernel<<<(unsigned)(R * nx * ny), dim3(bx, by), 0, ctx.stream>>>(
+        src.p, dst.p, L0, X, nx, L1, Y, ny, d1.ss, d1.sd, d, sc);
   } else {
     require(dims[0].ss == 1 && dims[pfast].sd == 1, "permute: stride logic");
-    const int64_t L0 = dims[0].len, Lp = dims[pfast].len;
+    const int L0 = (int)dims[0].len, Lp = (int)dims[pfast].len;
     int64_t R = 1;
-    d.nrest = 0;
-    for (size_t k = 1; k < dims.size(); ++k) {
-      if ((int)k == pfast) continue;
-      d.rlen[d.nrest] = dims[k].len;
-      d.rss[d.nrest] = dims[k].ss;
-      d.rsd[d.nrest] = dims[k].sd;
-      d.nrest++;
-      R *= dims[k].len;
-    }
-    const int64_t tx = (L0 + 31) / 32, ty = (Lp + 31) / 32;
-    require(tx * ty * R < (1LL << 31), "permute: grid too large");
-    perm_tile_kernel<<<(unsigned)(tx * ty * R), dim3(32, 8), 0, ctx.stream>>>(
-        src.p, dst.p, L0, Lp, dims[pfast].ss, dims[0].sd, tx, ty, d, alpha,
-        beta);
+    for (size_t k = 1; k < dims.size(); ++k)
+      if ((int)k != pfast) R *= add_rest(dims[k]);
+    const int tx = (L0 + 31) / 32, ty = (Lp + 31) / 32;
+    require((int64_t)tx * ty * R < (1LL << 31), "permute: grid too large");
+    perm_tile_kernel<<<(unsigned)((int64_t)tx * ty * R), dim3(32, 8), 0, ctx.stream>>>(
+        src.p, dst.p, L0, Lp, dims[pfast].ss, dims[0].sd, tx, ty, d, sc);
   }
   GBCC_CHECK_LAUNCH(ctx);
 }

@@ -1,0 +1,50 @@
+"""Times one (T) evaluation on a seeded synthetic system.
+
+    python -m sisi4s_gb300.triples_bench No Nv NG [--prec emu|fp64] [--reps R]
+
+The amplitudes are the MP2 amplitudes of the system (T1 = 0) plus a small
+seeded T1, so that every term of the (T) energy is exercised.  Prints one JSON
+line with the wall time of each repetition and E_(T).
+"""
+import argparse
+import json
+import time
+
+import numpy as np
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("No", type=int)
+    ap.add_argument("Nv", type=int)
+    ap.add_argument("NG", type=int)
+    ap.add_argument("--prec", default="emu", choices=["emu", "fp64"])
+    ap.add_argument("--reps", type=int, default=2)
+    ap.add_argument("--seed", type=int, default=1)
+    args = ap.parse_args()
+
+    import torch  # device synchronisation only
+
+    from . import capi
+    from . import ccsd as gpu
+    from .inputs import make_system, mp2_amplitudes
+
+    s = make_system(args.No, args.Nv, args.NG, args.seed)
+    T1, T2 = mp2_amplitudes(s)
+    T1 = T1 + 1e-3 * np.random.default_rng(args.seed + 1).normal(size=T1.shape)
+    ctx = capi.Context(0)
+    times, e_t = [], None
+    for _ in range(args.reps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e_t, _ = gpu.triples(ctx, s.eps_h, s.eps_p, s.gamma, T1, T2,
+                             precision=args.prec)
+        times.append(time.perf_counter() - t0)
+    print(json.dumps({"No": args.No, "Nv": args.Nv, "NG": args.NG,
+                      "precision": args.prec, "seconds": times, "e_t": e_t,
+                      "hole_triples": args.No * (args.No + 1) * (args.No + 2) // 6}))
+    ctx.close()
+
+
+if __name__ == "__main__":
+    main()
