@@ -76,6 +76,12 @@ gbcc_status gbcc_ctx_set_graphs(gbcc_ctx *ctx, int enable);
 gbcc_status gbcc_ctx_profile(gbcc_ctx *ctx, int enable);
 gbcc_status gbcc_ctx_gemm_stats(gbcc_ctx *ctx, double *ms, int64_t *launches,
                                 double *tc_flops, double *fp64_flops);
+/* Per-launch records behind those statistics (new in this library; sisi4s
+ * has per-step timers only): the M, N, K (3 values per launch, into mnk) and
+ * device milliseconds (into ms) of up to cap profiled GEMM launches, oldest
+ * first; *count receives the number written.  The records are cleared. */
+gbcc_status gbcc_ctx_gemm_records(gbcc_ctx *ctx, int64_t *mnk, double *ms, int64_t cap,
+                                  int64_t *count);
 
 /* ------------------------------------------------------------- CCSD input */
 /* Replaces ClusterSinglesDoublesAlgorithm::run<double> +

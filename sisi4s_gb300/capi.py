@@ -65,6 +65,8 @@ _SIGS = {
     "gbcc_ctx_set_graphs": (C.c_int, [C.c_void_p, C.c_int]),
     "gbcc_ctx_gemm_stats": (C.c_int, [C.c_void_p, _dp, C.POINTER(C.c_int64),
                                       _dp, _dp]),
+    "gbcc_ctx_gemm_records": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), _dp,
+                                        C.c_int64, C.POINTER(C.c_int64)]),
     "gbcc_ccsd_opts_default": (None, [C.POINTER(CcsdOpts)]),
     "gbcc_ccsd_solve": (C.c_int, [C.c_void_p, C.POINTER(CcsdIn),
                                   C.POINTER(CcsdOpts), C.POINTER(CcsdOut)]),
@@ -180,6 +182,16 @@ class Context:
                                                 C.byref(tc), C.byref(f64)))
         return {"ms": ms.value, "launches": n.value, "tc_flops": tc.value,
                 "fp64_flops": f64.value}
+
+    def gemm_records(self, cap=1 << 16):
+        """[(M, N, K, ms)] of the profiled GEMM launches since the last call."""
+        mnk = np.zeros(3 * cap, dtype=np.int64)
+        ms = np.zeros(cap)
+        n = C.c_int64()
+        self.check(self.lib.gbcc_ctx_gemm_records(
+            self.h, mnk.ctypes.data_as(C.POINTER(C.c_int64)), ptr(ms), cap, C.byref(n)))
+        return [(int(mnk[3 * i]), int(mnk[3 * i + 1]), int(mnk[3 * i + 2]), float(ms[i]))
+                for i in range(n.value)]
 
     @property
     def launches(self):

@@ -190,6 +190,25 @@ gbcc_status gbcc_ctx_gemm_stats(gbcc_ctx *ctx, double *ms, int64_t *launches,
   });
 }
 
+gbcc_status gbcc_ctx_gemm_records(gbcc_ctx *ctx, int64_t *mnk, double *ms, int64_t cap,
+                                  int64_t *count) {
+  if (!ctx || cap < 0 || (cap > 0 && (!mnk || !ms))) return GBCC_BAD_ARG;
+  return guard(ctx, [&]() {
+    ctx->c.prof_harvest();
+    auto &log = ctx->c.prof_log;
+    const int64_t n = std::min<int64_t>(cap, (int64_t)log.size());
+    for (int64_t i = 0; i < n; ++i) {
+      mnk[3 * i] = log[i].M;
+      mnk[3 * i + 1] = log[i].N;
+      mnk[3 * i + 2] = log[i].K;
+      ms[i] = log[i].ms;
+    }
+    if (count) *count = n;
+    log.clear();
+    return GBCC_OK;
+  });
+}
+
 void gbcc_ccsd_opts_default(gbcc_ccsd_opts *o) {
   if (!o) return;
   o->mixer = 0;

@@ -742,13 +742,31 @@ EmuPlan emu_plan(int S, int64_t M, int64_t N, int64_t K, int sm_count,
   int lg = 0;
   while ((1 << lg) < nchunks) ++lg;
   p.frac = std::min(FRAC, 38 - lg);
+  // K-split: the persistent grid of G CTAs runs ceil(units / G) rounds of
+  // cps chunks each; pick the split that minimises that, plus the cost of
+  // the split-total reduction (ks int64 partials per output), so that the
+  // last round of a few-tile GEMM is not mostly idle
   const int64_t ctas = (int64_t)p.mt * p.nt;
-  const int64_t want = 2LL * std::max(sm_count, 1);
-  int ks = 1;
-  if (allow_split && ctas < want && nchunks > 1)
-    ks = (int)std::min<int64_t>({(want + ctas - 1) / ctas, (int64_t)nchunks, 64});
-  const int cps = (nchunks + ks - 1) / ks;  // chunks per split
-  p.kb_per_split = cps * p.kc_blocks;
+  const int64_t G = std::max(sm_count, 1);
+  // one chunk of one tile: 21 * 2 * 128 * 64 * 512 bf16 flop at ~1.6 PF/s / G
+  const double chunk_s = (double)S * (S + 1) * 128.0 * 64.0 * p.kc_blocks * KB /
+                         (1.6e15 / (double)G);
+  int best_cps = nchunks;
+  double best_t = 1e300;
+  const int max_ks = allow_split ? std::min(nchunks, 64) : 1;
+  for (int ks = 1; ks <= max_ks; ++ks) {
+    const int cps = (nchunks + ks - 1) / ks;
+    const int kse = (nchunks + cps - 1) / cps;
+    if (kse != ks) continue;  // same split as a smaller ks
+    const double rounds = (double)((ctas * kse + G - 1) / G);
+    double t = rounds * cps * chunk_s;
+    if (kse > 1) t += 16.0 * (double)M * (double)N * (kse + 1) / 6.0e12;  // reduce
+    if (t < best_t * 0.97) {
+      best_t = t;
+      best_cps = cps;
+    }
+  }
+  p.kb_per_split = best_cps * p.kc_blocks;
   p.ksplit = (p.kt + p.kb_per_split - 1) / p.kb_per_split;
   return p;
 }
@@ -834,7 +852,7 @@ void run_emu(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
     // algorithmic tensor-core work of the scheme: S(S+1)/2 bf16 products of
     // the unpadded M x N x K problem
     const double f = 2.0 * (double)M * (double)N * (double)K;
-    ctx.prof_recs.push_back({ev0, ev1, f * S * (S + 1) / 2.0, f});
+    ctx.prof_recs.push_back({ev0, ev1, f * S * (S + 1) / 2.0, f, M, N, K});
   }
   if (P.ksplit > 1) {
     const int64_t n = M * N;
@@ -937,7 +955,7 @@ void gemm_panels(Context &ctx, const EmuPanels &A, int ia, const EmuPanels &B, i
   if (ctx.prof) {
     GBCC_CUDA(cudaEventRecord(ev1, ctx.stream));
     const double f = 2.0 * (double)M * (double)N * (double)K;
-    ctx.prof_recs.push_back({ev0, ev1, f * S * (S + 1) / 2.0, f});
+    ctx.prof_recs.push_back({ev0, ev1, f * S * (S + 1) / 2.0, f, M, N, K});
   }
   if (P.ksplit > 1) {
     const int64_t n = M * N;

@@ -183,6 +183,86 @@ void launch(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
   ctx.flops += 2.0 * (double)M * (double)N * (double)K * (double)batch;
 }
 
+// ------------------------------------------------------------------ GEMV
+// y[i] = alpha * sum_k A(i, k) x[k] + beta * y[i], FP64, deterministic.
+// A(i, k) = A[i * ars + k * aks], x[k] = x[k * incx], y[i] = y[i * incy].
+// The GEMV shapes of the CCSD iteration (one index of length 1) are bound by
+// the FP64 FMA pipe and HBM, not by tensor cores, so they stay in FP64.
+//
+// Rows contiguous in k (aks == 1): one warp per output, lanes stride over k,
+// shuffle reduction in a fixed order.
+__global__ void gemv_rows_kernel(int64_t Mo, int64_t K, double alpha,
+                                 const double *__restrict__ A, int64_t ars,
+                                 const double *__restrict__ x, int64_t incx,
+                                 double beta, double *__restrict__ y, int64_t incy) {
+  const int lane = threadIdx.x % 32;
+  for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32; i < Mo;
+       i += (int64_t)gridDim.x * blockDim.x / 32) {
+    const double *a = A + i * ars;
+    double s = 0.0;
+    for (int64_t k = lane; k < K; k += 32) s = fma(a[k], x[k * incx], s);
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane == 0) {
+      double v = alpha * s;
+      if (beta != 0.0) v = fma(beta, y[i * incy], v);
+      y[i * incy] = v;
+    }
+  }
+}
+
+// Outputs contiguous (ars == 1): threads over i (coalesced), blockIdx.y over
+// K-chunks; partials [kchunks][Mo] are summed in chunk order afterwards.
+__global__ void gemv_cols_kernel(int64_t Mo, int64_t K, int64_t kchunk,
+                                 const double *__restrict__ A, int64_t aks,
+                                 const double *__restrict__ x, int64_t incx,
+                                 double *__restrict__ part) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= Mo) return;
+  const int64_t k0 = (int64_t)blockIdx.y * kchunk, k1 = min(K, k0 + kchunk);
+  double s = 0.0;
+  for (int64_t k = k0; k < k1; ++k) s = fma(A[i + k * aks], x[k * incx], s);
+  part[(int64_t)blockIdx.y * Mo + i] = s;
+}
+
+__global__ void gemv_sum_kernel(int64_t Mo, int nparts, const double *__restrict__ part,
+                                double alpha, double beta, double *__restrict__ y,
+                                int64_t incy) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < Mo;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int c = 0; c < nparts; ++c) s += part[(int64_t)c * Mo + i];
+    double v = alpha * s;
+    if (beta != 0.0) v = fma(beta, y[i * incy], v);
+    y[i * incy] = v;
+  }
+}
+
+void gemv(Context &ctx, int64_t Mo, int64_t K, double alpha, const double *A,
+          int64_t ars, int64_t aks, const double *x, int64_t incx, double beta,
+          double *y, int64_t incy) {
+  const int64_t G = std::max(ctx.sm_count, 1);
+  if (aks == 1) {
+    const int64_t blocks = std::min<int64_t>((Mo * 32 + 255) / 256, G * 32);
+    gemv_rows_kernel<<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, ctx.stream>>>(
+        Mo, K, alpha, A, ars, x, incx, beta, y, incy);
+    GBCC_CHECK_LAUNCH(ctx);
+    return;
+  }
+  require(ars == 1, "gemv: one operand index must be contiguous");
+  const int64_t bx = (Mo + 255) / 256;
+  int64_t nch = std::max<int64_t>(1, std::min<int64_t>((G * 8 + bx - 1) / bx, (K + 63) / 64));
+  nch = std::min<int64_t>(nch, 65535);
+  const int64_t kchunk = (K + nch - 1) / nch;
+  nch = (K + kchunk - 1) / kchunk;
+  DBuf part(ctx, sizeof(double) * Mo * nch);
+  gemv_cols_kernel<<<dim3((unsigned)bx, (unsigned)nch), 256, 0, ctx.stream>>>(
+      Mo, K, kchunk, A, aks, x, incx, part.as<double>());
+  GBCC_CHECK_LAUNCH(ctx);
+  gemv_sum_kernel<<<(unsigned)std::min<int64_t>(bx, G * 8), 256, 0, ctx.stream>>>(
+      Mo, (int)nch, part.as<double>(), alpha, beta, y, incy);
+  GBCC_CHECK_LAUNCH(ctx);
+}
+
 }  // namespace
 
 void gemm_f64(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
@@ -215,6 +295,16 @@ void gemm(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
           int64_t ldb, double beta, double *C, int64_t ldc, int64_t batch,
           int64_t sA, int64_t sB, int64_t sC, int precision) {
   const double fl = 2.0 * (double)M * (double)N * (double)K * (double)batch;
+  if (batch == 1 && K > 0 && (M == 1 || N == 1)) {
+    // matrix-vector product: FP64 GEMV (both precision modes)
+    if (N == 1) {  // C[i,0] = sum_k op(A)(i,k) op(B)(k,0)
+      gemv(ctx, M, K, alpha, A, ta ? lda : 1, ta ? 1 : lda, B, tb ? ldb : 1, beta, C, 1);
+    } else {       // C[0,j] = sum_k op(B)(k,j) op(A)(0,k)
+      gemv(ctx, N, K, alpha, B, tb ? 1 : ldb, tb ? ldb : 1, A, ta ? 1 : lda, beta, C, ldc);
+    }
+    ctx.flops += fl;
+    return;
+  }
   if (precision == GBCC_PREC_EMU && K > 0 && fl >= ctx.emu_min_flops) {
     gemm_emu(ctx, ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, batch,
              sA, sB, sC);

@@ -90,8 +90,14 @@ struct Context {
   struct ProfRec {
     cudaEvent_t a, b;
     double tc_flops, fp64_flops;
+    int64_t M, N, K;
+  };
+  struct GemmLog {
+    int64_t M, N, K;
+    double ms;
   };
   std::vector<ProfRec> prof_recs;
+  std::vector<GemmLog> prof_log;  // per launch, until read through the ABI
   std::vector<cudaEvent_t> prof_pool;
   double prof_ms = 0, prof_tc_flops = 0, prof_fp64_flops = 0;
   int64_t prof_launches = 0;
@@ -111,6 +117,7 @@ struct Context {
       float ms = 0;
       cudaEventElapsedTime(&ms, r.a, r.b);
       prof_ms += ms;
+      if (prof_log.size() < (size_t)1 << 20) prof_log.push_back({r.M, r.N, r.K, (double)ms});
       prof_tc_flops += r.tc_flops;
       prof_fp64_flops += r.fp64_flops;
       prof_launches++;

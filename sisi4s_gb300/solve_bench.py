@@ -44,6 +44,10 @@ def main():
     ap.add_argument("--iterations", type=int, default=3)
     ap.add_argument("--no-triples", action="store_true")
     ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--slices", type=int, default=6,
+                    help="bf16 digits per operand in precision mode")
+    ap.add_argument("--emu-only", action="store_true",
+                    help="skip the FP64 run (compare against a recorded one)")
     args = ap.parse_args()
 
     from . import capi
@@ -51,14 +55,19 @@ def main():
 
     s = make_system(args.No, args.Nv, args.NG, args.seed)
     ctx = capi.Context(0)
+    ctx.set_emulation(args.slices, 1e7)
     trip = not args.no_triples
     emu = run(ctx, s, "emu", args.iterations, trip)
-    f64 = run(ctx, s, "fp64", args.iterations, trip)
     line = {"No": args.No, "Nv": args.Nv, "NG": args.NG, "seed": args.seed,
             "iterations": args.iterations, "mixer": "DiisMixer(5), MP2 start",
-            "emu": emu, "fp64": f64,
-            "dE_ccsd_ha": emu["energy"] - f64["energy"],
-            "speedup_iteration": f64["seconds_per_iteration"] / emu["seconds_per_iteration"]}
+            "slices": args.slices, "emu": emu}
+    if args.emu_only:
+        print(json.dumps(line), flush=True)
+        ctx.close()
+        return
+    f64 = run(ctx, s, "fp64", args.iterations, trip)
+    line.update(fp64=f64, dE_ccsd_ha=emu["energy"] - f64["energy"],
+                speedup_iteration=f64["seconds_per_iteration"] / emu["seconds_per_iteration"])
     if trip:
         line["dE_t_ha"] = emu["e_t"] - f64["e_t"]
         line["dE_ccsd_t_ha"] = line["dE_ccsd_ha"] + line["dE_t_ha"]

@@ -58,6 +58,38 @@ def test_dgemm_all_transposes(ctx):
         assert np.abs(got - ref).max() < 1e-12 * max(1, np.abs(ref).max()) * np.sqrt(K)
 
 
+@pytest.mark.parametrize("prec", [capi.PREC_FP64, capi.PREC_EMU])
+def test_matrix_vector_products(ctx, prec):
+    # M = 1 or N = 1 runs as a deterministic FP64 GEMV in both precision
+    # modes, with either operand layout and the ldc stride of a row result
+    import torch  # device memory plumbing only
+    rng = np.random.default_rng(4)
+    cases = [(0, 0, 3000, 1, 5000), (1, 0, 3000, 1, 5000), (0, 1, 2500, 1, 700),
+             (1, 1, 17, 1, 20000), (0, 0, 1, 3000, 4000), (1, 0, 1, 2999, 4001),
+             (0, 1, 1, 1500, 9000), (1, 1, 1, 64, 33), (0, 0, 1, 1, 70000)]
+    for (ta, tb, M, N, K) in cases:
+        A = rng.normal(size=(K, M) if ta else (M, K))
+        B = rng.normal(size=(N, K) if tb else (K, N))
+        ldc = M + 3 if M == 1 else M
+        Cfull = rng.normal(size=(ldc, N))
+        ref = 0.7 * ((A.T if ta else A) @ (B.T if tb else B)) - 0.3 * Cfull[:M]
+        dA = torch.tensor(A.T.copy().ravel(), device="cuda")
+        dB = torch.tensor(B.T.copy().ravel(), device="cuda")
+        dC = torch.tensor(Cfull.T.copy().ravel(), device="cuda")
+        torch.cuda.synchronize()
+        ctx.set_emulation(6, 0.0)
+        ctx.check(ctx.lib.gbcc_dgemm(ctx.h, ta, tb, M, N, K, 0.7, dA.data_ptr(),
+                                     A.shape[0], dB.data_ptr(), B.shape[0], -0.3,
+                                     dC.data_ptr(), ldc, prec))
+        torch.cuda.synchronize()
+        ctx.set_emulation(6, 1e7)
+        got_full = dC.cpu().numpy().reshape(N, ldc).T
+        got = got_full[:M]
+        scale = np.abs(A).max() * np.abs(B).max() * K
+        assert np.abs(got - ref).max() < 1e-14 * scale, (ta, tb, M, N, K)
+        assert np.array_equal(got_full[M:], Cfull[M:])  # padding rows untouched
+
+
 def test_coulomb_integrals_match_oracle(ctx):
     s = make_system(6, 20, 48, seed=5)
     got = gpu.coulomb_integrals(ctx, s.gamma, 6)
