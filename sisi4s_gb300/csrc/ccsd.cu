@@ -304,7 +304,15 @@ void Ccsd::residual(int it, const double *Tp, double *Rp) {
       for (int64_t n = m; n < ns; ++n) {                           // :419
         const int64_t nx = sl[n].t.lens[1], ny = sl[m].t.lens[1];
         OTen Vs(ctx, {nx, ny, Nv, Nv});                            // :425-434
-        C(1.0, sl[n], "Gxc", sl[m], "Gyd", 0.0, Vs, "xycd");
+        if (prec == GBCC_PREC_EMU) {
+          // V[(x,c),(y,d)] = sum_G sl_n[G,(x,c)] sl_m[G,(y,d)], written
+          // straight into the V[x,y,c,d] layout of the next product
+          const OutMap vmap{nx, 1, nx * ny, ny, nx, nx * ny * Nv};
+          gemm_emu_mapped(ctx, true, false, nx * Nv, ny * Nv, NG, 1.0, sl[n].p(), NG,
+                          sl[m].p(), NG, Vs.p(), vmap);
+        } else {
+          C(1.0, sl[n], "Gxc", sl[m], "Gyd", 0.0, Vs, "xycd");
+        }
         OTen Rxy(ctx, {nx, ny, No, No});                           // :443
         C(1.0, Vs, "xycd", X, "cdij", 0.0, Rxy, "xyij");
         const int64_t a0 = n * s, b0 = m * s;                      // :444-447

@@ -239,6 +239,10 @@ struct EmuArgs {
   OutScale os;             // alpha
   double beta;
   int *err;
+  // output index map (OutMap); mapped = 0: C(m, n) at C + m + n ldc
+  int mapped;
+  unsigned ml0, nl0;
+  int64_t ms0, ms1, ns0, ns1;
 };
 
 // work unit u (a K-split of one output tile) -> split index and tile.
@@ -539,6 +543,26 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) emu_gemm_kernel(EmuArgs a) {
             }
           }
         } else {
+        if (a.mapped) {
+          // permuted output layout, beta = 0 (host-checked): row offset once,
+          // column offsets stepped through the mixed radix of n; every lane
+          // runs the same loop (the shuffles stay converged)
+          const unsigned mu = mrow ? (unsigned)m : 0u;
+          const unsigned mq = mu / a.ml0;
+          double *rp = a.C + (int64_t)(mu - mq * a.ml0) * a.ms0 + (int64_t)mq * a.ms1;
+          unsigned nq = (unsigned)n0 / a.nl0, nr = (unsigned)n0 - nq * a.nl0;
+#pragma unroll
+          for (int j = 0; j < EPI_COLS; ++j) {
+            const int eb = __shfl_sync(0xffffffffu, ebl, j);
+            if (mrow && n0 + j < a.N)
+              rp[(int64_t)nr * a.ns0 + (int64_t)nq * a.ns1] = scaled_total(tot[j], ea + eb, a.os);
+            if (++nr == a.nl0) {
+              nr = 0;
+              ++nq;
+            }
+          }
+          continue;
+        }
         double *cp = a.C + m + n0 * a.ldc;
 #pragma unroll
         for (int j0 = 0; j0 < EPI_COLS; j0 += 8) {
@@ -702,7 +726,8 @@ __global__ void emu_splitk_reduce_kernel(const long long *__restrict__ W, int ks
                                          const int *__restrict__ ea,
                                          const int *__restrict__ eb, int frac,
                                          OutScale os, double beta,
-                                         double *__restrict__ C, int64_t ldc) {
+                                         double *__restrict__ C, int64_t ldc,
+                                         OutMap map) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < M * N;
        i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t m = i % M, n = i / M;
@@ -710,7 +735,9 @@ __global__ void emu_splitk_reduce_kernel(const long long *__restrict__ W, int ks
     for (int s = 0; s < ks; ++s) t += W[((int64_t)s * N + n) * M + m];
     const int e = max(ea[m], EXP_FLOOR) + max(eb[n], EXP_FLOOR) - 14 - frac;
     double v = scaled_total(t, e, os);
-    double *cp = C + m + n * ldc;
+    double *cp = map.ml0 ? C + (m % map.ml0) * map.ms0 + (m / map.ml0) * map.ms1 +
+                               (n % map.nl0) * map.ns0 + (n / map.nl0) * map.ns1
+                         : C + m + n * ldc;
     if (beta != 0.0) v = fma(beta, *cp, v);
     *cp = v;
   }
@@ -774,7 +801,8 @@ EmuPlan emu_plan(int S, int64_t M, int64_t N, int64_t K, int sm_count,
 template <int S>
 void run_emu(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
              double alpha, const double *A, int64_t lda, const double *B,
-             int64_t ldb, double beta, double *C, int64_t ldc) {
+             int64_t ldb, double beta, double *C, int64_t ldc,
+             const OutMap &map = OutMap{}) {
   const EmuPlan P = emu_plan(S, M, N, K, ctx.sm_count, true);
   const int mt = P.mt, nt = P.nt, kt = P.kt;
   require((int64_t)mt * nt * P.ksplit < (1LL << 31), "emu gemm: grid too large");
@@ -835,6 +863,17 @@ void run_emu(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
   args.ksplit = P.ksplit;
   args.frac = P.frac;
   args.W = P.ksplit > 1 ? wsp.as<long long>() : nullptr;
+  if (map.ml0 > 0) {
+    require(beta == 0.0 && map.ml0 < (1LL << 31) && map.nl0 > 0 && map.nl0 < (1LL << 31),
+            "emulated GEMM: output map needs beta = 0 and 32-bit index lengths");
+    args.mapped = 1;
+    args.ml0 = (unsigned)map.ml0;
+    args.nl0 = (unsigned)map.nl0;
+    args.ms0 = map.ms0;
+    args.ms1 = map.ms1;
+    args.ns0 = map.ns0;
+    args.ns1 = map.ns1;
+  }
   args.os = out_scale(alpha);
   args.beta = beta;
   args.err = err;
@@ -859,7 +898,7 @@ void run_emu(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
     const int64_t g = std::min<int64_t>((n + 255) / 256, (int64_t)std::max(ctx.sm_count, 1) * 8);
     emu_splitk_reduce_kernel<<<(unsigned)std::max<int64_t>(g, 1), 256, 0, ctx.stream>>>(
         wsp.as<long long>(), P.ksplit, M, N, ea.as<int>(), eb.as<int>(), P.frac, args.os,
-        beta, C, ldc);
+        beta, C, ldc, map);
     GBCC_CHECK_LAUNCH(ctx);
   }
   // a bounded wait that gave up sets the context's sticky error word; it is
@@ -961,7 +1000,7 @@ void gemm_panels(Context &ctx, const EmuPanels &A, int ia, const EmuPanels &B, i
     const int64_t n = M * N;
     const int64_t g = std::min<int64_t>((n + 255) / 256, (int64_t)std::max(ctx.sm_count, 1) * 8);
     emu_splitk_reduce_kernel<<<(unsigned)std::max<int64_t>(g, 1), 256, 0, ctx.stream>>>(
-        wsp.as<long long>(), P.ksplit, M, N, args.ea, args.eb, P.frac, args.os, beta, C, ldc);
+        wsp.as<long long>(), P.ksplit, M, N, args.ea, args.eb, P.frac, args.os, beta, C, ldc, OutMap{});
     GBCC_CHECK_LAUNCH(ctx);
   }
   ctx.flops += 2.0 * (double)M * (double)N * (double)K;
@@ -1012,6 +1051,21 @@ void emu_gemm_panels(Context &ctx, const EmuPanels &A, int ia, const EmuPanels &
     case 8: gemm_panels<8>(ctx, A, ia, B, ib, alpha, beta, C, Cdf, ldc); break;
     default: throw Error(GBCC_BAD_ARG, "emu_slices must be in [4, 8]");
   }
+}
+
+void gemm_emu_mapped(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
+                     double alpha, const double *A, int64_t lda, const double *B,
+                     int64_t ldb, double *C, const OutMap &map) {
+  require(map.ml0 > 0 && map.nl0 > 0, "gemm_emu_mapped: empty map");
+  switch (ctx.emu_slices) {
+    case 4: run_emu<4>(ctx, ta, tb, M, N, K, alpha, A, lda, B, ldb, 0.0, C, 0, map); break;
+    case 5: run_emu<5>(ctx, ta, tb, M, N, K, alpha, A, lda, B, ldb, 0.0, C, 0, map); break;
+    case 6: run_emu<6>(ctx, ta, tb, M, N, K, alpha, A, lda, B, ldb, 0.0, C, 0, map); break;
+    case 7: run_emu<7>(ctx, ta, tb, M, N, K, alpha, A, lda, B, ldb, 0.0, C, 0, map); break;
+    case 8: run_emu<8>(ctx, ta, tb, M, N, K, alpha, A, lda, B, ldb, 0.0, C, 0, map); break;
+    default: throw Error(GBCC_BAD_ARG, "emu_slices must be in [4, 8]");
+  }
+  ctx.flops += 2.0 * (double)M * (double)N * (double)K;
 }
 
 void gemm_emu(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,

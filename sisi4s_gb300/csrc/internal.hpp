@@ -245,6 +245,15 @@ struct df32;
 void emu_gemm_panels(Context &ctx, const EmuPanels &A, int ia, const EmuPanels &B,
                      int ib, double alpha, double beta, double *C, int64_t ldc,
                      df32 *Cdf = nullptr);
+// Output index map of an emulated GEMM with two indices on each side: C(m, n)
+// lives at C + (m % ml0) ms0 + (m / ml0) ms1 + (n % nl0) ns0 + (n / nl0) ns1,
+// so a product can write a permuted layout directly (beta must be 0).
+struct OutMap {
+  int64_t ml0, ms0, ms1, nl0, ns0, ns1;
+};
+void gemm_emu_mapped(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
+                     double alpha, const double *A, int64_t lda, const double *B,
+                     int64_t ldb, double *C, const OutMap &map);
 // emulated GEMM with its scratch in a fixed file-scope device array
 void gemm_emu_noalloc(Context &ctx, bool ta, bool tb, int64_t M, int64_t N,
                       int64_t K, double alpha, const double *A, int64_t lda,

@@ -118,6 +118,28 @@ def test_residual_matches_oracle(ctx, No, Nv, NG, dist, ppl, slice_size):
     assert _rel(g2, r2) < RTOL_RES
 
 
+@pytest.mark.parametrize("No,Nv,NG,slice_size,dist", [(4, 23, 50, 5, 0), (3, 40, 64, 16, 0),
+                                                      (5, 30, 70, 30, 1), (2, 9, 20, 4, 0)])
+def test_residual_emulated_matches_oracle(ctx, No, Nv, NG, slice_size, dist):
+    # every GEMM emulated (threshold 0), ragged ladder slices: the ladder's
+    # V_xycd is written by the emulated GEMM straight into its permuted layout
+    s = make_system(No, Nv, NG, seed=No * 7 + Nv)
+    ints = oracle_ints(s.gamma, No)
+    T1, T2 = _rand_amplitudes(Nv, No, seed=Nv + 1)
+    r1, r2 = oracle_residual(1, T1, T2, ints, s.gamma, distinguishable=dist,
+                             slice_size=slice_size)
+    ctx.set_emulation(6, 0.0)
+    try:
+        g1, g2 = gpu.ccsd_residual(ctx, 1, T1, T2, s.eps_h, s.eps_p, s.gamma,
+                                   distinguishable=dist, slice_size=slice_size,
+                                   precision="emu")
+    finally:
+        ctx.set_emulation(6, 1e7)
+    # six bf16 digits: ~2^-42 K relative to the operand scales per product
+    assert _rel(g1, r1) < 1e-10
+    assert _rel(g2, r2) < 1e-10
+
+
 def test_mp2_start_is_exact(ctx):
     s = make_system(4, 12, 30, seed=1)
     ints = oracle_ints(s.gamma, 4)
