@@ -174,11 +174,13 @@ def serve_measure(args):
         st = serve.latency_stats(recs, wall)
         out["one_at_a_time_" + prec] = {"requests": args.serve_single,
                                         "solves_per_s": st["solves_per_s"]}
+    lam = args.serve_lambda if args.serve_lambda > 0 else None
     srv = serve.Server(slots=args.serve_slots)
-    recs, wall = serve.run_stream(srv, reqs[:args.serve_requests], lam=None,
+    recs, wall = serve.run_stream(srv, reqs[:args.serve_requests], lam=lam,
                                   precision="emu", **SERVE_OPTS)
     srv.close()
     st = serve.latency_stats(recs, wall)
+    st["arrivals"] = ("Poisson, rate %g /s (seed 0)" % lam) if lam else "all at t = 0"
     out["batched_emu"] = st
     out["status_counts"] = {str(k): sum(1 for r in recs if r["status"] == k)
                             for k in sorted(set(r["status"] for r in recs))}
@@ -229,6 +231,11 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=32)
     ap.add_argument("--serve-single", type=int, default=4)
     ap.add_argument("--serve-slots", type=int, default=8)
+    ap.add_argument("--serve-lambda", type=float, default=0.0,
+                    help="Poisson arrival rate of the batched serving run "
+                         "(0: all requests at t = 0)")
+    ap.add_argument("--serve-only", action="store_true",
+                    help="run only the serving measurement (one JSON line)")
     ap.add_argument("--no-triples", action="store_true",
                     help="skip the (T) correction on the final amplitudes")
     ap.add_argument("--triples-fp64", action="store_true",
@@ -246,6 +253,10 @@ def main():
     from sisi4s_gb300.inputs import make_system
 
     torch.cuda.set_device(local)
+    if args.serve_only:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "serving": serve_measure(args)}), flush=True)
+        return
     W = WORKLOAD
     s = make_system(W["No"], W["Nv"], W["NG"], W["seed"])
     ctx = capi.Context(local)

@@ -113,10 +113,14 @@ Ccsd::Ccsd(Context &ctx, std::unique_ptr<CcsdInputs> in,
   if (o_.integrals_slice_size > 0) slice_ = o_.integrals_slice_size;
   else if (o_.integrals_slice_factor >= 0) slice_ = (int64_t)(Nv * o_.integrals_slice_factor);
   else {
-    // device default: the largest slice whose V_xycd (plus its GEMM-layout
-    // copy) stays within 4 GiB; the energy does not depend on the slicing
+    // device default: Nv / 8 (at least 16), capped so that V_xycd plus its
+    // digit panels stay within 4 GiB.  Slice pairs m <= n redo the diagonal
+    // blocks, so smaller slices do less redundant ladder work (1/(2 ns) of
+    // the a >= b half) while Nv / 8 keeps the GEMMs large; the energy does
+    // not depend on the slicing
     const double budget = 4.0 * 1024 * 1024 * 1024 / 16.0;
-    slice_ = (int64_t)std::floor(std::sqrt(budget / (double)(Nv * Nv)));
+    const int64_t cap = (int64_t)std::floor(std::sqrt(budget / (double)(Nv * Nv)));
+    slice_ = std::min<int64_t>(cap, std::max<int64_t>(16, Nv / 8));
   }
   slice_ = std::max<int64_t>(1, std::min<int64_t>(slice_, Nv));
   const size_t fb = sizeof(double) * L_.ntot;
@@ -300,11 +304,20 @@ void Ccsd::residual(int it, const double *Tp, double *Rp) {
       sl.emplace_back(ctx, std::initializer_list<int64_t>{NG, nx, Nv});
       gather_slice(ctx, sl.back().p(), dG.p(), NG, Nv, x0, nx);
     }
+    // precision mode: X[c,d,i,j] (rows ij, K = cd) is the B operand of every
+    // slice pair's R = V.X, so its digit panels are split once
+    const bool emu = prec == GBCC_PREC_EMU;
+    auto emulated = [&](int64_t M, int64_t N, int64_t K) {
+      return emu && 2.0 * (double)M * (double)N * (double)K >= ctx.emu_min_flops;
+    };
+    EmuPanels Xp;
+    if (emulated(s * s, No * No, Nv * Nv))
+      Xp = emu_split(ctx, false, X.p(), No * No, Nv * Nv, Nv * Nv, 1, 1, 0);
     for (int64_t m = 0; m < ns; ++m) {                             // :418
       for (int64_t n = m; n < ns; ++n) {                           // :419
         const int64_t nx = sl[n].t.lens[1], ny = sl[m].t.lens[1];
         OTen Vs(ctx, {nx, ny, Nv, Nv});                            // :425-434
-        if (prec == GBCC_PREC_EMU) {
+        if (emulated(nx * Nv, ny * Nv, NG)) {
           // V[(x,c),(y,d)] = sum_G sl_n[G,(x,c)] sl_m[G,(y,d)], written
           // straight into the V[x,y,c,d] layout of the next product
           const OutMap vmap{nx, 1, nx * ny, ny, nx, nx * ny * Nv};
@@ -314,7 +327,12 @@ void Ccsd::residual(int it, const double *Tp, double *Rp) {
           C(1.0, sl[n], "Gxc", sl[m], "Gyd", 0.0, Vs, "xycd");
         }
         OTen Rxy(ctx, {nx, ny, No, No});                           // :443
-        C(1.0, Vs, "xycd", X, "cdij", 0.0, Rxy, "xyij");
+        if (Xp.count > 0 && emulated(nx * ny, No * No, Nv * Nv)) {
+          const EmuPanels Vp = emu_split(ctx, true, Vs.p(), nx * ny, Nv * Nv, 1, nx * ny, 1, 0);
+          emu_gemm_panels(ctx, Vp, 0, Xp, 0, 1.0, 0.0, Rxy.p(), nx * ny);
+        } else {
+          C(1.0, Vs, "xycd", X, "cdij", 0.0, Rxy, "xyij");
+        }
         const int64_t a0 = n * s, b0 = m * s;                      // :444-447
         slice_add(ctx, R2.p, Rxy.p(), Nv, No, a0, b0, nx, ny, a0 > b0);
       }

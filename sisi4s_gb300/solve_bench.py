@@ -13,7 +13,7 @@ import json
 import time
 
 
-def run(ctx, s, precision, iterations, triples):
+def run(ctx, s, precision, iterations, triples, triples_fp64=False):
     import torch  # device synchronisation only
 
     from . import ccsd as gpu
@@ -32,6 +32,14 @@ def run(ctx, s, precision, iterations, triples):
         t0 = time.perf_counter()
         e_t, _ = sol.triples(precision)
         out.update(e_t=e_t, triples_seconds=time.perf_counter() - t0)
+    if triples_fp64:
+        # FP64 (T) on these same amplitudes: isolates the error of the (T)
+        # emulation from the propagation of CCSD amplitude differences
+        t0 = time.perf_counter()
+        e_t64, _ = sol.triples("fp64")
+        out.update(e_t_fp64_same_amplitudes=e_t64,
+                   dE_t_same_amplitudes_ha=out["e_t"] - e_t64,
+                   triples_fp64_seconds=time.perf_counter() - t0)
     sol.close()
     return out
 
@@ -48,6 +56,8 @@ def main():
                     help="bf16 digits per operand in precision mode")
     ap.add_argument("--emu-only", action="store_true",
                     help="skip the FP64 run (compare against a recorded one)")
+    ap.add_argument("--triples-fp64-on-emu", action="store_true",
+                    help="also run the FP64 (T) on the precision-mode amplitudes")
     args = ap.parse_args()
 
     from . import capi
@@ -57,7 +67,7 @@ def main():
     ctx = capi.Context(0)
     ctx.set_emulation(args.slices, 1e7)
     trip = not args.no_triples
-    emu = run(ctx, s, "emu", args.iterations, trip)
+    emu = run(ctx, s, "emu", args.iterations, trip, trip and args.triples_fp64_on_emu)
     line = {"No": args.No, "Nv": args.Nv, "NG": args.NG, "seed": args.seed,
             "iterations": args.iterations, "mixer": "DiisMixer(5), MP2 start",
             "slices": args.slices, "emu": emu}
