@@ -76,6 +76,29 @@ gbcc_status gbcc_ctx_set_graphs(gbcc_ctx *ctx, int enable);
 gbcc_status gbcc_ctx_profile(gbcc_ctx *ctx, int enable);
 gbcc_status gbcc_ctx_gemm_stats(gbcc_ctx *ctx, double *ms, int64_t *launches,
                                 double *tc_flops, double *fp64_flops);
+/* Fault injection for failure-path tests (new in this library: sisi4s has
+ * none).  The next event of the chosen kind fails as if it had happened, then
+ * injection switches itself off:
+ *   GBCC_FAULT_DIIS_SINGULAR  the next DIIS mixing step reports a singular
+ *                             matrix (the solve returns GBCC_DIIS_SINGULAR)
+ *   GBCC_FAULT_NAN            the next CCSD iteration's norms read NaN
+ *                             (GBCC_DIVERGED)
+ *   GBCC_FAULT_OOM            the next device allocation fails (GBCC_OOM)
+ *   GBCC_FAULT_DEVICE_WAIT    the next tensor-core GEMM launch first waits on
+ *                             a barrier that nothing completes; the bounded
+ *                             wait gives up in well under a second, every
+ *                             other role of the kernel stops, and the call
+ *                             returns GBCC_TIMEOUT with the context usable
+ * No injected fault touches memory out of bounds or leaves a kernel hung. */
+enum {
+  GBCC_FAULT_NONE = 0,
+  GBCC_FAULT_DIIS_SINGULAR = 1,
+  GBCC_FAULT_NAN = 2,
+  GBCC_FAULT_OOM = 3,
+  GBCC_FAULT_DEVICE_WAIT = 4
+};
+gbcc_status gbcc_ctx_inject_fault(gbcc_ctx *ctx, int kind);
+
 /* Per-launch records behind those statistics (new in this library; sisi4s
  * has per-step timers only): the M, N, K (3 values per launch, into mnk) and
  * device milliseconds (into ms) of up to cap profiled GEMM launches, oldest

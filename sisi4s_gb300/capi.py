@@ -14,6 +14,7 @@ LIB_PATH = os.path.join(HERE, "_lib", "libgbcc.so")
 OK, NOT_CONVERGED, DIIS_SINGULAR, DIVERGED, OOM, BAD_ARG, CUDA_ERROR, \
     TIMEOUT, COMPLEX_UNSUPPORTED, NO_DEVICE = range(10)
 PREC_FP64, PREC_EMU = 0, 1
+FAULT_NONE, FAULT_DIIS_SINGULAR, FAULT_NAN, FAULT_OOM, FAULT_DEVICE_WAIT = range(5)
 
 _dp = C.POINTER(C.c_double)
 
@@ -65,6 +66,7 @@ _SIGS = {
     "gbcc_ctx_set_graphs": (C.c_int, [C.c_void_p, C.c_int]),
     "gbcc_ctx_gemm_stats": (C.c_int, [C.c_void_p, _dp, C.POINTER(C.c_int64),
                                       _dp, _dp]),
+    "gbcc_ctx_inject_fault": (C.c_int, [C.c_void_p, C.c_int]),
     "gbcc_ctx_gemm_records": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), _dp,
                                         C.c_int64, C.POINTER(C.c_int64)]),
     "gbcc_ccsd_opts_default": (None, [C.POINTER(CcsdOpts)]),
@@ -182,6 +184,10 @@ class Context:
                                                 C.byref(tc), C.byref(f64)))
         return {"ms": ms.value, "launches": n.value, "tc_flops": tc.value,
                 "fp64_flops": f64.value}
+
+    def inject_fault(self, kind):
+        """Make the next event of ``kind`` (FAULT_*) fail once (tests)."""
+        self.check(self.lib.gbcc_ctx_inject_fault(self.h, int(kind)))
 
     def gemm_records(self, cap=1 << 16):
         """[(M, N, K, ms)] of the profiled GEMM launches since the last call."""

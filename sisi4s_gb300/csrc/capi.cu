@@ -190,6 +190,12 @@ gbcc_status gbcc_ctx_gemm_stats(gbcc_ctx *ctx, double *ms, int64_t *launches,
   });
 }
 
+gbcc_status gbcc_ctx_inject_fault(gbcc_ctx *ctx, int kind) {
+  if (!ctx || kind < GBCC_FAULT_NONE || kind > GBCC_FAULT_DEVICE_WAIT) return GBCC_BAD_ARG;
+  ctx->c.fault = kind;
+  return GBCC_OK;
+}
+
 gbcc_status gbcc_ctx_gemm_records(gbcc_ctx *ctx, int64_t *mnk, double *ms, int64_t cap,
                                   int64_t *count) {
   if (!ctx || cap < 0 || (cap > 0 && (!mnk || !ms))) return GBCC_BAD_ARG;

@@ -8,6 +8,7 @@
 // symmetrisation (:292) are not symmetrised.
 #include <algorithm>
 #include <cmath>
+#include <limits>
 #include <cstring>
 
 #include "ccsd.hpp"
@@ -502,6 +503,8 @@ gbcc_status Ccsd::run(int n, double *energy, int *converged) {
     exc_ = info.exchange;
     hist_.push_back(e_);
     ++it_;
+    if (o_.mixer == 1 && ctx_.take_fault(GBCC_FAULT_DIIS_SINGULAR)) info.diis_status = 1;
+    if (ctx_.take_fault(GBCC_FAULT_NAN)) info.dtdt = std::numeric_limits<double>::quiet_NaN();
     if (info.diis_status) {
       st = GBCC_DIIS_SINGULAR;
       break;

@@ -64,7 +64,9 @@ constexpr int GROUP_M = 16;    // m-tiles per rasterization group
 constexpr int EXP_FLOOR = -1100;
 
 enum : int { ERR_NONE = 0, ERR_FULL = 1, ERR_EMPTY = 2, ERR_ACCF = 3,
-             ERR_ACCE = 4, ERR_DRAIN = 5 };
+             ERR_ACCE = 4, ERR_DRAIN = 5, ERR_INJECTED = 6 };
+// polls of the injected wait (a barrier nothing completes): well under a second
+constexpr long long INJECTED_WAIT_LIMIT = 1LL << 16;
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -90,6 +92,19 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
   for (long long i = 0; i < WAIT_LIMIT; ++i)
     if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+// bounded wait that also gives up as soon as another role of the CTA has
+// aborted (checked every 64 polls), so that one failure ends the kernel
+// promptly instead of running every other wait to its limit
+__device__ __forceinline__ bool mbar_wait_or_abort(uint32_t bar, uint32_t parity,
+                                                   const volatile int *abort,
+                                                   long long limit = WAIT_LIMIT) {
+  for (long long i = 0; i < limit; ++i) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((i & 63) == 63 && *abort) return false;
+  }
   return false;
 }
 
@@ -239,6 +254,9 @@ struct EmuArgs {
   OutScale os;             // alpha
   double beta;
   int *err;
+  // test hook: the MMA issuer first waits on a barrier that nothing
+  // completes, so the bounded wait gives up (GBCC_FAULT_DEVICE_WAIT)
+  int inject_wait;
   // output index map (OutMap); mapped = 0: C(m, n) at C + m + n ldc
   int mapped;
   unsigned ml0, nl0;
@@ -298,7 +316,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) emu_gemm_kernel(EmuArgs a) {
 
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ __align__(8) uint64_t bar_full[4], bar_empty[4], bar_accf, bar_acce,
-      bar_drain;
+      bar_drain, bar_never;
   __shared__ uint32_t tmem_base_sh;
   __shared__ volatile int abort_sh;
 
@@ -313,6 +331,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) emu_gemm_kernel(EmuArgs a) {
     mbar_init(smem_u32(&bar_accf), 1);
     mbar_init(smem_u32(&bar_acce), 32 * EPI_WARPS);
     mbar_init(smem_u32(&bar_drain), 1);
+    mbar_init(smem_u32(&bar_never), 1);
     abort_sh = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -344,7 +363,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) emu_gemm_kernel(EmuArgs a) {
         for (int kl = 0; kl < nkb; ++kl) {
           const int st = (int)(g % STAGES);
           if (g >= STAGES &&
-              !mbar_wait(smem_u32(&bar_empty[st]), (int)((g / STAGES) - 1) & 1)) {
+              !mbar_wait_or_abort(smem_u32(&bar_empty[st]), (int)((g / STAGES) - 1) & 1,
+                                  &abort_sh)) {
             atomicCAS(a.err, 0, ERR_EMPTY);
             abort_sh = 1;
             ok = false;
@@ -383,6 +403,12 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) emu_gemm_kernel(EmuArgs a) {
       long long g = 0;   // k-blocks consumed
       long long cg = 0;  // chunks issued
       bool ok = true;
+      if (a.inject_wait &&
+          !mbar_wait_or_abort(smem_u32(&bar_never), 0, &abort_sh, INJECTED_WAIT_LIMIT)) {
+        atomicCAS(a.err, 0, ERR_INJECTED);
+        abort_sh = 1;
+        ok = false;
+      }
       for (int u = blockIdx.x; u < nunits && ok; u += gridDim.x) {
         int split, tile_m, tile_n;
         unit_coords(a, u, split, tile_m, tile_n);
@@ -392,8 +418,9 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) emu_gemm_kernel(EmuArgs a) {
         int kl = 0;
         for (int c = 0; c < nchunks; ++c) {
           // TMEM is free once the epilogue has folded the previous chunk
-          if (cg > 0 && !mbar_wait(smem_u32(&bar_acce), (int)(cg - 1) & 1)) {
+          if (cg > 0 && !mbar_wait_or_abort(smem_u32(&bar_acce), (int)(cg - 1) & 1, &abort_sh)) {
             atomicCAS(a.err, 0, ERR_ACCE);
+            abort_sh = 1;
             ok = false;
             break;
           }
@@ -402,8 +429,9 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) emu_gemm_kernel(EmuArgs a) {
           const int kfirst = kl;
           for (; kl < kend; ++kl) {
             const int st = (int)(g % STAGES);
-            if (!mbar_wait(smem_u32(&bar_full[st]), (int)(g / STAGES) & 1)) {
+            if (!mbar_wait_or_abort(smem_u32(&bar_full[st]), (int)(g / STAGES) & 1, &abort_sh)) {
               atomicCAS(a.err, 0, ERR_FULL);
+              abort_sh = 1;
               ok = false;
               break;
             }
@@ -468,8 +496,9 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) emu_gemm_kernel(EmuArgs a) {
       for (int j = 0; j < (DF ? EPI_COLS : 1); ++j) acc[j] = df_make(0.0f, 0.0f);
       bool ok = true;
       for (int c = 0; c < nchunks; ++c) {
-        if (!mbar_wait(smem_u32(&bar_accf), (int)(cg & 1))) {
+        if (!mbar_wait_or_abort(smem_u32(&bar_accf), (int)(cg & 1), &abort_sh)) {
           atomicCAS(a.err, 0, ERR_ACCF);
+          abort_sh = 1;
           ok = false;
           break;
         }
@@ -875,6 +904,7 @@ void run_emu(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
     args.ns1 = map.ns1;
   }
   args.os = out_scale(alpha);
+  args.inject_wait = ctx.take_fault(GBCC_FAULT_DEVICE_WAIT) ? 1 : 0;
   args.beta = beta;
   args.err = err;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -980,6 +1010,7 @@ void gemm_panels(Context &ctx, const EmuPanels &A, int ia, const EmuPanels &B, i
   args.frac = P.frac;
   args.W = P.ksplit > 1 ? wsp.as<long long>() : nullptr;
   args.os = out_scale(alpha);
+  args.inject_wait = ctx.take_fault(GBCC_FAULT_DEVICE_WAIT) ? 1 : 0;
   args.beta = beta;
   args.err = ctx.device_error_word();
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -1211,6 +1242,7 @@ void run_emu_static(Context &ctx, bool ta, bool tb, int64_t M, int64_t N,
     args.W = nullptr;
   }
   args.os = out_scale(alpha);
+  args.inject_wait = ctx.take_fault(GBCC_FAULT_DEVICE_WAIT) ? 1 : 0;
   args.beta = beta;
   args.err = err;
   emu_gemm_kernel<S, false><<<emu_grid(ctx, (int64_t)mt * nt), NUM_THREADS, smem, ctx.stream>>>(args);

@@ -58,6 +58,18 @@ struct Context {
   double emu_min_flops = 1e7;
   // replay steady-state CCSD iterations as captured CUDA graphs
   bool use_graphs = true;
+  // injected fault (GBCC_FAULT_*), consumed by the first matching event
+  // (never while the stream is being captured into a graph: the fault would
+  // be baked into every replay)
+  int fault = GBCC_FAULT_NONE;
+  bool take_fault(int kind) {
+    if (fault != kind) return false;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone)
+      return false;
+    fault = GBCC_FAULT_NONE;
+    return true;
+  }
   // sticky device error word: kernels whose bounded waits give up record a
   // code here; read (and cleared) at synchronisation points
   int *dev_err = nullptr;
@@ -153,6 +165,10 @@ class DBuf {
     stream_ = ctx.stream;
     bytes_ = bytes;
     if (bytes == 0) return;
+    if (ctx.take_fault(GBCC_FAULT_OOM)) {
+      bytes_ = 0;
+      throw Error(GBCC_OOM, "injected allocation failure");
+    }
     GBCC_CUDA(cudaMallocAsync(&p_, bytes, ctx.stream));
   }
   void release() {
