@@ -42,7 +42,9 @@ def make_system(No, Nv, NG, seed=1):
     Np = No + Nv
     iu = np.triu_indices(Np)
     vals = rng.normal(0.0, 0.03, size=(NG, iu[0].size))
-    gamma = np.empty((NG, Np, Np), dtype=np.float64)
+    # column-major (first index fastest), the layout CTF hands to the
+    # reference's algorithms, so the ABI wrappers pass it without a copy
+    gamma = np.empty((NG, Np, Np), dtype=np.float64, order="F")
     gamma[:, iu[0], iu[1]] = vals
     gamma[:, iu[1], iu[0]] = vals
     eps_h = np.sort(rng.uniform(-1.5, -0.5, size=No))
@@ -67,4 +69,4 @@ def mp2_amplitudes(system):
     ep, eh = system.eps_p, system.eps_h
     d = (((ep[:, None, None, None] - eh[None, None, :, None]) + ep[None, :, None, None])
          - eh[None, None, None, :])
-    return np.zeros((system.Nv, No)), -v / d
+    return np.zeros((system.Nv, No), order="F"), np.asfortranarray(-v / d)
