@@ -13,10 +13,13 @@
 // 2^24 over a K-chunk of 512 (256 for S > 6), so the FP32 sums are exact.
 // After each chunk the epilogue warps fold the diagonals into a per-output
 // int64 fixed-point total (29 fractional bits below the g = 0 unit), still
-// exact up to the rounding of diagonals g >= 5.  FP64 is touched once per
-// output at the very end: C = 2^(ea_i + eb_j - 14 - 29) * total.  No FP64
-// arithmetic runs inside the K loop (GB300's FP64 rate is ~1/1600 of its bf16
-// tensor rate, so even one FP64 op per output per chunk would dominate).
+// exact up to the rounding of diagonals g >= 5.  At the end the total becomes
+// C = 2^(ea_i + eb_j - 14 - 29) * total with integer instructions (one
+// rounding, the bits of ldexp((double)total, e)); only a non-zero beta costs
+// an FP64 instruction per output.  GB300's FP64 pipe issues a few operations
+// per clock per SM, so FP64 work per output would bound the short-K products.
+// A float-float output variant (DF) sums the exact FP32 diagonals into hi+lo
+// FP32 pairs instead, for consumers that compute in float-float.
 //
 // Data movement.  A split kernel writes the digits of A (B) as pre-tiled
 // operand panels: tiles of 128 (64) rows x 32 k in the no-swizzle K-major

@@ -48,8 +48,8 @@ struct EpiArgs {
   int distinct[6];
   int m[6][3];          // hole indices i o pi_p
   int img[6][3];        // Permutation<3>(s) images
-  int dinv[6][3];       // D.V read: u_m = y_{dinv[p][m]}  (y_n = u_{pi_p(n)})
-  int rinv[6][3];       // rho_r^-1: x_r(y)_m = y_{rinv[r][m]}
+  int dinv[6][3];       // D.V read: u_m = y_{dinv[p][m]}  (y_n = u_{pi_p(n)});
+                        // also rho_r^-1 of the energy read, x_r(y)_m = y_{dinv[r][m]}
   int odd[6];           // parity of Permutation<3>(r)
   int i3[3];
   const double *eps_h;
@@ -342,7 +342,6 @@ double triples_energy(Context &ctx, const CcsdInputs &I, const double *T1,
     for (int n = 0; n < 3; ++n) {
       base.img[p][n] = img[p][n];
       base.dinv[p][img[p][n]] = n;
-      base.rinv[p][img[p][n]] = n;
       for (int k = n + 1; k < 3; ++k) inversions += img[p][n] > img[p][k];
     }
     base.odd[p] = inversions & 1;
