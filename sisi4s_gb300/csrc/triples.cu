@@ -305,6 +305,16 @@ double triples_energy(Context &ctx, const CcsdInputs &I, const double *T1,
   // element types are 8 bytes.
   const bool emu = precision == GBCC_PREC_EMU;
   static_assert(sizeof(df32) == sizeof(double), "epilogue element size");
+  // (T) in precision mode uses one more digit than the CCSD iteration: its
+  // energy can be orders of magnitude larger than E_CCSD on far-from-converged
+  // amplitudes (a chaotic DIIS trajectory), and it is the per-element
+  // accuracy of W that its error follows
+  struct SlicesScope {
+    Context &c;
+    int saved;
+    ~SlicesScope() { c.emu_slices = saved; }
+  } slices_scope{ctx, ctx.emu_slices};
+  if (emu) ctx.emu_slices = std::min(8, ctx.emu_slices + 1);
   // Wvv[d,b,c,k] = sum_F Gab[F,b,d] Gai[F,c,k]
   OTen Wvv(ctx, {Nv, Nv, Nv, No});
   contract(ctx, 1.0, I.Gab, "Fbd", I.Gai, "Fck", 0.0, Wvv, "dbck", precision);
