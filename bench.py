@@ -374,8 +374,19 @@ def main():
             "launches": gs["launches"],
             "avg_launch_ms": gs["ms"] / max(gs["launches"], 1),
             "fp64_equiv_tflops": gs["fp64_flops"] / (gs["ms"] / 1e3) / 1e12 if gs["ms"] else None,
-            "gemm_share_of_step": gs["ms"] / prof_ms if prof_ms else None,
-            "traffic": None}
+            "gemm_share_of_step": gs["ms"] / prof_ms if prof_ms else None}
+    # DRAM traffic per launch: the ncu capture of the same kernel at M=N=K=4096
+    # (profiles/emu_gemm_4096.md: dram read + write = 1.942 + 0.153 GB for
+    # 21 * 2 * 4096^3 bf16 flop), scaled to this run's average launch by its
+    # algorithmic work (the panel re-reads grow with M*N*K for fixed tiles)
+    if gs["launches"]:
+        per_flop = (1.942e9 + 0.153e9) / (21 * 2.0 * 4096 ** 3)
+        roof["traffic"] = per_flop * gs["tc_flops"] / gs["launches"]
+        roof["traffic_unit"] = "bytes per launch"
+        roof["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum at "
+                                  "4096^3, scaled by work per launch")
+    else:
+        roof["traffic"] = None
 
     serving = None
     if not args.no_serve:
