@@ -177,15 +177,16 @@ def serve_measure(args):
     lam = args.serve_lambda if args.serve_lambda > 0 else None
     srv = serve.Server(slots=args.serve_slots)
     recs, wall = serve.run_stream(srv, reqs[:args.serve_requests], lam=lam,
-                                  precision="emu", **SERVE_OPTS)
+                                  precision=args.serve_precision, **SERVE_OPTS)
     srv.close()
     st = serve.latency_stats(recs, wall)
     st["arrivals"] = ("Poisson, rate %g /s (seed 0)" % lam) if lam else "all at t = 0"
-    out["batched_emu"] = st
+    out["batched_" + args.serve_precision] = st
     out["status_counts"] = {str(k): sum(1 for r in recs if r["status"] == k)
                             for k in sorted(set(r["status"] for r in recs))}
     out["batched_over_fp64_one_at_a_time"] = (
         st["solves_per_s"] / out["one_at_a_time_fp64"]["solves_per_s"])
+    out["batched_precision"] = args.serve_precision
     return out
 
 
@@ -234,6 +235,8 @@ def main():
     ap.add_argument("--serve-lambda", type=float, default=0.0,
                     help="Poisson arrival rate of the batched serving run "
                          "(0: all requests at t = 0)")
+    ap.add_argument("--serve-precision", default="emu", choices=["emu", "fp64"],
+                    help="precision of the batched serving run")
     ap.add_argument("--serve-only", action="store_true",
                     help="run only the serving measurement (one JSON line)")
     ap.add_argument("--no-triples", action="store_true",
