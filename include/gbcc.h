@@ -128,7 +128,8 @@ typedef struct {
   double integrals_slice_factor; /* integralsSliceFactor, < 0: not given */
   int precision;                 /* gbcc_precision, default GBCC_PREC_FP64 */
   int emu_slices;                /* bf16 slices per operand for GBCC_PREC_EMU
-                                    (0 = library default) */
+                                    (0 = library default); (T) uses one more,
+                                    at most 8 */
 } gbcc_ccsd_opts;
 
 void gbcc_ccsd_opts_default(gbcc_ccsd_opts *opts);
