@@ -38,29 +38,68 @@ def make_opts(mixer="LinearMixer", max_residua=4, mixing_ratio=1.0,
     return o
 
 
+def _eigenenergies(eps_h, eps_p):
+    eps_h = np.ascontiguousarray(eps_h, dtype=np.float64)
+    eps_p = np.ascontiguousarray(eps_p, dtype=np.float64)
+    if eps_h.ndim != 1 or eps_p.ndim != 1 or not eps_h.size or not eps_p.size:
+        raise ValueError("eps_h and eps_p must be non-empty vectors")
+    return eps_h, eps_p
+
+
+def _flat(arr, shape, name):
+    """Column-major copy of a real tensor after checking its shape.  The ABI
+    takes bare pointers, so a wrong shape would be read past its end."""
+    a = np.asarray(arr)
+    if a.shape != tuple(shape):
+        raise ValueError("%s has shape %s, expected %s" % (name, a.shape, tuple(shape)))
+    if np.iscomplexobj(a):
+        raise ValueError("%s must be real" % name)
+    return fortran_flat(a)
+
+
+def _vertex(gamma, No, Nv):
+    """(real part, imaginary part or None) of the vertex Gamma[G, p, q].  The
+    imaginary part is handed to the library, which refuses it unless it is
+    zero (COMPLEX_UNSUPPORTED), as for the reference's complex CoulombVertex."""
+    g = np.asarray(gamma)
+    if g.ndim != 3 or g.shape[1:] != (No + Nv, No + Nv) or not g.shape[0]:
+        raise ValueError("gamma has shape %s, expected (NG, %d, %d)"
+                         % (g.shape, No + Nv, No + Nv))
+    if np.iscomplexobj(g):
+        return fortran_flat(g.real), fortran_flat(g.imag)
+    return fortran_flat(g), None
+
+
+_INTEGRAL_SHAPES = {"PPHH": "vvoo", "PHPH": "vovo", "HHHH": "oooo", "HHHP": "ooov"}
+
+
+def _shape(code, No, Nv):
+    return tuple(No if c == "o" else Nv for c in code)
+
+
 class CcsdInput:
     """Owns the column-major host buffers behind a ``gbcc_ccsd_in``."""
 
     def __init__(self, eps_h, eps_p, gamma, ints=None, initial=None):
-        eps_h = np.ascontiguousarray(eps_h, dtype=np.float64)
-        eps_p = np.ascontiguousarray(eps_p, dtype=np.float64)
-        self.No, self.Nv, self.NG = eps_h.size, eps_p.size, gamma.shape[0]
-        self._keep = [eps_h, eps_p]
+        eps_h, eps_p = _eigenenergies(eps_h, eps_p)
+        No, Nv = eps_h.size, eps_p.size
+        g, self.gamma_imag = _vertex(gamma, No, Nv)
+        self.No, self.Nv, self.NG = No, Nv, np.shape(gamma)[0]
+        self._keep = [eps_h, eps_p, g, self.gamma_imag]
         s = capi.CcsdIn()
         s.No, s.Nv, s.NG = self.No, self.Nv, self.NG
         s.eps_h, s.eps_p = ptr(eps_h), ptr(eps_p)
-        g = fortran_flat(gamma)
-        self._keep.append(g)
-        s.gamma = ptr(g)
+        s.gamma, s.gamma_imag = ptr(g), ptr(self.gamma_imag)
         ints = ints or {}
         for key, field in (("PPHH", "Vabij"), ("PHPH", "Vaibj"),
                            ("HHHH", "Vijkl"), ("HHHP", "Vijka")):
             if key in ints and ints[key] is not None:
-                f = fortran_flat(ints[key])
+                f = _flat(ints[key], _shape(_INTEGRAL_SHAPES[key], No, Nv), key)
                 self._keep.append(f)
                 setattr(s, field, ptr(f))
         if initial is not None:
-            t1, t2 = fortran_flat(initial[0]), fortran_flat(initial[1])
+            t1 = _flat(initial[0], (Nv, No), "initial T1")
+            t2 = _flat(initial[1], (Nv, Nv, No, No), "initial T2")
             self._keep += [t1, t2]
             s.init_T1, s.init_T2 = ptr(t1), ptr(t2)
         self.s = s
@@ -162,16 +201,19 @@ class Solver:
 def triples(ctx, eps_h, eps_p, gamma, T1, T2, e_ccsd=0.0, Vabij=None,
             Vijka=None, precision="fp64"):
     """Returns (E_(T), E_CCSD + E_(T))."""
-    eps_h = np.ascontiguousarray(eps_h, dtype=np.float64)
-    eps_p = np.ascontiguousarray(eps_p, dtype=np.float64)
+    eps_h, eps_p = _eigenenergies(eps_h, eps_p)
+    No, Nv = eps_h.size, eps_p.size
+    g, gi = _vertex(gamma, No, Nv)
     s = capi.TriplesIn()
-    s.No, s.Nv, s.NG = eps_h.size, eps_p.size, gamma.shape[0]
-    keep = [eps_h, eps_p]
+    s.No, s.Nv, s.NG = No, Nv, np.shape(gamma)[0]
+    keep = [eps_h, eps_p, g, gi]
     s.eps_h, s.eps_p = ptr(eps_h), ptr(eps_p)
-    for name, arr in (("gamma", gamma), ("T1", T1), ("T2", T2),
-                      ("Vabij", Vabij), ("Vijka", Vijka)):
+    s.gamma, s.gamma_imag = ptr(g), ptr(gi)
+    for name, arr, shape in (("T1", T1, (Nv, No)), ("T2", T2, (Nv, Nv, No, No)),
+                             ("Vabij", Vabij, (Nv, Nv, No, No)),
+                             ("Vijka", Vijka, (No, No, No, Nv))):
         if arr is not None:
-            f = fortran_flat(arr)
+            f = _flat(arr, shape, name)
             keep.append(f)
             setattr(s, name, ptr(f))
     s.e_ccsd = float(e_ccsd)
@@ -184,9 +226,14 @@ def triples(ctx, eps_h, eps_p, gamma, T1, T2, e_ccsd=0.0, Vabij=None,
 
 
 def coulomb_integrals(ctx, gamma, No):
-    NG, Np = gamma.shape[0], gamma.shape[1]
+    NG, Np = np.shape(gamma)[0], np.shape(gamma)[1]
     Nv = Np - No
-    g = fortran_flat(gamma)
+    if not 0 < No < Np:
+        raise ValueError("No must lie in 1..Np-1")
+    g, gi = _vertex(gamma, No, Nv)
+    if gi is not None and np.any(gi):
+        raise capi.GbccError(capi.COMPLEX_UNSUPPORTED,
+                             "the vertex has a non-zero imaginary part")
     vabij = np.zeros(Nv * Nv * No * No)
     vaibj = np.zeros(Nv * Nv * No * No)
     vijkl = np.zeros(No ** 4)

@@ -17,6 +17,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <fstream>
@@ -236,8 +237,21 @@ struct Algorithm {
       throw StepError("argument " + k + " (" + d->name + ") is not a tensor");
     return *d->tensor;
   }
-  const double *tensor_or_null(const std::string &k) const {
-    return given(k) ? tensor(k).re.data() : nullptr;
+  // The ABI takes bare pointers, so every tensor handed to it must have
+  // exactly the lengths of the reference's tensor for that key.
+  const HTensor &tensor(const std::string &k, const std::vector<int64_t> &lens) const {
+    const HTensor &t = tensor(k);
+    if (t.lens != lens) throw StepError("argument " + k + " has lengths " + lens_str(t.lens) +
+                                        ", expected " + lens_str(lens));
+    return t;
+  }
+  const double *tensor_or_null(const std::string &k, const std::vector<int64_t> &lens) const {
+    return given(k) ? tensor(k, lens).re.data() : nullptr;
+  }
+  static std::string lens_str(const std::vector<int64_t> &l) {
+    std::string s = "[";
+    for (size_t i = 0; i < l.size(); ++i) s += (i ? "," : "") + std::to_string(l[i]);
+    return s + "]";
   }
   void set_tensor(const std::string &k, std::shared_ptr<HTensor> t) {
     auto d = arg(k);
@@ -276,13 +290,29 @@ std::string replace_ext(const std::string &p, const std::string &ext) {
 
 std::shared_ptr<HTensor> read_cc4s(const std::string &file) {
   auto h = yl::parse_file(file);
+  if (!h->is_map()) throw StepError(file + ": header is not a map");
   for (const char *k : {"dimensions", "elements", "scalarType", "type", "unit", "version"})
     if (!h->get(k)) throw StepError(file + ": header key " + k + " missing");
   auto t = std::make_shared<HTensor>();
-  for (auto &d : h->get("dimensions")->seq) t->lens.push_back(d->get("length")->as_int());
+  auto dims = h->get("dimensions");
+  if (!dims->is_seq() && dims->kind != yl::Node::Null)
+    throw StepError(file + ": dimensions must be a list");
+  int64_t n = 1;
+  for (auto &d : dims->seq) {
+    auto len = d->is_map() ? d->get("length") : nullptr;
+    if (!len) throw StepError(file + ": a dimension has no length");
+    const long long l = len->as_int();
+    // the element count must fit a signed 64-bit byte count of Complex64 data
+    if (l < 0 || (l > 0 && n > (INT64_MAX / 16) / l))
+      throw StepError(file + ": bad dimension length " + std::to_string(l));
+    n *= l;
+    t->lens.push_back(l);
+  }
+  auto elements = h->get("elements");
+  auto etype = elements->is_map() ? elements->get("type") : nullptr;
+  if (!etype) throw StepError(file + ": elements.type missing");
   const std::string st = h->get("scalarType")->str();
-  const std::string et = h->get("elements")->get("type")->str();
-  const int64_t n = t->size();
+  const std::string et = etype->str();
   const std::string ef = replace_ext(file, "elements");
   if (st == "Real64") {
     t->re.resize(n);
@@ -424,11 +454,16 @@ struct Sizes {
 Sizes sizes_of(const Algorithm &a) {
   const HTensor &eh = a.tensor("HoleEigenEnergies");
   const HTensor &ep = a.tensor("ParticleEigenEnergies");
-  Sizes s{(int)eh.size(), (int)ep.size(), 0};
+  if (eh.lens.size() != 1 || ep.lens.size() != 1)
+    throw StepError("HoleEigenEnergies and ParticleEigenEnergies must be vectors");
+  if (eh.lens[0] < 1 || ep.lens[0] < 1 || eh.lens[0] + ep.lens[0] > (1 << 20))
+    throw StepError("No and Nv must be positive and No+Nv at most 2^20");
+  Sizes s{(int)eh.lens[0], (int)ep.lens[0], 0};
   if (a.given("CoulombVertex")) {
     const HTensor &g = a.tensor("CoulombVertex");
     if (g.lens.size() != 3 || g.lens[1] != s.No + s.Nv || g.lens[2] != s.No + s.Nv)
       throw StepError("CoulombVertex must be [NG, No+Nv, No+Nv]");
+    if (g.lens[0] < 1 || g.lens[0] > INT32_MAX) throw StepError("CoulombVertex: bad NG");
     s.NG = (int)g.lens[0];
   }
   return s;
@@ -523,13 +558,13 @@ struct CcsdEnergyFromCoulombIntegrals : Algorithm {
     const HTensor &g = tensor("CoulombVertex");
     in.gamma = g.re.data();
     in.gamma_imag = g.complex ? g.im.data() : nullptr;
-    in.Vabij = tensor_or_null("PPHHCoulombIntegrals");
-    in.Vaibj = tensor_or_null("PHPHCoulombIntegrals");
-    in.Vijkl = tensor_or_null("HHHHCoulombIntegrals");
-    in.Vijka = tensor_or_null("HHHPCoulombIntegrals");
-    in.init_T1 = tensor_or_null("initialSinglesAmplitudes");
-    in.init_T2 = tensor_or_null("initialDoublesAmplitudes");
     const int64_t o1 = s.No, v1 = s.Nv;
+    in.Vabij = tensor_or_null("PPHHCoulombIntegrals", {v1, v1, o1, o1});
+    in.Vaibj = tensor_or_null("PHPHCoulombIntegrals", {v1, o1, v1, o1});
+    in.Vijkl = tensor_or_null("HHHHCoulombIntegrals", {o1, o1, o1, o1});
+    in.Vijka = tensor_or_null("HHHPCoulombIntegrals", {o1, o1, o1, v1});
+    in.init_T1 = tensor_or_null("initialSinglesAmplitudes", {v1, o1});
+    in.init_T2 = tensor_or_null("initialDoublesAmplitudes", {v1, v1, o1, o1});
     auto t1 = std::make_shared<HTensor>(), t2 = std::make_shared<HTensor>(),
          pe = std::make_shared<HTensor>();
     t1->lens = {v1, o1};
@@ -590,10 +625,11 @@ struct CcsdPerturbativeTriples : Algorithm {
     const HTensor &g = tensor("CoulombVertex");
     in.gamma = g.re.data();
     in.gamma_imag = g.complex ? g.im.data() : nullptr;
-    in.Vabij = tensor_or_null("PPHHCoulombIntegrals");
-    in.Vijka = tensor_or_null("HHHPCoulombIntegrals");
-    in.T1 = tensor("CcsdSinglesAmplitudes").re.data();
-    in.T2 = tensor("CcsdDoublesAmplitudes").re.data();
+    const int64_t o1 = s.No, v1 = s.Nv;
+    in.Vabij = tensor_or_null("PPHHCoulombIntegrals", {v1, v1, o1, o1});
+    in.Vijka = tensor_or_null("HHHPCoulombIntegrals", {o1, o1, o1, v1});
+    in.T1 = tensor("CcsdSinglesAmplitudes", {v1, o1}).re.data();
+    in.T2 = tensor("CcsdDoublesAmplitudes", {v1, v1, o1, o1}).re.data();
     in.e_ccsd = real("CcsdEnergy");
     double etot = 0, et = 0;
     check(gbcc_triples(gpu(), &in, precision_of(*this), &etot, &et),

@@ -198,3 +198,62 @@ def test_list_algorithms():
               "CoulombIntegralsFromVertex", "Read", "Write", "TensorWriter",
               "DefineHolesAndParticles", "Nop"):
         assert n in names
+
+
+def _read_steps(names):
+    return "".join("- name: Read\n  in: { fileName: %s.yaml }\n  out: { destination: $%s }\n"
+                   % (n, n) for n in names)
+
+
+@pytest.mark.parametrize("step,bad,msg", [
+    ("CcsdPerturbativeTriples", None, None),
+    ("CcsdPerturbativeTriples", "T2",
+     "CcsdDoublesAmplitudes has lengths [3,3,2,3], expected [3,3,2,2]"),
+    ("CcsdEnergyFromCoulombIntegrals", "V",
+     "PPHHCoulombIntegrals has lengths [3,3,2,3], expected [3,3,2,2]"),
+])
+def test_tensor_lengths_are_checked_before_the_library_is_called(tmp_path, step, bad, msg):
+    # the C ABI takes bare pointers: a tensor of the wrong lengths must be
+    # refused by the runner, not read past its end
+    rng = np.random.default_rng(1)
+    No, Nv, NG = 2, 3, 4
+    good = {"Eh": (No,), "Ep": (Nv,), "G": (NG, No + Nv, No + Nv), "T1": (Nv, No),
+            "T2": (Nv, Nv, No, No), "V": (Nv, Nv, No, No)}
+    for n, shape in good.items():
+        if n == bad:
+            shape = shape[:-1] + (shape[-1] + 1,)
+        _write_tensor(tmp_path / ("%s.yaml" % n), rng.normal(size=shape))
+    r, out = _run(tmp_path, _read_steps(good) + """
+- name: %s
+  in:
+    CoulombVertex: $G
+    HoleEigenEnergies: $Eh
+    ParticleEigenEnergies: $Ep
+    PPHHCoulombIntegrals: $V
+    CcsdEnergy: 0.0
+    CcsdSinglesAmplitudes: $T1
+    CcsdDoublesAmplitudes: $T2
+  out: {}
+""" % step)
+    if bad is None:  # right lengths: the step reaches the library
+        assert r.returncode == 0 or "GPU context: NO_DEVICE" in out["error"], out
+        return
+    assert r.returncode == 1
+    assert msg in out["error"], out["error"]
+
+
+@pytest.mark.parametrize("header,msg", [
+    ("dimensions:\n  - type: State\nelements:\n  type: TextFile\n", "a dimension has no length"),
+    ("dimensions:\n  - length: -2\nelements:\n  type: TextFile\n", "bad dimension length -2"),
+    ("dimensions:\n  - length: 4294967296\n  - length: 4294967296\nelements:\n  type: TextFile\n",
+     "bad dimension length 4294967296"),
+    ("dimensions: 3\nelements:\n  type: TextFile\n", "dimensions must be a list"),
+    ("dimensions:\n  - length: 2\nelements: TextFile\n", "elements.type missing"),
+])
+def test_malformed_tensor_headers_are_errors(tmp_path, header, msg):
+    (tmp_path / "X.yaml").write_text("version: 100\ntype: Tensor\n" + header +
+                                     "scalarType: Real64\nunit: 1\n")
+    (tmp_path / "X.elements").write_text("1\n2\n")
+    r, out = _run(tmp_path, _read_steps(["X"]))
+    assert r.returncode == 1
+    assert msg in out["error"], out["error"]
