@@ -404,6 +404,7 @@ gbcc_status gbcc_coulomb_integrals(gbcc_ctx *ctx, int No, int Nv, int NG,
                                    double *Vijab) {
   if (!ctx || !gamma) return GBCC_BAD_ARG;
   return guard(ctx, [&]() {
+    gbcc::require(No > 0 && Nv > 0 && NG > 0, "No, Nv, NG must be positive");
     gbcc_ccsd_in ci{};
     ci.No = No; ci.Nv = Nv; ci.NG = NG;
     std::vector<double> eh(No, 0.0), ep(Nv, 0.0);
@@ -461,6 +462,7 @@ gbcc_status gbcc_energy(gbcc_ctx *ctx, int No, int Nv, const double *T1,
                         double *exchange) {
   if (!ctx || !T1 || !T2 || !Vabij) return GBCC_BAD_ARG;
   return guard(ctx, [&]() {
+    gbcc::require(No > 0 && Nv > 0, "No and Nv must be positive");
     gbcc::Context &c = ctx->c;
     const int64_t o = No, v = Nv;
     gbcc::OTen Vx(c, {v, v, o, o});
