@@ -365,6 +365,7 @@ def main():
         fms = f0e.elapsed_time(f1e)
         fp64 = {"iter_per_s": 1e3 / fms, "energy": e_fp64,
                 "energy_mixed": e_mixed, "dE_ha": e_mixed - e_fp64,
+                "dE_rel": (e_mixed - e_fp64) / abs(e_fp64) if e_fp64 else None,
                 "mixed_over_fp64": (1e3 / (ms / args.steps)) / (1e3 / fms),
                 "iterations_compared": total_it}
 

@@ -23,6 +23,11 @@ What it is: a numpy restatement of the reference's CTF statements, one
 * ``CcsdPerturbativeTriples`` (src/algorithms/CcsdPerturbativeTriples.cxx:32-248,
   src/math/Permutation.hpp:50-118)                              -> ``triples.py``
 * ``UegVertexGenerator`` (src/algorithms/UegVertexGenerator.cxx:10-229) -> ``ueg.py``
+* the complex (k-point) branch: complex integrals
+  (src/algorithms/CoulombIntegralsFromVertex.cxx:613-816), the complex
+  residual (src/algorithms/CcsdEnergyFromCoulombIntegrals.cxx:496-891), the
+  complex driver with the linear mixer, and ``CcsdPerturbativeTriplesComplex``
+  (src/algorithms/CcsdPerturbativeTriplesComplex.cxx:32-348) -> ``ccsd_complex.py``
 
 Parity pin: the reference itself cannot be built here (Cyclops CTF, MPI and
 yaml-cpp are absent), so the oracle is pinned against the golden energies of
@@ -32,5 +37,7 @@ input vertex is downloaded at test time; ``ueg.py`` regenerates the same
 system from the restated ``UegVertexGenerator`` and rotates it to a real
 (standing-wave) orbital basis, which the reference's real code path assumes.
 The oracle reproduces those three golden numbers (see
-``tests/test_oracle_pin.py``).
+``tests/test_oracle_pin.py``).  The complex branch reproduces them too, on
+the plane-wave vertex itself made complex by random orbital phases (see
+``tests/test_oracle_complex.py``).
 """
