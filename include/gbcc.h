@@ -148,6 +148,11 @@ typedef struct {
   const double *Vijka;        /* HHHPCoulombIntegrals [No,No,No,Nv] */
   const double *init_T1;      /* initialSinglesAmplitudes [Nv,No] or NULL */
   const double *init_T2;      /* initialDoublesAmplitudes [Nv,Nv,No,No] or NULL */
+  const double *fock_hp;      /* HPFockMatrix f[i,a] [No,Nv] or NULL: adds the
+                                 noncanonical term spins * T1_ai f_ia to every
+                                 iteration's energy (getEnergy,
+                                 ClusterSinglesDoublesAlgorithm.cxx:199-209).
+                                 Callers zero-initialise the struct. */
 } gbcc_ccsd_in;
 
 typedef struct {

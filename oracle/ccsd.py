@@ -58,14 +58,15 @@ def update_amplitudes(R1, R2, T1, T2, d1, d2, level_shift=0.0):
     return -R1 / (d1 + s), -R2 / (d2 + s)
 
 
-def energy(T1, T2, Vabij, spins=2.0):
-    """``getEnergy`` non-antisymmetrized branch (ClusterSinglesDoublesAlgorithm.cxx:131-197).
+def energy(T1, T2, Vabij, spins=2.0, fock_hp=None):
+    """``getEnergy`` non-antisymmetrized branch (ClusterSinglesDoublesAlgorithm.cxx:131-209).
 
     Vijab["ijab"] = Vabij["abij"] (:146), so Vijab[i,j,a,b] = Vabij[a,b,i,j]
     and Vijab[i,j,b,a] = Vabij[b,a,i,j].
       direct   = 0.5 s^2 (T2.V  + T1T1.V)           :170-172
       exchange = -0.5 s  (T2.Vx + T1T1.Vx)          :175-177
-    Returns a dict with the emitted keys (:190-196).
+      noncanonical = s T1["ai"] f["ia"]             :199-206 (HPFockMatrix given)
+    Returns a dict with the emitted keys (:190-196, :207-208).
     """
     Vx = np.einsum("baij->abij", Vabij)
     d = 0.5 * spins * spins * _e("abij,abij->", T2, Vabij)
@@ -74,8 +75,13 @@ def energy(T1, T2, Vabij, spins=2.0):
     x = x + (-0.5) * spins * _e("ai,bj,abij->", T1, T1, Vx)
     d = float(d)
     x = float(x)
-    return {"direct": d, "exchange": x, "singlet": 0.25 * d - 0.5 * x,
-            "triplet": 0.75 * d + 1.5 * x, "value": d + x}
+    out = {"direct": d, "exchange": x, "singlet": 0.25 * d - 0.5 * x,
+           "triplet": 0.75 * d + 1.5 * x, "value": d + x}
+    if fock_hp is not None:
+        nc = float(spins * _e("ai,ia->", T1, fock_hp))
+        out["noncanonical"] = nc
+        out["value"] = out["value"] + nc
+    return out
 
 
 def pair_energy(T1, T2, Vabij):
@@ -331,7 +337,7 @@ def ccsd(eps_h, eps_p, ints, gamma=None, *, mixer="LinearMixer", max_residua=4,
          mixing_ratio=1.0, max_iterations=16, energy_convergence=1e-6,
          amplitudes_convergence=1e-5, level_shift=0.0, distinguishable=0,
          ppl=1, slice_size=-1, slice_factor=None, initial=None,
-         formulation="vertex", callback=None):
+         formulation="vertex", callback=None, fock_hp=None):
     """``ClusterSinglesDoublesAlgorithm::run<double>``
     (src/algorithms/ClusterSinglesDoublesAlgorithm.cxx:38-128).
 
@@ -376,7 +382,7 @@ def ccsd(eps_h, eps_p, ints, gamma=None, *, mixer="LinearMixer", max_residua=4,
         else:
             mix.append(est, dT)
         amp = mix.get()                                           # :101
-        en = energy(amp[0], amp[1], ints["PPHH"])                 # :102
+        en = energy(amp[0], amp[1], ints["PPHH"], fock_hp=fock_hp)  # :102
         e = en["value"]
         rec = {"iteration": it + 1, "energy": en}
         if isinstance(mix, DiisMixer):
@@ -395,6 +401,6 @@ def ccsd(eps_h, eps_p, ints, gamma=None, *, mixer="LinearMixer", max_residua=4,
         prev = e
     n_iter = it + 1 if max_iterations > 0 else 0
     if max_iterations == 0:                                       # :116-119
-        e = energy(amp[0], amp[1], ints["PPHH"])["value"]
+        e = energy(amp[0], amp[1], ints["PPHH"], fock_hp=fock_hp)["value"]
     return {"energy": e, "T1": amp[0], "T2": amp[1], "iterations": n_iter,
             "converged": converged, "history": history}

@@ -35,7 +35,7 @@ class CcsdIn(C.Structure):
                 ("eps_h", _dp), ("eps_p", _dp), ("gamma", _dp),
                 ("gamma_imag", _dp), ("Vabij", _dp), ("Vaibj", _dp),
                 ("Vijkl", _dp), ("Vijka", _dp), ("init_T1", _dp),
-                ("init_T2", _dp)]
+                ("init_T2", _dp), ("fock_hp", _dp)]
 
 
 class CcsdOut(C.Structure):

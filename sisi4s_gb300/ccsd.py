@@ -80,7 +80,7 @@ def _shape(code, No, Nv):
 class CcsdInput:
     """Owns the column-major host buffers behind a ``gbcc_ccsd_in``."""
 
-    def __init__(self, eps_h, eps_p, gamma, ints=None, initial=None):
+    def __init__(self, eps_h, eps_p, gamma, ints=None, initial=None, fock_hp=None):
         eps_h, eps_p = _eigenenergies(eps_h, eps_p)
         No, Nv = eps_h.size, eps_p.size
         g, self.gamma_imag = _vertex(gamma, No, Nv)
@@ -102,12 +102,16 @@ class CcsdInput:
             t2 = _flat(initial[1], (Nv, Nv, No, No), "initial T2")
             self._keep += [t1, t2]
             s.init_T1, s.init_T2 = ptr(t1), ptr(t2)
+        if fock_hp is not None:  # HPFockMatrix f[i, a]
+            f = _flat(fock_hp, (No, Nv), "fock_hp")
+            self._keep.append(f)
+            s.fock_hp = ptr(f)
         self.s = s
 
 
 def ccsd_solve(ctx, eps_h, eps_p, gamma, ints=None, initial=None,
-               want_amplitudes=True, pair_energy=False, **opts):
-    inp = CcsdInput(eps_h, eps_p, gamma, ints, initial)
+               want_amplitudes=True, pair_energy=False, fock_hp=None, **opts):
+    inp = CcsdInput(eps_h, eps_p, gamma, ints, initial, fock_hp)
     o = make_opts(**opts)
     No, Nv = inp.No, inp.Nv
     out = capi.CcsdOut()
@@ -149,9 +153,9 @@ class Solver:
     """Device-resident solver: inputs uploaded once, iterations on demand."""
 
     def __init__(self, ctx, eps_h, eps_p, gamma, ints=None, initial=None,
-                 **opts):
+                 fock_hp=None, **opts):
         self.ctx = ctx
-        self.inp = CcsdInput(eps_h, eps_p, gamma, ints, initial)
+        self.inp = CcsdInput(eps_h, eps_p, gamma, ints, initial, fock_hp)
         self.opts = make_opts(**opts)
         h = C.c_void_p()
         ctx.check(ctx.lib.gbcc_ccsd_setup(ctx.h, C.byref(self.inp.s),

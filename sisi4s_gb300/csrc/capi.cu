@@ -318,8 +318,14 @@ gbcc_status gbcc_ccsd_solve(gbcc_ctx *ctx, const gbcc_ccsd_in *in,
   int conv = 0;
   st = gbcc_ccsd_step(s, s->opts.max_iterations, &e, &conv);
   if (st == GBCC_OK && s->opts.max_iterations == 0) {
-    // ClusterSinglesDoublesAlgorithm.cxx:116-119: energy of given amplitudes
-    // is not supported without iterating; report the zero-iteration energy
+    // ClusterSinglesDoublesAlgorithm.cxx:113-119: no iteration runs; the
+    // energy of the given (or zero) amplitudes is reported, without the
+    // non-convergence warning
+    st = guard(ctx, [&]() {
+      s->s->evaluate_energy();
+      return GBCC_OK;
+    });
+    conv = 1;
   }
   gbcc_status st2 = GBCC_OK;
   if (out) st2 = gbcc_ccsd_result(s, out);

@@ -25,6 +25,7 @@ constexpr int SC_EN = 20;      // [20..23] energy sums
 constexpr int SC_TT = 24;      // amp.amp from DIIS combine
 constexpr int SC_LAMBDA = 25;  // DIIS lambda
 constexpr int SC_LIN = 26;     // [26..27] linear mix sums
+constexpr int SC_FOCK = 28;    // T1.f (HPFockMatrix given)
 constexpr int SC_STATUS = 30;  // DIIS status (as double)
 constexpr int SC_N = 32;
 }  // namespace
@@ -99,6 +100,14 @@ std::unique_ptr<CcsdInputs> upload_inputs(Context &ctx, const gbcc_ccsd_in &in,
   }
   p->Vx = OTen(ctx, {Nv, Nv, No, No});
   assign(ctx, 1.0, p->Vabij, "baij", 0.0, p->Vx, "abij");
+  if (in.fock_hp) {
+    // f[i,a] is kept as f[a,i], so the noncanonical energy term is a plain
+    // dot with T1[a,i]
+    std::vector<double> fai((size_t)(Nv * No));
+    for (int64_t i = 0; i < No; ++i)
+      for (int64_t a = 0; a < Nv; ++a) fai[a + Nv * i] = in.fock_hp[i + No * a];
+    up(p->fock_ai, fai.data(), {Nv, No});
+  }
   return p;
 }
 
@@ -411,10 +420,51 @@ void Ccsd::iteration_body() {
     }
     amp = E_.as<double>();                                         // becomes T below
   }
-  energy_terms(ctx, amp, amp + L_.off2, in_->Vabij.p(), in_->Vx.p(), L_.Nv,
-               L_.No, partials_.as<double>(), sc + SC_EN);         // :102
+  energy_sums(amp);                                                // :102
   GBCC_CUDA(cudaMemcpyAsync(pinned_, sc, sizeof(double) * SC_N,
                             cudaMemcpyDeviceToHost, ctx.stream));
+}
+
+// the device sums getEnergy needs for the amplitudes at amp (T1 then T2)
+void Ccsd::energy_sums(const double *amp) {
+  Context &ctx = ctx_;
+  double *sc = scal_.as<double>();
+  energy_terms(ctx, amp, amp + L_.off2, in_->Vabij.p(), in_->Vx.p(), L_.Nv,
+               L_.No, partials_.as<double>(), sc + SC_EN);
+  if (in_->fock_ai.p())                                            // :199-202
+    gemm(ctx, false, false, 1, 1, L_.Nv * L_.No, 1.0, amp, 1, in_->fock_ai.p(),
+         L_.Nv * L_.No, 0.0, sc + SC_FOCK, 1);
+}
+
+// getEnergy (ClusterSinglesDoublesAlgorithm.cxx:131-209) from the sums
+void Ccsd::energy_from_sums(const double *h, IterInfo &info) const {
+  const double spins = 2.0;
+  double d = 0.5 * spins * spins * h[SC_EN + 0];                   // :170-172
+  d = d + 0.5 * spins * spins * h[SC_EN + 1];
+  double x = (-0.5) * spins * h[SC_EN + 2];                        // :175-177
+  x = x + (-0.5) * spins * h[SC_EN + 3];
+  info.direct = d;
+  info.exchange = x;
+  info.energy = d + x;                                             // :189
+  if (in_->fock_ai.p()) {                                          // :202-206
+    info.noncanonical = spins * h[SC_FOCK];
+    info.energy += info.noncanonical;
+  }
+}
+
+void Ccsd::evaluate_energy() {
+  // ClusterSinglesDoublesAlgorithm.cxx:116-119: with maxIterations 0 the
+  // energy of the given amplitudes is reported
+  Context &ctx = ctx_;
+  energy_sums(T_.as<double>());
+  GBCC_CUDA(cudaMemcpyAsync(pinned_, scal_.as<double>(), sizeof(double) * SC_N,
+                            cudaMemcpyDeviceToHost, ctx.stream));
+  ctx.check_device_errors();
+  IterInfo info;
+  energy_from_sums(pinned_, info);
+  e_ = info.energy;
+  dir_ = info.direct;
+  exc_ = info.exchange;
 }
 
 IterInfo Ccsd::iterate() {
@@ -476,14 +526,7 @@ IterInfo Ccsd::iterate() {
   }
   ctx.check_device_errors();  // the one host synchronisation per iteration
   const double *h = pinned_;
-  const double spins = 2.0;
-  double d = 0.5 * spins * spins * h[SC_EN + 0];                   // :170-172
-  d = d + 0.5 * spins * spins * h[SC_EN + 1];
-  double x = (-0.5) * spins * h[SC_EN + 2];                        // :175-177
-  x = x + (-0.5) * spins * h[SC_EN + 3];
-  info.direct = d;
-  info.exchange = x;
-  info.energy = d + x;                                             // :189
+  energy_from_sums(h, info);
   info.dtdt = h[SC_UPD + 0];
   info.tt = (o_.mixer == 1) ? h[SC_TT] : h[SC_UPD + 1];
   info.lambda = h[SC_LAMBDA];

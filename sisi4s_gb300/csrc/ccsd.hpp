@@ -13,6 +13,7 @@ struct CcsdInputs {
   OTen eps_h, eps_p;          // [No], [Nv]
   OTen Gai, Gab, Gij;         // [NG,Nv,No], [NG,Nv,Nv], [NG,No,No]
   OTen Vabij, Vx, Vaibj, Vijkl, Vijka;  // Vx[a,b,i,j] = Vabij[b,a,i,j]
+  OTen fock_ai;               // HPFockMatrix as f[a,i] [Nv,No], if given
 };
 
 // Upload eps and Gamma, slice the vertex blocks, upload or build the
@@ -21,7 +22,8 @@ std::unique_ptr<CcsdInputs> upload_inputs(Context &ctx, const gbcc_ccsd_in &in,
                                           int precision, bool need_vaibj);
 
 struct IterInfo {
-  double energy = 0, direct = 0, exchange = 0, dtdt = 0, tt = 0, lambda = 0;
+  double energy = 0, direct = 0, exchange = 0, noncanonical = 0, dtdt = 0, tt = 0,
+         lambda = 0;
   int diis_status = 0;
 };
 
@@ -50,6 +52,8 @@ class Ccsd {
   const std::vector<double> &history() const { return hist_; }
   void pair_energies(double *dev_out);
   int64_t slice_size() const { return slice_; }
+  // energy of the current amplitudes without iterating (maxIterations 0)
+  void evaluate_energy();
 
  private:
   Context &ctx_;
@@ -79,6 +83,8 @@ class Ccsd {
   std::vector<Graph> graphs_;
   uint64_t swaps_ = 0;
   void iteration_body();
+  void energy_sums(const double *amp);
+  void energy_from_sums(const double *h, IterInfo &info) const;
 };
 
 }  // namespace gbcc

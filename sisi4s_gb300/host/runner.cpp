@@ -565,6 +565,7 @@ struct CcsdEnergyFromCoulombIntegrals : Algorithm {
     in.Vijka = tensor_or_null("HHHPCoulombIntegrals", {o1, o1, o1, v1});
     in.init_T1 = tensor_or_null("initialSinglesAmplitudes", {v1, o1});
     in.init_T2 = tensor_or_null("initialDoublesAmplitudes", {v1, v1, o1, o1});
+    in.fock_hp = tensor_or_null("HPFockMatrix", {o1, v1});
     auto t1 = std::make_shared<HTensor>(), t2 = std::make_shared<HTensor>(),
          pe = std::make_shared<HTensor>();
     t1->lens = {v1, o1};

@@ -211,6 +211,7 @@ def _read_steps(names):
      "CcsdDoublesAmplitudes has lengths [3,3,2,3], expected [3,3,2,2]"),
     ("CcsdEnergyFromCoulombIntegrals", "V",
      "PPHHCoulombIntegrals has lengths [3,3,2,3], expected [3,3,2,2]"),
+    ("CcsdEnergyFromCoulombIntegrals", "F", "HPFockMatrix has lengths [2,4], expected [2,3]"),
 ])
 def test_tensor_lengths_are_checked_before_the_library_is_called(tmp_path, step, bad, msg):
     # the C ABI takes bare pointers: a tensor of the wrong lengths must be
@@ -218,7 +219,7 @@ def test_tensor_lengths_are_checked_before_the_library_is_called(tmp_path, step,
     rng = np.random.default_rng(1)
     No, Nv, NG = 2, 3, 4
     good = {"Eh": (No,), "Ep": (Nv,), "G": (NG, No + Nv, No + Nv), "T1": (Nv, No),
-            "T2": (Nv, Nv, No, No), "V": (Nv, Nv, No, No)}
+            "T2": (Nv, Nv, No, No), "V": (Nv, Nv, No, No), "F": (No, Nv)}
     for n, shape in good.items():
         if n == bad:
             shape = shape[:-1] + (shape[-1] + 1,)
@@ -230,6 +231,7 @@ def test_tensor_lengths_are_checked_before_the_library_is_called(tmp_path, step,
     HoleEigenEnergies: $Eh
     ParticleEigenEnergies: $Ep
     PPHHCoulombIntegrals: $V
+    HPFockMatrix: $F
     CcsdEnergy: 0.0
     CcsdSinglesAmplitudes: $T1
     CcsdDoublesAmplitudes: $T2
@@ -257,3 +259,37 @@ def test_malformed_tensor_headers_are_errors(tmp_path, header, msg):
     r, out = _run(tmp_path, _read_steps(["X"]))
     assert r.returncode == 1
     assert msg in out["error"], out["error"]
+
+
+def test_ctypes_structs_match_the_c_header(tmp_path):
+    """Every struct the Python binding mirrors has the C header's size and
+    field offsets (compiled with the host C compiler)."""
+    from sisi4s_gb300 import capi
+    from sisi4s_gb300.serve import Result, ServerOpts
+    mirrors = {"gbcc_ccsd_opts": capi.CcsdOpts, "gbcc_ccsd_in": capi.CcsdIn,
+               "gbcc_ccsd_out": capi.CcsdOut, "gbcc_triples_in": capi.TriplesIn,
+               "gbcc_server_opts": ServerOpts, "gbcc_result": Result}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "gbcc.h"',
+             'int main(void) {']
+    for cname, py in mirrors.items():
+        lines.append('printf("%s size %%zu\\n", sizeof(%s));' % (cname, cname))
+        for f, _ in py._fields_:
+            lines.append('printf("%s %s %%zu\\n", offsetof(%s, %s));'
+                         % (cname, f, cname, f))
+    lines += ['return 0;', '}']
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", "-I", os.path.join(ROOT, "include"), str(src),
+                    "-o", str(exe)], check=True, capture_output=True, text=True)
+    got = {}
+    for line in subprocess.run([str(exe)], check=True, capture_output=True,
+                               text=True).stdout.split("\n"):
+        if line:
+            name, field, value = line.split()
+            got[(name, field)] = int(value)
+    import ctypes
+    for cname, py in mirrors.items():
+        assert got[(cname, "size")] == ctypes.sizeof(py), cname
+        for f, _ in py._fields_:
+            assert got[(cname, f)] == getattr(py, f).offset, (cname, f)
