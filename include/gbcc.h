@@ -193,6 +193,44 @@ gbcc_status gbcc_ccsd_residual(gbcc_ctx *ctx, const gbcc_ccsd_in *in,
                                const double *T1, const double *T2,
                                double *R1, double *R2);
 
+/* ------------------------------------------------------- complex CCSD */
+/* The complex (k-point) branch of the same algorithm: ClusterSinglesDoubles
+ * Algorithm::run<complex> (src/algorithms/ClusterSinglesDoublesAlgorithm.cxx:
+ * 25-128) with CcsdEnergyFromCoulombIntegrals::getResiduum for complex
+ * amplitudes (src/algorithms/CcsdEnergyFromCoulombIntegrals.cxx:496-891) and
+ * the complex integrals of CoulombIntegralsFromVertex (:613-816).  Complex
+ * tensors are interleaved (re, im) pairs in the reference's dense layout, as
+ * CTF stores complex<double>.  Only the linear mixer exists for complex
+ * amplitudes: the reference's complex DIIS solve is unimplemented
+ * (src/mixers/DiisMixer.cxx:43-48), and DiisMixer gives GBCC_BAD_ARG. */
+typedef struct {
+  int No, Nv, NG;
+  const double *eps_h;        /* HoleEigenEnergies [No] (real) */
+  const double *eps_p;        /* ParticleEigenEnergies [Nv] (real) */
+  const double *gamma;        /* CoulombVertex, complex [NG,Np,Np] */
+  const double *init_T1;      /* initialSinglesAmplitudes, complex [Nv,No] or NULL */
+  const double *init_T2;      /* initialDoublesAmplitudes, complex [Nv,Nv,No,No] or NULL */
+} gbcc_ccsd_complex_in;
+
+typedef struct {
+  double energy[2];           /* (re, im); CcsdEnergy is the real part (:32) */
+  double direct[2], exchange[2];
+  int iterations;
+  int converged;
+  double *T1;                 /* optional caller buffer, complex [Nv,No] */
+  double *T2;                 /* optional caller buffer, complex [Nv,Nv,No,No] */
+  double *energy_history;     /* optional [2*max_iterations]: (re, im) per iteration */
+} gbcc_ccsd_complex_out;
+
+gbcc_status gbcc_ccsd_solve_complex(gbcc_ctx *ctx, const gbcc_ccsd_complex_in *in,
+                                    const gbcc_ccsd_opts *opts,
+                                    gbcc_ccsd_complex_out *out);
+/* One complex getResiduum call: R = residual(it, T), complex buffers. */
+gbcc_status gbcc_ccsd_residual_complex(gbcc_ctx *ctx, const gbcc_ccsd_complex_in *in,
+                                       const gbcc_ccsd_opts *opts, int it,
+                                       const double *T1, const double *T2,
+                                       double *R1, double *R2);
+
 /* ---------------------------------------------------------------- (T) */
 /* Replaces CcsdPerturbativeTriples::run (src/algorithms/CcsdPerturbativeTriples.cxx:119-248).
  * e_total = e_ccsd + E_(T) (the reference's CcsdPerturbativeTriplesEnergy),

@@ -45,6 +45,19 @@ class CcsdOut(C.Structure):
                 ("pair_energy", _dp), ("energy_history", _dp)]
 
 
+class ComplexIn(C.Structure):
+    _fields_ = [("No", C.c_int), ("Nv", C.c_int), ("NG", C.c_int),
+                ("eps_h", _dp), ("eps_p", _dp), ("gamma", _dp),
+                ("init_T1", _dp), ("init_T2", _dp)]
+
+
+class ComplexOut(C.Structure):
+    _fields_ = [("energy", C.c_double * 2), ("direct", C.c_double * 2),
+                ("exchange", C.c_double * 2), ("iterations", C.c_int),
+                ("converged", C.c_int), ("T1", _dp), ("T2", _dp),
+                ("energy_history", _dp)]
+
+
 class TriplesIn(C.Structure):
     _fields_ = [("No", C.c_int), ("Nv", C.c_int), ("NG", C.c_int),
                 ("eps_h", _dp), ("eps_p", _dp), ("gamma", _dp),
@@ -83,6 +96,11 @@ _SIGS = {
     "gbcc_ccsd_residual": (C.c_int, [C.c_void_p, C.POINTER(CcsdIn),
                                      C.POINTER(CcsdOpts), C.c_int, _dp, _dp,
                                      _dp, _dp]),
+    "gbcc_ccsd_solve_complex": (C.c_int, [C.c_void_p, C.POINTER(ComplexIn),
+                                          C.POINTER(CcsdOpts), C.POINTER(ComplexOut)]),
+    "gbcc_ccsd_residual_complex": (C.c_int, [C.c_void_p, C.POINTER(ComplexIn),
+                                             C.POINTER(CcsdOpts), C.c_int, _dp, _dp,
+                                             _dp, _dp]),
     "gbcc_triples": (C.c_int, [C.c_void_p, C.POINTER(TriplesIn), C.c_int,
                                _dp, _dp]),
     "gbcc_triples_from_solver": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp]),

@@ -12,7 +12,8 @@ from . import capi
 from .capi import fortran_flat, from_fortran_flat, ptr
 
 __all__ = ["make_opts", "CcsdInput", "ccsd_solve", "ccsd_residual", "Solver",
-           "triples", "coulomb_integrals", "energy"]
+           "triples", "coulomb_integrals", "energy", "ComplexInput",
+           "ccsd_solve_complex", "ccsd_residual_complex"]
 
 
 def make_opts(mixer="LinearMixer", max_residua=4, mixing_ratio=1.0,
@@ -252,3 +253,89 @@ def coulomb_integrals(ctx, gamma, No):
             "HHHH": from_fortran_flat(vijkl, (No, No, No, No)),
             "HHHP": from_fortran_flat(vijka, (No, No, No, Nv)),
             "HHPP": from_fortran_flat(vijab, (No, No, Nv, Nv))}
+
+
+# ------------------------------------------------------------- complex branch
+def complex_flat(arr, shape, name):
+    """Interleaved (re, im) column-major copy of a complex tensor, after
+    checking its shape: the layout of CTF's complex<double> tensors."""
+    a = np.asarray(arr)
+    if a.shape != tuple(shape):
+        raise ValueError("%s has shape %s, expected %s" % (name, a.shape, tuple(shape)))
+    z = np.ascontiguousarray(np.asarray(a, dtype=np.complex128).transpose(
+        tuple(range(a.ndim - 1, -1, -1)))).ravel()
+    return z.view(np.float64)
+
+
+def from_complex_flat(flat, shape):
+    z = np.asarray(flat).view(np.complex128)
+    return z.reshape(tuple(reversed(shape))).transpose(
+        tuple(range(len(shape) - 1, -1, -1)))
+
+
+class ComplexInput:
+    """Owns the host buffers behind a ``gbcc_ccsd_complex_in``."""
+
+    def __init__(self, eps_h, eps_p, gamma, initial=None):
+        eps_h, eps_p = _eigenenergies(eps_h, eps_p)
+        No, Nv = eps_h.size, eps_p.size
+        g = np.asarray(gamma)
+        if g.ndim != 3 or not g.shape[0]:
+            raise ValueError("gamma must be [NG, Np, Np]")
+        NG = g.shape[0]
+        self.No, self.Nv, self.NG = No, Nv, NG
+        gf = complex_flat(g, (NG, No + Nv, No + Nv), "gamma")
+        self._keep = [eps_h, eps_p, gf]
+        s = capi.ComplexIn()
+        s.No, s.Nv, s.NG = No, Nv, NG
+        s.eps_h, s.eps_p, s.gamma = ptr(eps_h), ptr(eps_p), ptr(gf)
+        if initial is not None:
+            t1 = complex_flat(initial[0], (Nv, No), "initial T1")
+            t2 = complex_flat(initial[1], (Nv, Nv, No, No), "initial T2")
+            self._keep += [t1, t2]
+            s.init_T1, s.init_T2 = ptr(t1), ptr(t2)
+        self.s = s
+
+
+def ccsd_solve_complex(ctx, eps_h, eps_p, gamma, initial=None, **opts):
+    """Complex CCSD (linear mixer).  Returns complex energies, the complex
+    per-iteration history and the complex amplitudes."""
+    inp = ComplexInput(eps_h, eps_p, gamma, initial)
+    o = make_opts(**opts)
+    No, Nv = inp.No, inp.Nv
+    out = capi.ComplexOut()
+    t1 = np.zeros(2 * Nv * No)
+    t2 = np.zeros(2 * Nv * Nv * No * No)
+    hist = np.zeros(2 * max(o.max_iterations, 1))
+    out.T1, out.T2, out.energy_history = ptr(t1), ptr(t2), ptr(hist)
+    st = ctx.check(ctx.lib.gbcc_ccsd_solve_complex(ctx.h, C.byref(inp.s), C.byref(o),
+                                                   C.byref(out)),
+                   allow=(capi.OK, capi.NOT_CONVERGED))
+    n = out.iterations
+    return {"energy": complex(out.energy[0], out.energy[1]),
+            "direct": complex(out.direct[0], out.direct[1]),
+            "exchange": complex(out.exchange[0], out.exchange[1]),
+            "iterations": n, "converged": bool(out.converged), "status": st,
+            "history": hist[:2 * n].view(np.complex128).copy(),
+            "T1": from_complex_flat(t1, (Nv, No)),
+            "T2": from_complex_flat(t2, (Nv, Nv, No, No))}
+
+
+def ccsd_residual_complex(ctx, it, T1, T2, eps_h, eps_p, gamma,
+                          initial_doubles=False, **opts):
+    """One complex getResiduum call; ``initial_doubles`` selects the
+    reference's behaviour when initialDoublesAmplitudes is given (no MP2
+    start at it = 0)."""
+    inp = ComplexInput(eps_h, eps_p, gamma)
+    o = make_opts(**opts)
+    No, Nv = inp.No, inp.Nv
+    t1 = complex_flat(T1, (Nv, No), "T1")
+    t2 = complex_flat(T2, (Nv, Nv, No, No), "T2")
+    if initial_doubles:
+        inp.s.init_T2 = ptr(t2)
+    r1 = np.zeros(2 * Nv * No)
+    r2 = np.zeros(2 * Nv * Nv * No * No)
+    ctx.check(ctx.lib.gbcc_ccsd_residual_complex(ctx.h, C.byref(inp.s), C.byref(o),
+                                                 int(it), ptr(t1), ptr(t2), ptr(r1),
+                                                 ptr(r2)))
+    return from_complex_flat(r1, (Nv, No)), from_complex_flat(r2, (Nv, Nv, No, No))

@@ -9,6 +9,10 @@
 namespace gbcc {
 double triples_energy(Context &ctx, const CcsdInputs &I, const double *T1,
                       const double *T2, int precision);
+gbcc_status complex_solve(Context &ctx, const gbcc_ccsd_complex_in &in,
+                          const gbcc_ccsd_opts &o, gbcc_ccsd_complex_out *out);
+void complex_residual(Context &ctx, const gbcc_ccsd_complex_in &in, const gbcc_ccsd_opts &o,
+                      int it, const double *T1, const double *T2, double *R1, double *R2);
 }
 
 struct gbcc_ctx {
@@ -359,6 +363,35 @@ gbcc_status gbcc_ccsd_residual(gbcc_ctx *ctx, const gbcc_ccsd_in *in,
                               cudaMemcpyDeviceToHost, ctx->c.stream));
     GBCC_CUDA(cudaMemcpyAsync(R2, R.as<double>() + L.off2, 8 * L.n2,
                               cudaMemcpyDeviceToHost, ctx->c.stream));
+    ctx->c.check_device_errors();
+    return GBCC_OK;
+  });
+}
+
+gbcc_status gbcc_ccsd_solve_complex(gbcc_ctx *ctx, const gbcc_ccsd_complex_in *in,
+                                    const gbcc_ccsd_opts *opts,
+                                    gbcc_ccsd_complex_out *out) {
+  if (!ctx || !in) return GBCC_BAD_ARG;
+  return guard(ctx, [&]() {
+    gbcc_ccsd_opts o;
+    if (opts) o = *opts; else gbcc_ccsd_opts_default(&o);
+    check_opts(o);
+    apply_precision_opts(ctx->c, o);
+    return gbcc::complex_solve(ctx->c, *in, o, out);
+  });
+}
+
+gbcc_status gbcc_ccsd_residual_complex(gbcc_ctx *ctx, const gbcc_ccsd_complex_in *in,
+                                       const gbcc_ccsd_opts *opts, int it,
+                                       const double *T1, const double *T2,
+                                       double *R1, double *R2) {
+  if (!ctx || !in || !T1 || !T2 || !R1 || !R2) return GBCC_BAD_ARG;
+  return guard(ctx, [&]() {
+    gbcc_ccsd_opts o;
+    if (opts) o = *opts; else gbcc_ccsd_opts_default(&o);
+    check_opts(o);
+    apply_precision_opts(ctx->c, o);
+    gbcc::complex_residual(ctx->c, *in, o, it, T1, T2, R1, R2);
     ctx->c.check_device_errors();
     return GBCC_OK;
   });

@@ -1,0 +1,228 @@
+// Complex (k-point) CCSD on the GPU: the CUDA backend of ccsd_complex.hpp.
+//
+// Every primitive maps onto a routine the real path already uses: the
+// contraction engine (permutes + FP64 or emulated GEMMs), the elementwise
+// copies, the slice gather/scatter of the ladder, the Jacobi update and the
+// linear mixer, each applied to one real plane at a time.  Interleaved
+// complex host data become two planes through one transpose of a [2, n]
+// view.
+#include <algorithm>
+#include <cmath>
+
+#include "ccsd_complex.hpp"
+#include "ccsd_kernels.hpp"
+
+namespace gbcc {
+namespace {
+
+Ten as_ten(const cx::View &v) {
+  Ten t;
+  t.p = v.p;
+  t.order = v.order;
+  t.lens = v.lens;
+  return t;
+}
+
+struct DeviceBackend {
+  Context &ctx;
+  int precision;
+
+  struct Buf {
+    DBuf mem;
+    cx::View v;
+  };
+
+  Buf alloc(std::initializer_list<int64_t> l) {
+    Buf b;
+    b.v = cx::view(nullptr, l);
+    b.mem.alloc(ctx, sizeof(double) * (size_t)std::max<int64_t>(b.v.size(), 1));
+    b.v.p = b.mem.as<double>();
+    return b;
+  }
+  void contract(double al, const cx::View &A, const char *ia, const cx::View &B,
+                const char *ib, double be, const cx::View &C, const char *ic) {
+    gbcc::contract(ctx, al, as_ten(A), ia, as_ten(B), ib, be, as_ten(C), ic, precision);
+  }
+  void assign(double al, const cx::View &A, const char *ia, double be, const cx::View &C,
+              const char *ic) {
+    gbcc::assign(ctx, al, as_ten(A), ia, be, as_ten(C), ic);
+  }
+  void fill(const cx::View &x, double v) { gbcc::fill(ctx, x.p, x.size(), v); }
+  void axpby(double a, const cx::View &x, double b, const cx::View &y) {
+    require(x.size() == y.size(), "axpby: size mismatch");
+    gbcc::axpby(ctx, y.size(), a, x.p, b, y.p);
+  }
+  void gather_slice(const cx::View &dst, const cx::View &src, int64_t x0, int64_t nx) {
+    require(dst.lens[0] == src.lens[0] && dst.lens[1] == nx && dst.lens[2] == src.lens[1] &&
+                x0 + nx <= src.lens[1],
+            "gather_slice: bad shape");
+    gbcc::gather_slice(ctx, dst.p, src.p, src.lens[0], src.lens[1], x0, nx);
+  }
+  void slice_add(const cx::View &R, const cx::View &Rxy, int64_t a0, int64_t b0, bool mirror) {
+    require(a0 + Rxy.lens[0] <= R.lens[0] && b0 + Rxy.lens[1] <= R.lens[1],
+            "slice_add: out of range");
+    gbcc::slice_add(ctx, R.p, Rxy.p, R.lens[0], R.lens[2], a0, b0, Rxy.lens[0],
+                    Rxy.lens[1], mirror);
+  }
+  void vertex_block(const cx::View &dst, const cx::View &src, int64_t p0, int64_t np,
+                    int64_t q0, int64_t nq) {
+    require(p0 + np <= src.lens[1] && q0 + nq <= src.lens[2], "vertex_block: out of range");
+    gbcc::vertex_block(ctx, dst.p, src.p, src.lens[0], src.lens[1], p0, np, q0, nq);
+  }
+  void read_sums(const double *dev, double *host, int n) {
+    GBCC_CUDA(cudaMemcpyAsync(host, dev, sizeof(double) * n, cudaMemcpyDeviceToHost,
+                              ctx.stream));
+    ctx.check_device_errors();
+  }
+  void jacobi(const cx::Layout &L, const cx::View &eh, const cx::View &ep, const cx::View &R,
+              const cx::View &T, const cx::View &est, const cx::View &dT, double shift,
+              double sums[2]) {
+    const FockLayout fl(L.Nv, L.No);
+    require(fl.ntot == L.ntot && R.size() == L.ntot, "jacobi: layout mismatch");
+    DBuf part(ctx, sizeof(double) * reduction_blocks(ctx, fl.ntot) * 2), out(ctx, 16);
+    jacobi_update(ctx, fl, R.p, T.p, est.p, dT.p, eh.p, ep.p, shift, 0, nullptr,
+                  part.as<double>(), out.as<double>());
+    read_sums(out.as<double>(), sums, 2);
+  }
+  void linear_mix(const cx::View &next, const cx::View &nres, const cx::View &last,
+                  const cx::View &lres, double r, double sums[2]) {
+    const int64_t n = next.size();
+    DBuf part(ctx, sizeof(double) * reduction_blocks(ctx, n) * 2), out(ctx, 16);
+    gbcc::linear_mix(ctx, next.p, nres.p, last.p, lres.p, r, n, part.as<double>(),
+                     out.as<double>());
+    read_sums(out.as<double>(), sums, 2);
+  }
+  double scalar(const cx::View &x) {
+    double h = 0.0;
+    read_sums(x.p, &h, 1);
+    return h;
+  }
+  Buf load_real(const double *h, std::initializer_list<int64_t> l) {
+    Buf b = alloc(l);
+    GBCC_CUDA(cudaMemcpyAsync(b.v.p, h, sizeof(double) * b.v.size(),
+                              cudaMemcpyHostToDevice, ctx.stream));
+    return b;
+  }
+  // interleaved [2, n] on the host -> [n, 2] on the device -> two planes
+  void load_complex(const double *h, const cx::CView &dst) {
+    const int64_t n = dst.re.size();
+    DBuf a(ctx, 16 * n), b(ctx, 16 * n);
+    GBCC_CUDA(cudaMemcpyAsync(a.as<double>(), h, 16 * n, cudaMemcpyHostToDevice,
+                              ctx.stream));
+    gbcc::assign(ctx, 1.0, ten(a.as<double>(), {2, n}), "zn", 0.0,
+                 ten(b.as<double>(), {n, 2}), "nz");
+    gbcc::copy(ctx, dst.re.p, b.as<double>(), n);
+    gbcc::copy(ctx, dst.im.p, b.as<double>() + n, n);
+  }
+  void store_complex(const cx::CView &src, double *h) {
+    const int64_t n = src.re.size();
+    DBuf a(ctx, 16 * n), b(ctx, 16 * n);
+    gbcc::copy(ctx, b.as<double>(), src.re.p, n);
+    gbcc::copy(ctx, b.as<double>() + n, src.im.p, n);
+    gbcc::assign(ctx, 1.0, ten(b.as<double>(), {n, 2}), "nz", 0.0,
+                 ten(a.as<double>(), {2, n}), "zn");
+    GBCC_CUDA(cudaMemcpyAsync(h, a.as<double>(), 16 * n, cudaMemcpyDeviceToHost,
+                              ctx.stream));
+    ctx.check_device_errors();
+  }
+};
+
+cx::HostIn host_in(const gbcc_ccsd_complex_in &in) {
+  require(in.No > 0 && in.Nv > 0 && in.NG > 0, "No, Nv, NG must be positive");
+  require(in.eps_h && in.eps_p && in.gamma, "eigenenergies and the vertex are required");
+  cx::HostIn h;
+  h.No = in.No;
+  h.Nv = in.Nv;
+  h.NG = in.NG;
+  h.eps_h = in.eps_h;
+  h.eps_p = in.eps_p;
+  h.gamma = in.gamma;
+  h.init_T1 = in.init_T1;
+  h.init_T2 = in.init_T2;
+  return h;
+}
+
+// integralsSliceSize: given, else the real path's device default (Nv / 8, at
+// least 16), capped so that one complex V_xycd slice stays within 4 GiB
+int64_t slice_size(const gbcc_ccsd_opts &o, int64_t Nv) {
+  int64_t s;
+  if (o.integrals_slice_size > 0) s = o.integrals_slice_size;
+  else if (o.integrals_slice_factor >= 0) s = (int64_t)(Nv * o.integrals_slice_factor);
+  else {
+    const double budget = 4.0 * 1024 * 1024 * 1024 / 16.0;
+    const int64_t cap = (int64_t)std::floor(std::sqrt(budget / (double)(Nv * Nv)));
+    s = std::min<int64_t>(cap, std::max<int64_t>(16, Nv / 8));
+  }
+  return std::max<int64_t>(1, std::min<int64_t>(s, Nv));
+}
+
+}  // namespace
+
+void complex_residual(Context &ctx, const gbcc_ccsd_complex_in &in, const gbcc_ccsd_opts &o,
+                      int it, const double *T1, const double *T2, double *R1, double *R2) {
+  DeviceBackend rb{ctx, o.precision};
+  cx::Inputs<DeviceBackend> I;
+  cx::CBuf<DeviceBackend> T;
+  cx::HostIn h = host_in(in);
+  h.init_T1 = T1;
+  h.init_T2 = T2;
+  cx::setup(rb, I, h, T);
+  cx::ResidualOpts ro;
+  // getResiduum's MP2 start depends on whether initial doubles were given
+  ro.init_doubles = in.init_T2 != nullptr;
+  ro.distinguishable = o.distinguishable != 0;
+  ro.ppl = o.ppl != 0;
+  ro.slice = slice_size(o, in.Nv);
+  const cx::Layout L(in.Nv, in.No);
+  auto R = cx::cbuf(rb, {L.ntot});
+  cx::residual(rb, I, it, ro, cx::t1_of(T, L), cx::t2_of(T, L), cx::t1_of(R, L),
+               cx::t2_of(R, L));
+  rb.store_complex(cx::t1_of(R, L), R1);
+  rb.store_complex(cx::t2_of(R, L), R2);
+}
+
+gbcc_status complex_solve(Context &ctx, const gbcc_ccsd_complex_in &in,
+                          const gbcc_ccsd_opts &o, gbcc_ccsd_complex_out *out) {
+  require(o.mixer == 0,
+          "DiisMixer is not available for complex amplitudes: the reference's complex "
+          "DIIS solve is unimplemented (src/mixers/DiisMixer.cxx:43-48)");
+  DeviceBackend rb{ctx, o.precision};
+  cx::Inputs<DeviceBackend> I;
+  cx::CBuf<DeviceBackend> T;
+  cx::SolveOpts so;
+  so.res.init_doubles = cx::setup(rb, I, host_in(in), T);
+  so.res.distinguishable = o.distinguishable != 0;
+  so.res.ppl = o.ppl != 0;
+  so.res.slice = slice_size(o, in.Nv);
+  so.max_iterations = o.max_iterations;
+  so.energy_convergence = o.energy_convergence;
+  so.amplitudes_convergence = o.amplitudes_convergence;
+  so.level_shift = o.level_shift;
+  so.mixing_ratio = o.mixing_ratio;
+  const cx::SolveResult r = cx::solve(rb, I, so, T);
+  for (const auto &e : r.history)
+    if (!std::isfinite(e.real()) || !std::isfinite(e.imag()))
+      throw Error(GBCC_DIVERGED, "the complex CCSD energy is not finite");
+  if (out) {
+    out->energy[0] = r.energy.value.real();
+    out->energy[1] = r.energy.value.imag();
+    out->direct[0] = r.energy.direct.real();
+    out->direct[1] = r.energy.direct.imag();
+    out->exchange[0] = r.energy.exchange.real();
+    out->exchange[1] = r.energy.exchange.imag();
+    out->iterations = r.iterations;
+    out->converged = r.converged ? 1 : 0;
+    const cx::Layout L(in.Nv, in.No);
+    if (out->T1) rb.store_complex(cx::t1_of(T, L), out->T1);
+    if (out->T2) rb.store_complex(cx::t2_of(T, L), out->T2);
+    if (out->energy_history)
+      for (size_t q = 0; q < r.history.size(); ++q) {
+        out->energy_history[2 * q] = r.history[q].real();
+        out->energy_history[2 * q + 1] = r.history[q].imag();
+      }
+  }
+  ctx.check_device_errors();
+  return (r.converged || o.max_iterations == 0) ? GBCC_OK : GBCC_NOT_CONVERGED;
+}
+
+}  // namespace gbcc

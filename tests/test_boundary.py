@@ -268,6 +268,8 @@ def test_ctypes_structs_match_the_c_header(tmp_path):
     from sisi4s_gb300.serve import Result, ServerOpts
     mirrors = {"gbcc_ccsd_opts": capi.CcsdOpts, "gbcc_ccsd_in": capi.CcsdIn,
                "gbcc_ccsd_out": capi.CcsdOut, "gbcc_triples_in": capi.TriplesIn,
+               "gbcc_ccsd_complex_in": capi.ComplexIn,
+               "gbcc_ccsd_complex_out": capi.ComplexOut,
                "gbcc_server_opts": ServerOpts, "gbcc_result": Result}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "gbcc.h"',
              'int main(void) {']

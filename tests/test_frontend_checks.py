@@ -59,3 +59,21 @@ def test_bad_vertex_and_amplitudes_are_refused(system):
                     np.zeros((No, Nv)), np.zeros((Nv, Nv, No, No)))
     with pytest.raises(ValueError, match="No must"):
         gpu.coulomb_integrals(None, system.gamma, No + Nv)
+
+
+def test_complex_front_end_layout_and_checks(system):
+    g = system.gamma.astype(complex)
+    g[2, 1, 4] += 0.5j
+    inp = gpu.ComplexInput(system.eps_h, system.eps_p, g)
+    # interleaved (re, im), first index fastest: element (G, p, q) at
+    # 2 * (G + p*NG + q*NG*Np)
+    Np = No + Nv
+    e = 2 + 1 * NG + 4 * NG * Np
+    assert inp._keep[2][2 * e + 1] == 0.5 and inp._keep[2][2 * e] == g[2, 1, 4].real
+    with pytest.raises(ValueError, match="gamma"):
+        gpu.ComplexInput(system.eps_h, system.eps_p, g[:, :-1, :])
+    with pytest.raises(ValueError, match="initial T2"):
+        gpu.ComplexInput(system.eps_h, system.eps_p, g,
+                         initial=(np.zeros((Nv, No)), np.zeros((Nv, Nv, No))))
+    z = (np.arange(6) + 1j * np.arange(6)).reshape(2, 3)
+    assert np.array_equal(gpu.from_complex_flat(gpu.complex_flat(z, (2, 3), "z"), (2, 3)), z)

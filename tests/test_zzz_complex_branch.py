@@ -1,0 +1,111 @@
+"""Complex (k-point) CCSD through the C ABI against the complex oracle (GPU).
+
+The statement sequence is shared with the host-backend check of
+``tests/test_complex_program.py``; these tests run it on the device.  This
+file is collected after the other GPU tests on purpose, so that a failure
+here cannot stop them in a run that stops at the first failure.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from oracle.ccsd_complex import ccsd_complex, coulomb_integrals_complex, residual_complex
+from oracle.ueg import UEG_GOLDEN, ueg_planewave
+from sisi4s_gb300 import capi
+from sisi4s_gb300 import ccsd as gpu
+from sisi4s_gb300.inputs import make_system
+
+pytestmark = pytest.mark.gpu
+
+
+def _system(No, Nv, NG, seed):
+    s = make_system(No, Nv, NG, seed=seed)
+    rng = np.random.default_rng(seed + 100)
+    W, _ = np.linalg.qr(rng.normal(size=(NG, NG)) + 1j * rng.normal(size=(NG, NG)))
+    ph = np.exp(1j * rng.uniform(0, 2 * np.pi, No + Nv))
+    g = np.einsum("GH,Hpq->Gpq", W, np.conj(ph)[None, :, None] * s.gamma * ph[None, None, :])
+    T1 = rng.normal(0, 0.05, (Nv, No)) + 1j * rng.normal(0, 0.05, (Nv, No))
+    T2 = rng.normal(0, 0.05, (Nv, Nv, No, No)) + 1j * rng.normal(0, 0.05, (Nv, Nv, No, No))
+    return s, g, T1, 0.5 * (T2 + T2.transpose(1, 0, 3, 2))
+
+
+def _rel(a, b):
+    return np.abs(a - b).max() / np.abs(b).max()
+
+
+@pytest.mark.parametrize("No,Nv,NG,dist,ppl,slice_size", [
+    (3, 7, 11, 0, 1, -1), (3, 9, 14, 1, 1, 2), (2, 10, 12, 0, 0, -1), (4, 11, 20, 0, 1, 4)])
+def test_complex_residual_matches_oracle(ctx, No, Nv, NG, dist, ppl, slice_size):
+    s, g, T1, T2 = _system(No, Nv, NG, seed=No + Nv)
+    ci = coulomb_integrals_complex(g, No)
+    r1, r2 = gpu.ccsd_residual_complex(ctx, 1, T1, T2, s.eps_h, s.eps_p, g,
+                                       initial_doubles=True, distinguishable=dist,
+                                       ppl=ppl, slice_size=slice_size)
+    o1, o2 = residual_complex(1, T1, T2, ci, g, distinguishable=dist, ppl=ppl,
+                              slice_size=slice_size, initial_doubles=True)
+    assert _rel(r1, o1) < 1e-12 and _rel(r2, o2) < 1e-12
+
+
+def test_complex_residual_emulated_matches_oracle(ctx):
+    No, Nv, NG = 4, 40, 64
+    s, g, T1, T2 = _system(No, Nv, NG, seed=9)
+    ci = coulomb_integrals_complex(g, No)
+    ctx.set_emulation(6, 0.0)  # every GEMM emulated
+    try:
+        r1, r2 = gpu.ccsd_residual_complex(ctx, 1, T1, T2, s.eps_h, s.eps_p, g,
+                                           initial_doubles=True, precision="emu",
+                                           slice_size=16)
+    finally:
+        ctx.set_emulation(6, 1e7)
+    o1, o2 = residual_complex(1, T1, T2, ci, g, slice_size=16, initial_doubles=True)
+    assert _rel(r1, o1) < 1e-10 and _rel(r2, o2) < 1e-10
+
+
+@pytest.mark.parametrize("ratio", [1.0, 0.7])
+def test_complex_iterations_match_oracle(ctx, ratio):
+    No, Nv, NG = 3, 9, 14
+    s, g, _, _ = _system(No, Nv, NG, seed=6)
+    ci = coulomb_integrals_complex(g, No)
+    kw = dict(mixing_ratio=ratio, max_iterations=40, energy_convergence=1e-10,
+              amplitudes_convergence=1e-8, slice_size=2)
+    ref = ccsd_complex(s.eps_h, s.eps_p, ci, g, **kw)
+    got = gpu.ccsd_solve_complex(ctx, s.eps_h, s.eps_p, g, **kw)
+    rh = np.array([h["energy"]["value"] for h in ref["history"]])
+    assert got["iterations"] == ref["iterations"] and got["converged"] == ref["converged"]
+    assert np.abs(got["history"] - rh).max() < 1e-12
+    assert _rel(got["T2"], ref["T2"]) < 1e-9
+
+
+def test_real_vertex_through_the_complex_branch_equals_the_real_branch(ctx):
+    s = make_system(4, 12, 30, seed=5)
+    kw = dict(max_iterations=6, energy_convergence=0.0, amplitudes_convergence=0.0)
+    real = gpu.ccsd_solve(ctx, s.eps_h, s.eps_p, s.gamma, **kw)
+    cplx = gpu.ccsd_solve_complex(ctx, s.eps_h, s.eps_p, s.gamma.astype(complex), **kw)
+    assert np.abs(cplx["history"].real - np.array(real["history"])).max() < 1e-12
+    assert np.abs(cplx["history"].imag).max() < 1e-15
+
+
+def test_ueg_golden_through_the_complex_branch(ctx):
+    """The reference's UEG test on its own plane-wave vertex, made complex by
+    random orbital phases, with the linear mixer (no complex DIIS exists)."""
+    gd = UEG_GOLDEN
+    _, eps, gam, _ = ueg_planewave(gd["No"], gd["Nv"], gd["rs"])
+    ph = np.exp(1j * np.random.default_rng(11).uniform(0, 2 * np.pi, gam.shape[1]))
+    gam = np.conj(ph)[None, :, None] * gam * ph[None, None, :]
+    n = gd["No"]
+    r = gpu.ccsd_solve_complex(ctx, eps[:n], eps[n:], gam, max_iterations=60,
+                               energy_convergence=1e-11, amplitudes_convergence=1e-9)
+    assert r["converged"]
+    assert abs(r["history"][0].real - gd["mp2"]) < 1e-12
+    assert abs(r["energy"].real - gd["ccsd"]) < 1e-8 * abs(gd["ccsd"])
+    assert abs(r["energy"].imag) < 1e-14
+
+
+def test_complex_diis_is_refused(ctx):
+    s, g, _, _ = _system(2, 5, 7, seed=1)
+    inp = gpu.ComplexInput(s.eps_h, s.eps_p, g)
+    o = gpu.make_opts(mixer="DiisMixer")
+    out = capi.ComplexOut()
+    st = ctx.lib.gbcc_ccsd_solve_complex(ctx.h, C.byref(inp.s), C.byref(o), C.byref(out))
+    assert st == capi.BAD_ARG
