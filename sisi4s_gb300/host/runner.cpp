@@ -526,8 +526,95 @@ int precision_of(const Algorithm &a) {
   throw StepError("precision must be fp64 or emu");
 }
 
+bool has_imaginary_part(const HTensor &t) {
+  if (!t.complex) return false;
+  for (double v : t.im)
+    if (v != 0.0) return true;
+  return false;
+}
+
+// interleaved (re, im) copy of a tensor, as CTF stores complex<double>
+std::vector<double> interleaved(const HTensor &t) {
+  std::vector<double> z(2 * (size_t)t.size(), 0.0);
+  for (int64_t e = 0; e < t.size(); ++e) {
+    z[2 * e] = t.re[e];
+    if (t.complex) z[2 * e + 1] = t.im[e];
+  }
+  return z;
+}
+
+std::shared_ptr<HTensor> complex_tensor(const std::vector<int64_t> &lens,
+                                        const std::vector<double> &z) {
+  auto t = std::make_shared<HTensor>();
+  t->lens = lens;
+  t->complex = true;
+  t->re.resize(t->size());
+  t->im.resize(t->size());
+  for (int64_t e = 0; e < t->size(); ++e) {
+    t->re[e] = z[2 * e];
+    t->im[e] = z[2 * e + 1];
+  }
+  return t;
+}
+
 // CcsdEnergyFromCoulombIntegrals (ClusterSinglesDoublesAlgorithm.cxx:25-128)
 struct CcsdEnergyFromCoulombIntegrals : Algorithm {
+  // the complex branch, taken when the vertex is complex (:25-35); the
+  // integrals are built from the vertex on the device
+  void run_complex(const Sizes &s, const gbcc_ccsd_opts &o) {
+    const int64_t o1 = s.No, v1 = s.Nv;
+    const std::vector<double> g = interleaved(tensor("CoulombVertex"));
+    std::vector<double> t1i, t2i;
+    gbcc_ccsd_complex_in in{};
+    in.No = s.No; in.Nv = s.Nv; in.NG = s.NG;
+    in.eps_h = tensor("HoleEigenEnergies").re.data();
+    in.eps_p = tensor("ParticleEigenEnergies").re.data();
+    in.gamma = g.data();
+    if (given("initialSinglesAmplitudes")) {
+      t1i = interleaved(tensor("initialSinglesAmplitudes", {v1, o1}));
+      in.init_T1 = t1i.data();
+    }
+    if (given("initialDoublesAmplitudes")) {
+      t2i = interleaved(tensor("initialDoublesAmplitudes", {v1, v1, o1, o1}));
+      in.init_T2 = t2i.data();
+    }
+    std::vector<double> t1(2 * v1 * o1), t2(2 * v1 * v1 * o1 * o1);
+    std::vector<double> hist(2 * std::max(o.max_iterations, 1));
+    gbcc_ccsd_complex_out out{};
+    out.T1 = t1.data();
+    out.T2 = t2.data();
+    out.energy_history = hist.data();
+    emit["complex"] = 1;
+    const gbcc_status st = gbcc_ccsd_solve_complex(gpu(), &in, &o, &out);
+    check(st, "CcsdEnergyFromCoulombIntegrals (complex)", true);
+    Json its = Json::array();
+    for (int i = 0; i < out.iterations; ++i) {
+      Json it = Json::object();
+      it["iteration"] = i + 1;
+      it["energy"]["value"] = hist[2 * i];
+      its.push(it);
+    }
+    emit["iterations"] = its;
+    const double d = out.direct[0], x = out.exchange[0];       // real parts (:190-196)
+    emit["energy"]["direct"] = d;
+    emit["energy"]["exchange"] = x;
+    emit["energy"]["singlet"] = 0.25 * d - 0.5 * x;
+    emit["energy"]["triplet"] = 0.75 * d + 1.5 * x;
+    emit["energy"]["value"] = out.energy[0];
+    emit["energy"]["imaginary"] = out.energy[1];
+    emit["convergenceReached"] = out.converged;
+    if (st == GBCC_NOT_CONVERGED)
+      log(0, "CCSD", "WARNING: energy or amplitudes convergence not reached.");
+    std::ostringstream m;
+    m << std::setprecision(10) << "energy= " << out.energy[0];
+    log(0, "CCSD", m.str());
+    set_real("CcsdEnergy", out.energy[0]);                      // std::real (:32)
+    if (given("CcsdSinglesAmplitudes"))
+      set_tensor("CcsdSinglesAmplitudes", complex_tensor({v1, o1}, t1));
+    if (given("CcsdDoublesAmplitudes"))
+      set_tensor("CcsdDoublesAmplitudes", complex_tensor({v1, v1, o1, o1}, t2));
+  }
+
   void run() override {
     const Sizes s = sizes_of(*this);
     if (!given("CoulombVertex")) throw StepError("CoulombVertex is required");
@@ -551,6 +638,16 @@ struct CcsdEnergyFromCoulombIntegrals : Algorithm {
     o.emu_slices = (int)integer("emulationDigits", 0);
     if (integer("unrestricted", 0) || integer("antisymmetrize", 0))
       throw StepError("unrestricted / antisymmetrized amplitudes are not supported");
+    emit["maxIterations"] = o.max_iterations;
+    emit["amplitudesConvergence"] = std::abs(o.amplitudes_convergence);
+    emit["energyConvergence"] = std::abs(o.energy_convergence);
+    emit["precision"] = o.precision == GBCC_PREC_FP64 ? "fp64" : "emu";
+    if (has_imaginary_part(tensor("CoulombVertex"))) {
+      if (given("HPFockMatrix"))
+        throw StepError("HPFockMatrix is not supported for complex amplitudes");
+      run_complex(s, o);
+      return;
+    }
     gbcc_ccsd_in in{};
     in.No = s.No; in.Nv = s.Nv; in.NG = s.NG;
     in.eps_h = tensor("HoleEigenEnergies").re.data();
@@ -580,10 +677,6 @@ struct CcsdEnergyFromCoulombIntegrals : Algorithm {
     out.T2 = t2->re.data();
     out.pair_energy = given("PairEnergy") ? pe->re.data() : nullptr;
     out.energy_history = hist.data();
-    emit["maxIterations"] = o.max_iterations;
-    emit["amplitudesConvergence"] = std::abs(o.amplitudes_convergence);
-    emit["energyConvergence"] = std::abs(o.energy_convergence);
-    emit["precision"] = o.precision == GBCC_PREC_FP64 ? "fp64" : "emu";
     gbcc_status st = gbcc_ccsd_solve(gpu(), &in, &o, &out);
     check(st, "CcsdEnergyFromCoulombIntegrals", true);
     Json its = Json::array();
@@ -629,8 +722,13 @@ struct CcsdPerturbativeTriples : Algorithm {
     const int64_t o1 = s.No, v1 = s.Nv;
     in.Vabij = tensor_or_null("PPHHCoulombIntegrals", {v1, v1, o1, o1});
     in.Vijka = tensor_or_null("HHHPCoulombIntegrals", {o1, o1, o1, v1});
-    in.T1 = tensor("CcsdSinglesAmplitudes", {v1, o1}).re.data();
-    in.T2 = tensor("CcsdDoublesAmplitudes", {v1, v1, o1, o1}).re.data();
+    const HTensor &t1 = tensor("CcsdSinglesAmplitudes", {v1, o1});
+    const HTensor &t2 = tensor("CcsdDoublesAmplitudes", {v1, v1, o1, o1});
+    if (has_imaginary_part(t1) || has_imaginary_part(t2))
+      throw StepError("complex amplitudes: the complex (T) (CcsdPerturbativeTriplesComplex) "
+                      "is not built");
+    in.T1 = t1.re.data();
+    in.T2 = t2.re.data();
     in.e_ccsd = real("CcsdEnergy");
     double etot = 0, et = 0;
     check(gbcc_triples(gpu(), &in, precision_of(*this), &etot, &et),

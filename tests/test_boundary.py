@@ -295,3 +295,40 @@ def test_ctypes_structs_match_the_c_header(tmp_path):
         assert got[(cname, "size")] == ctypes.sizeof(py), cname
         for f, _ in py._fields_:
             assert got[(cname, f)] == getattr(py, f).offset, (cname, f)
+
+
+def _write_complex_tensor(path, arr):
+    z = np.ascontiguousarray(np.asarray(arr, dtype=np.complex128).transpose(
+        tuple(range(arr.ndim - 1, -1, -1)))).ravel()
+    dims = "".join("  - length: %d\n    type: State\n" % n for n in arr.shape)
+    path.write_text("version: 100\ntype: Tensor\ndimensions:\n%sscalarType: Complex64\n"
+                    "elements:\n  type: IeeeBinaryFile\nunit: 1.0\n" % dims)
+    z.view(np.float64).tofile(str(path)[:-5] + ".elements")
+
+
+def test_complex_vertex_takes_the_complex_branch(tmp_path):
+    # a vertex with a non-zero imaginary part selects the complex branch
+    # (ClusterSinglesDoublesAlgorithm.cxx:25-35); it has no noncanonical term
+    # and its amplitudes cannot enter the real (T)
+    rng = np.random.default_rng(2)
+    No, Nv, NG = 2, 3, 4
+    _write_tensor(tmp_path / "Eh.yaml", rng.normal(size=No))
+    _write_tensor(tmp_path / "Ep.yaml", rng.normal(size=Nv))
+    _write_tensor(tmp_path / "F.yaml", rng.normal(size=(No, Nv)))
+    g = rng.normal(size=(NG, No + Nv, No + Nv)) + 1j * rng.normal(size=(NG, No + Nv, No + Nv))
+    _write_complex_tensor(tmp_path / "G.yaml", g)
+    t1 = rng.normal(size=(Nv, No)) + 1j * rng.normal(size=(Nv, No))
+    _write_complex_tensor(tmp_path / "T1.yaml", t1)
+    _write_tensor(tmp_path / "T2.yaml", rng.normal(size=(Nv, Nv, No, No)))
+    reads = _read_steps(["Eh", "Ep", "F", "G", "T1", "T2"])
+    common = """    CoulombVertex: $G
+    HoleEigenEnergies: $Eh
+    ParticleEigenEnergies: $Ep
+"""
+    r, out = _run(tmp_path, reads + "- name: CcsdEnergyFromCoulombIntegrals\n  in:\n" + common
+                  + "    HPFockMatrix: $F\n  out: {}\n")
+    assert r.returncode == 1 and "not supported for complex" in out["error"], out
+    r, out = _run(tmp_path, reads + "- name: CcsdPerturbativeTriples\n  in:\n" + common
+                  + "    CcsdEnergy: 0.0\n    CcsdSinglesAmplitudes: $T1\n"
+                  "    CcsdDoublesAmplitudes: $T2\n  out: {}\n")
+    assert r.returncode == 1 and "complex (T)" in out["error"], out
