@@ -231,6 +231,22 @@ gbcc_status gbcc_ccsd_residual_complex(gbcc_ctx *ctx, const gbcc_ccsd_complex_in
                                        const double *T1, const double *T2,
                                        double *R1, double *R2);
 
+/* Replaces CcsdPerturbativeTriplesComplex::run with complex amplitudes
+ * (src/algorithms/CcsdPerturbativeTriplesComplex.cxx:32-268).  e_total =
+ * e_ccsd + Re E_(T) (CcsdPerturbativeTriplesComplexEnergy, :77-84); e_t =
+ * E_(T) as (re, im).  The PPHH and PHHH integrals are built from gamma. */
+typedef struct {
+  int No, Nv, NG;
+  const double *eps_h, *eps_p;  /* real [No], [Nv] */
+  const double *gamma;          /* CoulombVertex, complex [NG,Np,Np] */
+  const double *T1;             /* CcsdSinglesAmplitudes, complex [Nv,No] */
+  const double *T2;             /* CcsdDoublesAmplitudes, complex [Nv,Nv,No,No] */
+  double e_ccsd;                /* CcsdEnergy */
+} gbcc_triples_complex_in;
+
+gbcc_status gbcc_triples_complex(gbcc_ctx *ctx, const gbcc_triples_complex_in *in,
+                                 int precision, double *e_total, double *e_t);
+
 /* ---------------------------------------------------------------- (T) */
 /* Replaces CcsdPerturbativeTriples::run (src/algorithms/CcsdPerturbativeTriples.cxx:119-248).
  * e_total = e_ccsd + E_(T) (the reference's CcsdPerturbativeTriplesEnergy),

@@ -58,6 +58,12 @@ class ComplexOut(C.Structure):
                 ("energy_history", _dp)]
 
 
+class TriplesComplexIn(C.Structure):
+    _fields_ = [("No", C.c_int), ("Nv", C.c_int), ("NG", C.c_int),
+                ("eps_h", _dp), ("eps_p", _dp), ("gamma", _dp),
+                ("T1", _dp), ("T2", _dp), ("e_ccsd", C.c_double)]
+
+
 class TriplesIn(C.Structure):
     _fields_ = [("No", C.c_int), ("Nv", C.c_int), ("NG", C.c_int),
                 ("eps_h", _dp), ("eps_p", _dp), ("gamma", _dp),
@@ -103,6 +109,8 @@ _SIGS = {
                                              _dp, _dp]),
     "gbcc_triples": (C.c_int, [C.c_void_p, C.POINTER(TriplesIn), C.c_int,
                                _dp, _dp]),
+    "gbcc_triples_complex": (C.c_int, [C.c_void_p, C.POINTER(TriplesComplexIn), C.c_int,
+                                       _dp, _dp]),
     "gbcc_triples_from_solver": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp]),
     "gbcc_coulomb_integrals": (C.c_int, [C.c_void_p, C.c_int, C.c_int,
                                          C.c_int, _dp, _dp, _dp, _dp, _dp,

@@ -13,7 +13,7 @@ from .capi import fortran_flat, from_fortran_flat, ptr
 
 __all__ = ["make_opts", "CcsdInput", "ccsd_solve", "ccsd_residual", "Solver",
            "triples", "coulomb_integrals", "energy", "ComplexInput",
-           "ccsd_solve_complex", "ccsd_residual_complex"]
+           "ccsd_solve_complex", "ccsd_residual_complex", "triples_complex"]
 
 
 def make_opts(mixer="LinearMixer", max_residua=4, mixing_ratio=1.0,
@@ -339,3 +339,25 @@ def ccsd_residual_complex(ctx, it, T1, T2, eps_h, eps_p, gamma,
                                                  int(it), ptr(t1), ptr(t2), ptr(r1),
                                                  ptr(r2)))
     return from_complex_flat(r1, (Nv, No)), from_complex_flat(r2, (Nv, Nv, No, No))
+
+
+def triples_complex(ctx, eps_h, eps_p, gamma, T1, T2, e_ccsd=0.0, precision="fp64"):
+    """CcsdPerturbativeTriplesComplex: returns (complex E_(T), e_ccsd + Re E_(T))."""
+    eps_h, eps_p = _eigenenergies(eps_h, eps_p)
+    No, Nv = eps_h.size, eps_p.size
+    g = np.asarray(gamma)
+    if g.ndim != 3 or not g.shape[0]:
+        raise ValueError("gamma must be [NG, Np, Np]")
+    NG = g.shape[0]
+    keep = [eps_h, eps_p, complex_flat(g, (NG, No + Nv, No + Nv), "gamma"),
+            complex_flat(T1, (Nv, No), "T1"), complex_flat(T2, (Nv, Nv, No, No), "T2")]
+    s = capi.TriplesComplexIn()
+    s.No, s.Nv, s.NG = No, Nv, NG
+    s.eps_h, s.eps_p, s.gamma, s.T1, s.T2 = [ptr(a) for a in keep]
+    s.e_ccsd = float(e_ccsd)
+    et = np.zeros(2)
+    etot = C.c_double()
+    p = {"fp64": capi.PREC_FP64, "emu": capi.PREC_EMU}[precision]
+    ctx.check(ctx.lib.gbcc_triples_complex(ctx.h, C.byref(s), p, C.byref(etot), ptr(et)))
+    del keep
+    return complex(et[0], et[1]), etot.value

@@ -13,6 +13,8 @@ gbcc_status complex_solve(Context &ctx, const gbcc_ccsd_complex_in &in,
                           const gbcc_ccsd_opts &o, gbcc_ccsd_complex_out *out);
 void complex_residual(Context &ctx, const gbcc_ccsd_complex_in &in, const gbcc_ccsd_opts &o,
                       int it, const double *T1, const double *T2, double *R1, double *R2);
+void complex_triples(Context &ctx, const gbcc_triples_complex_in &in, int precision,
+                     double *e_total, double *e_t);
 }
 
 struct gbcc_ctx {
@@ -393,6 +395,17 @@ gbcc_status gbcc_ccsd_residual_complex(gbcc_ctx *ctx, const gbcc_ccsd_complex_in
     apply_precision_opts(ctx->c, o);
     gbcc::complex_residual(ctx->c, *in, o, it, T1, T2, R1, R2);
     ctx->c.check_device_errors();
+    return GBCC_OK;
+  });
+}
+
+gbcc_status gbcc_triples_complex(gbcc_ctx *ctx, const gbcc_triples_complex_in *in,
+                                 int precision, double *e_total, double *e_t) {
+  if (!ctx || !in) return GBCC_BAD_ARG;
+  return guard(ctx, [&]() {
+    gbcc::require(precision == GBCC_PREC_FP64 || precision == GBCC_PREC_EMU,
+                  "unknown precision");
+    gbcc::complex_triples(ctx->c, *in, precision, e_total, e_t);
     return GBCC_OK;
   });
 }

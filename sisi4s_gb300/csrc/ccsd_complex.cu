@@ -15,6 +15,22 @@
 namespace gbcc {
 namespace {
 
+// z[a,b,c] = conj(z / D) with D = (((e_i + e_j) + e_k) - e_a) - e_b) - e_c
+// (CcsdPerturbativeTriplesComplex.cxx:156-161, 224-229), on the two planes
+__global__ void conj_over_denominator_kernel(double *__restrict__ re, double *__restrict__ im,
+                                             const double *__restrict__ eh,
+                                             const double *__restrict__ ep, int i0, int i1,
+                                             int i2, int Nv) {
+  const int n = Nv * Nv * Nv;
+  const double hs = (eh[i0] + eh[i1]) + eh[i2];
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+    const int a = e % Nv, b = (e / Nv) % Nv, c = e / (Nv * Nv);
+    const double d = ((hs - ep[a]) - ep[b]) - ep[c];
+    re[e] = re[e] / d;
+    im[e] = -(im[e] / d);
+  }
+}
+
 Ten as_ten(const cx::View &v) {
   Ten t;
   t.p = v.p;
@@ -91,6 +107,20 @@ struct DeviceBackend {
     gbcc::linear_mix(ctx, next.p, nres.p, last.p, lres.p, r, n, part.as<double>(),
                      out.as<double>());
     read_sums(out.as<double>(), sums, 2);
+  }
+  void conj_over_denominator(const cx::View &re, const cx::View &im, const cx::View &eh,
+                             const cx::View &ep, int64_t i0, int64_t i1, int64_t i2) {
+    const int64_t Nv = ep.lens[0];
+    require(Nv * Nv * Nv < (int64_t(1) << 30) && re.size() == Nv * Nv * Nv &&
+                im.size() == re.size() && i0 < eh.lens[0] && i1 < eh.lens[0] &&
+                i2 < eh.lens[0],
+            "conj_over_denominator: bad shape");
+    const int64_t n = Nv * Nv * Nv;
+    const int64_t cap = (int64_t)std::max(ctx.sm_count, 1) * 8;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, cap));
+    conj_over_denominator_kernel<<<grid, 256, 0, ctx.stream>>>(
+        re.p, im.p, eh.p, ep.p, (int)i0, (int)i1, (int)i2, (int)Nv);
+    GBCC_CHECK_LAUNCH(ctx);
   }
   double scalar(const cx::View &x) {
     double h = 0.0;
@@ -223,6 +253,27 @@ gbcc_status complex_solve(Context &ctx, const gbcc_ccsd_complex_in &in,
   }
   ctx.check_device_errors();
   return (r.converged || o.max_iterations == 0) ? GBCC_OK : GBCC_NOT_CONVERGED;
+}
+
+void complex_triples(Context &ctx, const gbcc_triples_complex_in &in, int precision,
+                     double *e_total, double *e_t) {
+  require(in.T1 && in.T2, "CcsdSinglesAmplitudes and CcsdDoublesAmplitudes are required");
+  DeviceBackend rb{ctx, precision};
+  cx::Inputs<DeviceBackend> I;
+  cx::CBuf<DeviceBackend> T;
+  gbcc_ccsd_complex_in ci{};
+  ci.No = in.No; ci.Nv = in.Nv; ci.NG = in.NG;
+  ci.eps_h = in.eps_h; ci.eps_p = in.eps_p; ci.gamma = in.gamma;
+  ci.init_T1 = in.T1; ci.init_T2 = in.T2;
+  cx::setup(rb, I, host_in(ci), T);
+  const cx::Layout L(in.Nv, in.No);
+  const std::complex<double> e = cx::triples(rb, I, cx::t1_of(T, L), cx::t2_of(T, L));
+  ctx.check_device_errors();
+  if (e_t) {
+    e_t[0] = e.real();
+    e_t[1] = e.imag();
+  }
+  if (e_total) *e_total = in.e_ccsd + e.real();  // CcsdPerturbativeTriplesComplex.cxx:77-84
 }
 
 }  // namespace gbcc

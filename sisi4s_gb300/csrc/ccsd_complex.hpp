@@ -83,6 +83,9 @@ struct Layout {
 //   linear_mix(next, nres, last, lres, r, sums)      LinearMixer::append
 //   vertex_block(dst, src, p0, np, q0, nq)            Gamma sub-block
 //   double scalar(x)                      read an order-0 tensor (synchronises)
+//   conj_over_denominator(re, im, eps_h, eps_p, i, j, k)
+//                                         z[a,b,c] = conj(z / D^{ijk}_{abc}) for
+//                                         the (T) denominator of the reference
 
 template <class RB>
 struct CBuf {
@@ -473,6 +476,116 @@ SolveResult solve(RB &rb, const Inputs<RB> &I, const SolveOpts &o, CBuf<RB> &T) 
   }
   if (o.max_iterations == 0) out.energy = energy(rb, I, t1(T), t2(T));  // :116-119
   return out;
+}
+
+// ---------------------------------------------------------------------- (T)
+// view of the dense sub-block starting at element `offset`
+inline View sub(const View &v, int64_t offset, std::initializer_list<int64_t> l) {
+  return view(v.p + offset, l);
+}
+inline CView csub(const CView &v, int64_t offset, std::initializer_list<int64_t> l) {
+  return CView{sub(v.re, offset, l), sub(v.im, offset, l)};
+}
+
+// Permutation<3>(p) images (src/math/Permutation.hpp:52-62)
+inline std::array<int, 3> perm3(int p) {
+  std::array<int, 3> img{};
+  std::array<int, 2> s2{};
+  {  // Permutation<2>(p / 3)
+    const int r = (p / 3) % 2;
+    s2[r] = 0;
+    s2[1 - r] = 1;
+  }
+  const int r = p % 3;
+  for (int i = 0; i < r; ++i) img[i] = s2[i] + 1;
+  img[r] = 0;
+  for (int i = r + 1; i < 3; ++i) img[i] = s2[i - 1] + 1;
+  return img;
+}
+
+// s * pi: sPi[i] = s[pi(i)] (CcsdPerturbativeTriplesComplex.cxx:23-29)
+inline std::string pstr(const std::string &s, const std::array<int, 3> &pi) {
+  std::string r(s);
+  for (int i = 0; i < 3; ++i) r[i] = s[pi[i]];
+  return r;
+}
+
+// (T) of CcsdPerturbativeTriplesComplex::Calculator<complex>::calculate
+// (src/algorithms/CcsdPerturbativeTriplesComplex.cxx:166-268) on the complex
+// amplitudes T1 [Nv,No], T2 [Nv,Nv,No,No]; returns the complex E_(T)
+template <class RB>
+std::complex<double> triples(RB &rb, const Inputs<RB> &I, const CView &T1, const CView &T2) {
+  const int64_t No = I.No, Nv = I.Nv;
+  // Wvv[d,b,c,k] = sum_F conj(Gamma_Fdb) Gamma_Fck, built once (the reference
+  // forms it per image, :342-348)
+  CBuf<RB> Wvv = cbuf(rb, {Nv, Nv, Nv, No});
+  ccontract(rb, 1.0, I.Gab.v(), "Fdb", true, I.Gai.v(), "Fck", false, 0.0, Wvv.v(), "dbck");
+  // T2 as [a,b,l,i], so that T2[a,b,i,l] for fixed i is one dense block
+  CBuf<RB> T2p = cbuf(rb, {Nv, Nv, No, No});
+  cassign(rb, 1.0, T2, "abil", false, 0.0, T2p.v(), "abli");
+  const CView Vabij = I.Vabij.v(), Vaijk = I.Vaijk.v();
+  const int64_t n3 = Nv * Nv * Nv;
+  std::vector<CBuf<RB>> piDV(6);
+  for (auto &b : piDV) b = cbuf(rb, {Nv, Nv, Nv});
+  CBuf<RB> DV = cbuf(rb, {Nv, Nv, Nv}), S = cbuf(rb, {Nv, Nv, Nv}), Tabc = cbuf(rb, {Nv, Nv, Nv});
+  CBuf<RB> E = cbuf(rb, {});
+  czero(rb, E.v());
+  static const double spin_fermi[4] = {+2.0, -4.0, 0.0, +8.0};  // :181
+  const std::string abc = "abc";
+  std::array<std::array<int, 3>, 6> pi;
+  for (int p = 0; p < 6; ++p) pi[p] = perm3(p);
+  for (int64_t i0 = 0; i0 < No; ++i0)
+    for (int64_t i1 = i0; i1 < No; ++i1)
+      for (int64_t i2 = i1; i2 < No; ++i2) {
+        const int64_t iv[3] = {i0, i1, i2};
+        std::array<std::array<int64_t, 3>, 6> m;
+        std::array<int, 6> src;
+        for (int p = 0; p < 6; ++p) {
+          for (int k = 0; k < 3; ++k) m[p][k] = iv[pi[p][k]];  // Map * Permutation
+          src[p] = p;
+          for (int q = 0; q < p; ++q)
+            if (m[q] == m[p]) { src[p] = q; break; }       // :206-215
+        }
+        czero(rb, DV.v());
+        for (int p = 0; p < 6; ++p) {
+          if (src[p] == p) {
+            const CView W = piDV[p].v();
+            // getDoublesParticleContribution (:346-347)
+            ccontract(rb, 1.0, csub(T2, (m[p][0] + No * m[p][1]) * Nv * Nv, {Nv, Nv}), "ad",
+                      false, csub(Wvv.v(), m[p][2] * n3, {Nv, Nv, Nv}), "dbc", false, 0.0, W,
+                      "abc");
+            // addDoublesHoleContribution (:141): T_ab^{m0 l} V_{c l m2 m1}
+            ccontract(rb, -1.0, csub(T2p.v(), m[p][0] * Nv * Nv * No, {Nv, Nv, No}), "abl",
+                      false, csub(Vaijk, (m[p][2] + No * m[p][1]) * Nv * No, {Nv, No}), "cl",
+                      false, 1.0, W, "abc");
+          }
+          // :221 DV["abc"] += piDV[p]["abc" * pi]
+          cassign(rb, 1.0, piDV[src[p]].v(), pstr(abc, pi[p]).c_str(), false, 1.0, DV.v(),
+                  "abc");
+        }
+        // :224-229 DV = conj(DV / D)
+        rb.conj_over_denominator(DV.re.v, DV.im.v, I.eps_h.v, I.eps_p.v, i0, i1, i2);
+        for (int p = 0; p < 6; ++p) {
+          if (src[p] != p) continue;
+          // getSinglesContribution (:148): 0.5 T_a^{m0} V_bc^{m1 m2}
+          ccontract(rb, 0.5, csub(T1, m[p][0] * Nv, {Nv}), "a", false,
+                    csub(Vabij, (m[p][1] + No * m[p][2]) * Nv * Nv, {Nv, Nv}), "bc", false,
+                    0.0, S.v(), "abc");
+          czero(rb, Tabc.v());
+          for (int sg = 0; sg < 6; ++sg) {                          // :237-249
+            const std::array<int, 3> &sigma = pi[sg];
+            int fixed = 0;
+            for (int k = 0; k < 3; ++k) fixed += sigma[k] == k;
+            const double sf = spin_fermi[fixed];
+            const std::string u = pstr(pstr(abc, sigma), pi[p]);
+            cassign(rb, sf, piDV[p].v(), u.c_str(), false, 1.0, Tabc.v(), "abc");
+            cassign(rb, sf, S.v(), u.c_str(), false, 1.0, Tabc.v(), "abc");
+          }
+          // :253 energy += DV["abc"] Tabc["abc"]
+          ccontract(rb, 1.0, DV.v(), "abc", false, Tabc.v(), "abc", false, 1.0, E.v(), "");
+        }
+      }
+  return cscalar(rb, E.v());
 }
 
 // ------------------------------------------------------- host-side flow

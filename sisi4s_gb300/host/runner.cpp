@@ -725,8 +725,8 @@ struct CcsdPerturbativeTriples : Algorithm {
     const HTensor &t1 = tensor("CcsdSinglesAmplitudes", {v1, o1});
     const HTensor &t2 = tensor("CcsdDoublesAmplitudes", {v1, v1, o1, o1});
     if (has_imaginary_part(t1) || has_imaginary_part(t2))
-      throw StepError("complex amplitudes: the complex (T) (CcsdPerturbativeTriplesComplex) "
-                      "is not built");
+      throw StepError("complex amplitudes: use CcsdPerturbativeTriplesComplex, the reference's "
+                      "(T) for complex amplitudes");
     in.T1 = t1.re.data();
     in.T2 = t2.re.data();
     in.e_ccsd = real("CcsdEnergy");
@@ -742,6 +742,57 @@ struct CcsdPerturbativeTriples : Algorithm {
   }
 };
 REGISTER_ALGORITHM(CcsdPerturbativeTriples);
+
+// CcsdPerturbativeTriplesComplex (CcsdPerturbativeTriplesComplex.cxx:32-84):
+// complex amplitudes go through the complex Calculator; real amplitudes with a
+// real vertex are the real (T).  The PPHH / PHHH integrals are built from the
+// vertex on the device.
+struct CcsdPerturbativeTriplesComplex : Algorithm {
+  void run() override {
+    const Sizes s = sizes_of(*this);
+    if (!given("CoulombVertex")) throw StepError("CoulombVertex is required");
+    const int64_t o1 = s.No, v1 = s.Nv;
+    const HTensor &g = tensor("CoulombVertex");
+    const HTensor &t1 = tensor("CcsdSinglesAmplitudes", {v1, o1});
+    const HTensor &t2 = tensor("CcsdDoublesAmplitudes", {v1, v1, o1, o1});
+    const double e_ccsd = real("CcsdEnergy");
+    double etot = 0, et[2] = {0, 0};
+    if (t1.complex || t2.complex) {
+      const std::vector<double> gz = interleaved(g), t1z = interleaved(t1),
+                                t2z = interleaved(t2);
+      gbcc_triples_complex_in in{};
+      in.No = s.No; in.Nv = s.Nv; in.NG = s.NG;
+      in.eps_h = tensor("HoleEigenEnergies").re.data();
+      in.eps_p = tensor("ParticleEigenEnergies").re.data();
+      in.gamma = gz.data();
+      in.T1 = t1z.data();
+      in.T2 = t2z.data();
+      in.e_ccsd = e_ccsd;
+      check(gbcc_triples_complex(gpu(), &in, precision_of(*this), &etot, et),
+            "CcsdPerturbativeTriplesComplex");
+    } else {
+      gbcc_triples_in in{};
+      in.No = s.No; in.Nv = s.Nv; in.NG = s.NG;
+      in.eps_h = tensor("HoleEigenEnergies").re.data();
+      in.eps_p = tensor("ParticleEigenEnergies").re.data();
+      in.gamma = g.re.data();
+      in.gamma_imag = g.complex ? g.im.data() : nullptr;
+      in.T1 = t1.re.data();
+      in.T2 = t2.re.data();
+      in.e_ccsd = e_ccsd;
+      check(gbcc_triples(gpu(), &in, precision_of(*this), &etot, et),
+            "CcsdPerturbativeTriplesComplex");
+    }
+    std::ostringstream m;
+    m << std::setprecision(12) << "e=" << etot << " triples=" << et[0];
+    log(0, "CcsdPerturbativeTriplesComplex", m.str());
+    emit["energy"]["triples"] = et[0];
+    emit["energy"]["triplesImaginary"] = et[1];
+    emit["energy"]["value"] = etot;
+    set_real("CcsdPerturbativeTriplesComplexEnergy", etot);       // :84
+  }
+};
+REGISTER_ALGORITHM(CcsdPerturbativeTriplesComplex);
 
 // ------------------------------------------------------------------ parser
 std::vector<std::unique_ptr<Algorithm>> parse_steps(const std::string &file) {

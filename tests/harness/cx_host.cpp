@@ -235,6 +235,22 @@ struct HostBackend {
 
   double scalar(const View &x) { return x.p[0]; }
 
+  // z = conj(z / D), D = (((e_i + e_j) + e_k) - e_a) - e_b) - e_c in the
+  // reference's order (CcsdPerturbativeTriplesComplex.cxx:156-161, 224-229)
+  void conj_over_denominator(const View &re, const View &im, const View &eh, const View &ep,
+                             int64_t i0, int64_t i1, int64_t i2) {
+    const int64_t Nv = ep.lens[0];
+    const double hs = (eh.p[i0] + eh.p[i1]) + eh.p[i2];
+    for (int64_t c = 0; c < Nv; ++c)
+      for (int64_t b = 0; b < Nv; ++b)
+        for (int64_t a = 0; a < Nv; ++a) {
+          const int64_t e = a + Nv * (b + Nv * c);
+          const double d = ((hs - ep.p[a]) - ep.p[b]) - ep.p[c];
+          re.p[e] = re.p[e] / d;
+          im.p[e] = -(im.p[e] / d);
+        }
+  }
+
   Buf load_real(const double *h, std::initializer_list<int64_t> l) {
     Buf b = alloc(l);
     std::memcpy(b.v.p, h, sizeof(double) * b.v.size());
@@ -331,6 +347,26 @@ int cx_solve(int No, int Nv, int NG, const double *eh, const double *ep,
     const gbcc::cx::Layout L(Nv, No);
     rb.store_complex(gbcc::cx::t1_of(T, L), T1);
     rb.store_complex(gbcc::cx::t2_of(T, L), T2);
+    return 0;
+  } catch (const std::exception &e) {
+    g_err = e.what();
+    return 1;
+  }
+}
+
+// complex (T) energy (re, im) of the given complex amplitudes
+int cx_triples(int No, int Nv, int NG, const double *eh, const double *ep,
+               const double *gamma, const double *T1, const double *T2, double *et) {
+  try {
+    HostBackend rb;
+    gbcc::cx::Inputs<HostBackend> I;
+    gbcc::cx::CBuf<HostBackend> T;
+    gbcc::cx::setup(rb, I, host_in(No, Nv, NG, eh, ep, gamma, T1, T2), T);
+    const gbcc::cx::Layout L(Nv, No);
+    const std::complex<double> e =
+        gbcc::cx::triples(rb, I, gbcc::cx::t1_of(T, L), gbcc::cx::t2_of(T, L));
+    et[0] = e.real();
+    et[1] = e.imag();
     return 0;
   } catch (const std::exception &e) {
     g_err = e.what();

@@ -195,6 +195,7 @@ def test_list_algorithms():
     r = subprocess.run([RUNNER, "--list"], capture_output=True, text=True, check=True)
     names = r.stdout.split()
     for n in ("CcsdEnergyFromCoulombIntegrals", "CcsdPerturbativeTriples",
+              "CcsdPerturbativeTriplesComplex",
               "CoulombIntegralsFromVertex", "Read", "Write", "TensorWriter",
               "DefineHolesAndParticles", "Nop"):
         assert n in names
@@ -270,6 +271,7 @@ def test_ctypes_structs_match_the_c_header(tmp_path):
                "gbcc_ccsd_out": capi.CcsdOut, "gbcc_triples_in": capi.TriplesIn,
                "gbcc_ccsd_complex_in": capi.ComplexIn,
                "gbcc_ccsd_complex_out": capi.ComplexOut,
+               "gbcc_triples_complex_in": capi.TriplesComplexIn,
                "gbcc_server_opts": ServerOpts, "gbcc_result": Result}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "gbcc.h"',
              'int main(void) {']
@@ -331,4 +333,8 @@ def test_complex_vertex_takes_the_complex_branch(tmp_path):
     r, out = _run(tmp_path, reads + "- name: CcsdPerturbativeTriples\n  in:\n" + common
                   + "    CcsdEnergy: 0.0\n    CcsdSinglesAmplitudes: $T1\n"
                   "    CcsdDoublesAmplitudes: $T2\n  out: {}\n")
-    assert r.returncode == 1 and "complex (T)" in out["error"], out
+    assert r.returncode == 1 and "CcsdPerturbativeTriplesComplex" in out["error"], out
+    r, out = _run(tmp_path, reads + "- name: CcsdPerturbativeTriplesComplex\n  in:\n" + common
+                  + "    CcsdEnergy: 0.0\n    CcsdSinglesAmplitudes: $T1\n"
+                  "    CcsdDoublesAmplitudes: $T2\n  out: {}\n")
+    assert r.returncode == 0 or "GPU context: NO_DEVICE" in out["error"], out

@@ -14,7 +14,8 @@ import subprocess
 import numpy as np
 import pytest
 
-from oracle.ccsd_complex import ccsd_complex, coulomb_integrals_complex, residual_complex
+from oracle.ccsd_complex import (ccsd_complex, coulomb_integrals_complex, residual_complex,
+                                 triples_complex_loop)
 from sisi4s_gb300.inputs import make_system
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -123,3 +124,15 @@ def test_solve_program_matches_oracle(lib, ratio, shift):
 def test_program_reports_missing_inputs(lib):
     st = lib.cx_residual(0, 4, 5, None, None, None, 1, 1, 0, 1, -1, None, None, None, None)
     assert st == 1 and b"required" in lib.cx_last_error()
+
+
+@pytest.mark.parametrize("No,Nv,NG", [(3, 6, 9), (2, 5, 7), (4, 5, 8)])
+def test_triples_program_matches_oracle(lib, No, Nv, NG):
+    s, g, T1, T2 = _system(No, Nv, NG, seed=No + Nv)
+    ci = coulomb_integrals_complex(g, No)
+    ref = triples_complex_loop(s.eps_h, s.eps_p, T1, T2, ci["PPHH"], ci["PHHH"], g)
+    et = np.zeros(2)
+    st = lib.cx_triples(No, Nv, NG, _p(s.eps_h), _p(s.eps_p), _p(_flat(g)), _p(_flat(T1)),
+                        _p(_flat(T2)), _p(et))
+    assert st == 0, lib.cx_last_error()
+    assert abs(complex(et[0], et[1]) - ref) < 1e-13 * abs(ref)

@@ -10,7 +10,8 @@ import ctypes as C
 import numpy as np
 import pytest
 
-from oracle.ccsd_complex import ccsd_complex, coulomb_integrals_complex, residual_complex
+from oracle.ccsd_complex import (ccsd_complex, coulomb_integrals_complex, residual_complex,
+                                 triples_complex_loop)
 from oracle.ueg import UEG_GOLDEN, ueg_planewave
 from sisi4s_gb300 import capi
 from sisi4s_gb300 import ccsd as gpu
@@ -100,6 +101,10 @@ def test_ueg_golden_through_the_complex_branch(ctx):
     assert abs(r["history"][0].real - gd["mp2"]) < 1e-12
     assert abs(r["energy"].real - gd["ccsd"]) < 1e-8 * abs(gd["ccsd"])
     assert abs(r["energy"].imag) < 1e-14
+    et, etot = gpu.triples_complex(ctx, eps[:n], eps[n:], gam, r["T1"], r["T2"],
+                                   e_ccsd=r["energy"].real)
+    assert abs(et.real - gd["triples"]) < 1e-10 and abs(et.imag) < 1e-14
+    assert etot == r["energy"].real + et.real
 
 
 def test_complex_diis_is_refused(ctx):
@@ -109,3 +114,19 @@ def test_complex_diis_is_refused(ctx):
     out = capi.ComplexOut()
     st = ctx.lib.gbcc_ccsd_solve_complex(ctx.h, C.byref(inp.s), C.byref(o), C.byref(out))
     assert st == capi.BAD_ARG
+
+
+@pytest.mark.parametrize("No,Nv,NG,precision", [(3, 6, 9, "fp64"), (2, 7, 10, "fp64"),
+                                                (3, 12, 20, "emu")])
+def test_complex_triples_matches_oracle(ctx, No, Nv, NG, precision):
+    s, g, T1, T2 = _system(No, Nv, NG, seed=No + Nv)
+    ci = coulomb_integrals_complex(g, No)
+    ref = triples_complex_loop(s.eps_h, s.eps_p, T1, T2, ci["PPHH"], ci["PHHH"], g)
+    if precision == "emu":
+        ctx.set_emulation(6, 0.0)  # every GEMM emulated
+    try:
+        et, _ = gpu.triples_complex(ctx, s.eps_h, s.eps_p, g, T1, T2, precision=precision)
+    finally:
+        ctx.set_emulation(6, 1e7)
+    tol = 1e-12 if precision == "fp64" else 1e-10
+    assert abs(et - ref) < tol * abs(ref)
