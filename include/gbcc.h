@@ -130,6 +130,12 @@ typedef struct {
   int emu_slices;                /* bf16 slices per operand for GBCC_PREC_EMU
                                     (0 = library default); (T) uses one more,
                                     at most 8 */
+  int formulation;               /* 0: CcsdEnergyFromCoulombIntegrals (particle
+                                    ladder from the vertex, default);
+                                    1: CcsdEnergyFromCoulombIntegralsReference
+                                    (stored Vabcd / Vabci,
+                                    CcsdEnergyFromCoulombIntegralsReference.cxx:29-292) */
+  int only_ppl;                  /* onlyPPL of formulation 1, default 0 */
 } gbcc_ccsd_opts;
 
 void gbcc_ccsd_opts_default(gbcc_ccsd_opts *opts);
@@ -153,6 +159,10 @@ typedef struct {
                                  iteration's energy (getEnergy,
                                  ClusterSinglesDoublesAlgorithm.cxx:199-209).
                                  Callers zero-initialise the struct. */
+  /* formulation 1 only; built from gamma when NULL (gamma may then be NULL
+   * if every integral is given) */
+  const double *Vabcd;        /* PPPPCoulombIntegrals [Nv,Nv,Nv,Nv] */
+  const double *Vabci;        /* PPPHCoulombIntegrals [Nv,Nv,Nv,No] */
 } gbcc_ccsd_in;
 
 typedef struct {
@@ -314,6 +324,11 @@ gbcc_status gbcc_coulomb_integrals(gbcc_ctx *ctx, int No, int Nv, int NG,
                                    const double *gamma, double *Vabij,
                                    double *Vaibj, double *Vijkl, double *Vijka,
                                    double *Vijab);
+/* The particle blocks the stored formulation reads
+ * (CoulombIntegralsFromVertex.cxx:423-431): PPPP Vabcd [Nv,Nv,Nv,Nv] and
+ * PPPH Vabci [Nv,Nv,Nv,No].  Any NULL output is skipped. */
+gbcc_status gbcc_coulomb_integrals_pp(gbcc_ctx *ctx, int No, int Nv, int NG,
+                                      const double *gamma, double *Vabcd, double *Vabci);
 
 /* ------------------------------------------------------- building blocks */
 /* C[M,N] = alpha * op(A) op(B) + beta * C, column-major, device pointers,

@@ -243,16 +243,20 @@ def residual(it, T1, T2, ints, gamma, distinguishable=0, ppl=1,
     return R1, R2
 
 
-def residual_reference(it, T1, T2, ints, initial_doubles=False):
+def residual_reference(it, T1, T2, ints, initial_doubles=False, only_ppl=False):
     """``CcsdEnergyFromCoulombIntegralsReference::getResiduum`` (stored
-    Vabcd/Vabci; src/algorithms/CcsdEnergyFromCoulombIntegralsReference.cxx:131-292).
+    Vabcd/Vabci; src/algorithms/CcsdEnergyFromCoulombIntegralsReference.cxx:29-292).
     An independent second formulation of the same residual; ``ints`` must
-    also hold "PPPP" (Vabcd) and "PPPH" (Vabci)."""
+    also hold "PPPP" (Vabcd) and "PPPH" (Vabci).  ``only_ppl`` is the
+    onlyPPL option: R2 = Vabcd (T2 + T1 T1) alone (:56-70)."""
     Vabij = ints["PPHH"]
     R1 = np.zeros_like(T1)
     R2 = np.zeros_like(T2)
-    if it == 0 and not initial_doubles:
+    if it == 0 and not initial_doubles and not only_ppl:
         return R1, Vabij.copy()                                  # :50-54
+    if only_ppl:
+        X = T2 + _e("ai,bj->abij", T1, T1)                       # :66-67
+        return R1, _e("abcd,cdij->abij", ints["PPPP"], X)        # :70
     Vabcd, Vaibj, Vijkl = ints["PPPP"], ints["PHPH"], ints["HHHH"]
     Vijka, Vabci = ints["HHHP"], ints["PPPH"]
     Kac = (-2.0) * _e("cdkl,adkl->ac", Vabij, T2)                # :171

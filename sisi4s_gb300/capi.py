@@ -27,7 +27,8 @@ class CcsdOpts(C.Structure):
                 ("level_shift", C.c_double), ("distinguishable", C.c_int),
                 ("ppl", C.c_int), ("integrals_slice_size", C.c_int),
                 ("integrals_slice_factor", C.c_double),
-                ("precision", C.c_int), ("emu_slices", C.c_int)]
+                ("precision", C.c_int), ("emu_slices", C.c_int),
+                ("formulation", C.c_int), ("only_ppl", C.c_int)]
 
 
 class CcsdIn(C.Structure):
@@ -35,7 +36,8 @@ class CcsdIn(C.Structure):
                 ("eps_h", _dp), ("eps_p", _dp), ("gamma", _dp),
                 ("gamma_imag", _dp), ("Vabij", _dp), ("Vaibj", _dp),
                 ("Vijkl", _dp), ("Vijka", _dp), ("init_T1", _dp),
-                ("init_T2", _dp), ("fock_hp", _dp)]
+                ("init_T2", _dp), ("fock_hp", _dp), ("Vabcd", _dp),
+                ("Vabci", _dp)]
 
 
 class CcsdOut(C.Structure):
@@ -115,6 +117,8 @@ _SIGS = {
     "gbcc_coulomb_integrals": (C.c_int, [C.c_void_p, C.c_int, C.c_int,
                                          C.c_int, _dp, _dp, _dp, _dp, _dp,
                                          _dp]),
+    "gbcc_coulomb_integrals_pp": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int,
+                                            _dp, _dp, _dp]),
     "gbcc_dgemm": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int64,
                              C.c_int64, C.c_int64, C.c_double, C.c_void_p,
                              C.c_int64, C.c_void_p, C.c_int64, C.c_double,

@@ -13,14 +13,15 @@ from .capi import fortran_flat, from_fortran_flat, ptr
 
 __all__ = ["make_opts", "CcsdInput", "ccsd_solve", "ccsd_residual", "Solver",
            "triples", "coulomb_integrals", "energy", "ComplexInput",
-           "ccsd_solve_complex", "ccsd_residual_complex", "triples_complex"]
+           "ccsd_solve_complex", "ccsd_residual_complex", "triples_complex",
+           "coulomb_integrals_pp"]
 
 
 def make_opts(mixer="LinearMixer", max_residua=4, mixing_ratio=1.0,
               max_iterations=16, energy_convergence=1e-6,
               amplitudes_convergence=1e-5, level_shift=0.0, distinguishable=0,
               ppl=1, slice_size=-1, slice_factor=None, precision="fp64",
-              emu_slices=0):
+              emu_slices=0, formulation="vertex", only_ppl=0):
     o = capi.CcsdOpts()
     capi.load().gbcc_ccsd_opts_default(C.byref(o))
     o.mixer = {"LinearMixer": 0, "DiisMixer": 1}[mixer]
@@ -36,6 +37,10 @@ def make_opts(mixer="LinearMixer", max_residua=4, mixing_ratio=1.0,
     o.integrals_slice_factor = -1.0 if slice_factor is None else float(slice_factor)
     o.precision = {"fp64": capi.PREC_FP64, "emu": capi.PREC_EMU}[precision]
     o.emu_slices = int(emu_slices)
+    # "vertex": CcsdEnergyFromCoulombIntegrals; "stored":
+    # CcsdEnergyFromCoulombIntegralsReference (resident Vabcd / Vabci)
+    o.formulation = {"vertex": 0, "stored": 1}[formulation]
+    o.only_ppl = int(only_ppl)
     return o
 
 
@@ -71,7 +76,8 @@ def _vertex(gamma, No, Nv):
     return fortran_flat(g), None
 
 
-_INTEGRAL_SHAPES = {"PPHH": "vvoo", "PHPH": "vovo", "HHHH": "oooo", "HHHP": "ooov"}
+_INTEGRAL_SHAPES = {"PPHH": "vvoo", "PHPH": "vovo", "HHHH": "oooo", "HHHP": "ooov",
+                    "PPPP": "vvvv", "PPPH": "vvvo"}
 
 
 def _shape(code, No, Nv):
@@ -79,13 +85,19 @@ def _shape(code, No, Nv):
 
 
 class CcsdInput:
-    """Owns the column-major host buffers behind a ``gbcc_ccsd_in``."""
+    """Owns the column-major host buffers behind a ``gbcc_ccsd_in``.  The
+    vertex may be None for the stored formulation when every integral it
+    reads (PPHH, PHPH, HHHH, HHHP, PPPP, PPPH) is given."""
 
     def __init__(self, eps_h, eps_p, gamma, ints=None, initial=None, fock_hp=None):
         eps_h, eps_p = _eigenenergies(eps_h, eps_p)
         No, Nv = eps_h.size, eps_p.size
-        g, self.gamma_imag = _vertex(gamma, No, Nv)
-        self.No, self.Nv, self.NG = No, Nv, np.shape(gamma)[0]
+        if gamma is None:
+            g, self.gamma_imag, NG = None, None, 0
+        else:
+            g, self.gamma_imag = _vertex(gamma, No, Nv)
+            NG = np.shape(gamma)[0]
+        self.No, self.Nv, self.NG = No, Nv, NG
         self._keep = [eps_h, eps_p, g, self.gamma_imag]
         s = capi.CcsdIn()
         s.No, s.Nv, s.NG = self.No, self.Nv, self.NG
@@ -93,7 +105,8 @@ class CcsdInput:
         s.gamma, s.gamma_imag = ptr(g), ptr(self.gamma_imag)
         ints = ints or {}
         for key, field in (("PPHH", "Vabij"), ("PHPH", "Vaibj"),
-                           ("HHHH", "Vijkl"), ("HHHP", "Vijka")):
+                           ("HHHH", "Vijkl"), ("HHHP", "Vijka"),
+                           ("PPPP", "Vabcd"), ("PPPH", "Vabci")):
             if key in ints and ints[key] is not None:
                 f = _flat(ints[key], _shape(_INTEGRAL_SHAPES[key], No, Nv), key)
                 self._keep.append(f)
@@ -253,6 +266,24 @@ def coulomb_integrals(ctx, gamma, No):
             "HHHH": from_fortran_flat(vijkl, (No, No, No, No)),
             "HHHP": from_fortran_flat(vijka, (No, No, No, Nv)),
             "HHPP": from_fortran_flat(vijab, (No, No, Nv, Nv))}
+
+
+def coulomb_integrals_pp(ctx, gamma, No):
+    """PPPP (Vabcd) and PPPH (Vabci) integrals of the stored formulation."""
+    NG, Np = np.shape(gamma)[0], np.shape(gamma)[1]
+    Nv = Np - No
+    if not 0 < No < Np:
+        raise ValueError("No must lie in 1..Np-1")
+    g, gi = _vertex(gamma, No, Nv)
+    if gi is not None and np.any(gi):
+        raise capi.GbccError(capi.COMPLEX_UNSUPPORTED,
+                             "the vertex has a non-zero imaginary part")
+    vabcd = np.zeros(Nv ** 4)
+    vabci = np.zeros(Nv ** 3 * No)
+    ctx.check(ctx.lib.gbcc_coulomb_integrals_pp(ctx.h, No, Nv, NG, ptr(g), ptr(vabcd),
+                                                ptr(vabci)))
+    return {"PPPP": from_fortran_flat(vabcd, (Nv, Nv, Nv, Nv)),
+            "PPPH": from_fortran_flat(vabci, (Nv, Nv, Nv, No))}
 
 
 # ------------------------------------------------------------- complex branch

@@ -64,6 +64,9 @@ void check_opts(const gbcc_ccsd_opts &o) {
   gbcc::require(o.mixer == 0 || o.mixer == 1, "unknown mixer");
   gbcc::require(o.precision == GBCC_PREC_FP64 || o.precision == GBCC_PREC_EMU,
                 "unknown precision");
+  gbcc::require(o.formulation == 0 || o.formulation == 1, "unknown formulation");
+  gbcc::require(o.only_ppl == 0 || o.formulation == 1,
+                "onlyPPL belongs to CcsdEnergyFromCoulombIntegralsReference");
 }
 
 void apply_precision_opts(gbcc::Context &c, const gbcc_ccsd_opts &o) {
@@ -236,6 +239,8 @@ void gbcc_ccsd_opts_default(gbcc_ccsd_opts *o) {
   o->integrals_slice_factor = -1.0;
   o->precision = GBCC_PREC_FP64;
   o->emu_slices = 0;
+  o->formulation = 0;
+  o->only_ppl = 0;
 }
 
 gbcc_status gbcc_ccsd_setup(gbcc_ctx *ctx, const gbcc_ccsd_in *in,
@@ -247,7 +252,7 @@ gbcc_status gbcc_ccsd_setup(gbcc_ctx *ctx, const gbcc_ccsd_in *in,
     if (opts) o = *opts; else gbcc_ccsd_opts_default(&o);
     check_opts(o);
     apply_precision_opts(ctx->c, o);
-    auto inputs = gbcc::upload_inputs(ctx->c, *in, o.precision, true);
+    auto inputs = gbcc::upload_inputs(ctx->c, *in, o.precision, true, o.formulation == 1);
     auto s = std::make_unique<gbcc_solver>();
     s->ctx = ctx;
     s->opts = o;
@@ -351,7 +356,7 @@ gbcc_status gbcc_ccsd_residual(gbcc_ctx *ctx, const gbcc_ccsd_in *in,
     if (opts) o = *opts; else gbcc_ccsd_opts_default(&o);
     check_opts(o);
     apply_precision_opts(ctx->c, o);
-    auto inputs = gbcc::upload_inputs(ctx->c, *in, o.precision, true);
+    auto inputs = gbcc::upload_inputs(ctx->c, *in, o.precision, true, o.formulation == 1);
     gbcc::Ccsd c(ctx->c, std::move(inputs), o, in->init_T1, in->init_T2);
     const auto &L = c.layout();
     gbcc::DBuf T(ctx->c, 8 * L.ntot), R(ctx->c, 8 * L.ntot);
@@ -477,6 +482,27 @@ gbcc_status gbcc_coulomb_integrals(gbcc_ctx *ctx, int No, int Nv, int NG,
       GBCC_CUDA(cudaMemcpyAsync(Vijab, t.p(), 8 * v * v * o * o, cudaMemcpyDeviceToHost, st));
       GBCC_CUDA(cudaStreamSynchronize(st));
     }
+    GBCC_CUDA(cudaStreamSynchronize(st));
+    return GBCC_OK;
+  });
+}
+
+gbcc_status gbcc_coulomb_integrals_pp(gbcc_ctx *ctx, int No, int Nv, int NG,
+                                      const double *gamma, double *Vabcd, double *Vabci) {
+  if (!ctx || !gamma) return GBCC_BAD_ARG;
+  return guard(ctx, [&]() {
+    gbcc::require(No > 0 && Nv > 0 && NG > 0, "No, Nv, NG must be positive");
+    gbcc_ccsd_in ci{};
+    ci.No = No; ci.Nv = Nv; ci.NG = NG;
+    std::vector<double> eh(No, 0.0), ep(Nv, 0.0);
+    ci.eps_h = eh.data();
+    ci.eps_p = ep.data();
+    ci.gamma = gamma;
+    auto I = gbcc::upload_inputs(ctx->c, ci, GBCC_PREC_FP64, false, true);
+    cudaStream_t st = ctx->c.stream;
+    const int64_t o = No, v = Nv;
+    if (Vabcd) GBCC_CUDA(cudaMemcpyAsync(Vabcd, I->Vabcd.p(), 8 * v * v * v * v, cudaMemcpyDeviceToHost, st));
+    if (Vabci) GBCC_CUDA(cudaMemcpyAsync(Vabci, I->Vabci.p(), 8 * v * v * v * o, cudaMemcpyDeviceToHost, st));
     GBCC_CUDA(cudaStreamSynchronize(st));
     return GBCC_OK;
   });

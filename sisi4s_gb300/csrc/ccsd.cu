@@ -31,9 +31,14 @@ constexpr int SC_N = 32;
 }  // namespace
 
 std::unique_ptr<CcsdInputs> upload_inputs(Context &ctx, const gbcc_ccsd_in &in,
-                                          int precision, bool need_vaibj) {
-  require(in.No > 0 && in.Nv > 0 && in.NG > 0, "No, Nv, NG must be positive");
+                                          int precision, bool need_vaibj, bool stored) {
+  require(in.No > 0 && in.Nv > 0, "No and Nv must be positive");
   require(in.eps_h && in.eps_p, "eigenenergies are required");
+  // the stored formulation (CcsdEnergyFromCoulombIntegralsReference) takes
+  // its integrals and needs no vertex when all of them are given
+  const bool all_ints = in.Vabij && in.Vaibj && in.Vijkl && in.Vijka && in.Vabcd && in.Vabci;
+  require(in.gamma != nullptr || (stored && all_ints), "CoulombVertex is required");
+  require(in.gamma == nullptr || in.NG > 0, "NG must be positive");
   auto p = std::make_unique<CcsdInputs>();
   const int64_t No = in.No, Nv = in.Nv, NG = in.NG, Np = No + Nv;
   p->No = No; p->Nv = Nv; p->NG = NG;
@@ -43,8 +48,7 @@ std::unique_ptr<CcsdInputs> upload_inputs(Context &ctx, const gbcc_ccsd_in &in,
                             cudaMemcpyHostToDevice, ctx.stream));
   GBCC_CUDA(cudaMemcpyAsync(p->eps_p.p(), in.eps_p, 8 * Nv,
                             cudaMemcpyHostToDevice, ctx.stream));
-  require(in.gamma != nullptr, "CoulombVertex is required");
-  {
+  if (in.gamma) {
     OTen G(ctx, {NG, Np, Np});
     if (in.gamma_imag) {
       GBCC_CUDA(cudaMemcpyAsync(G.p(), in.gamma_imag, 8 * G.t.size(),
@@ -100,6 +104,19 @@ std::unique_ptr<CcsdInputs> upload_inputs(Context &ctx, const gbcc_ccsd_in &in,
   }
   p->Vx = OTen(ctx, {Nv, Nv, No, No});
   assign(ctx, 1.0, p->Vabij, "baij", 0.0, p->Vx, "abij");
+  if (stored) {
+    // CoulombIntegralsFromVertex.cxx:423-431
+    if (in.Vabcd) up(p->Vabcd, in.Vabcd, {Nv, Nv, Nv, Nv});
+    else {
+      p->Vabcd = OTen(ctx, {Nv, Nv, Nv, Nv});
+      contract(ctx, 1.0, p->Gab, "Gac", p->Gab, "Gbd", 0.0, p->Vabcd, "abcd", precision);
+    }
+    if (in.Vabci) up(p->Vabci, in.Vabci, {Nv, Nv, Nv, No});
+    else {
+      p->Vabci = OTen(ctx, {Nv, Nv, Nv, No});
+      contract(ctx, 1.0, p->Gab, "Gac", p->Gai, "Gbi", 0.0, p->Vabci, "abci", precision);
+    }
+  }
   if (in.fock_hp) {
     // f[i,a] is kept as f[a,i], so the noncanonical energy term is a plain
     // dot with T1[a,i]
@@ -183,6 +200,10 @@ void Ccsd::pair_energies(double *dev_out) {
 }
 
 void Ccsd::residual(int it, const double *Tp, double *Rp) {
+  if (o_.formulation == 1) {  // CcsdEnergyFromCoulombIntegralsReference
+    residual_stored(it, Tp, Rp);
+    return;
+  }
   Context &ctx = ctx_;
   CcsdInputs &I = *in_;
   const int prec = o_.precision;

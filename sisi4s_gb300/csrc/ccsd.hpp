@@ -14,12 +14,14 @@ struct CcsdInputs {
   OTen Gai, Gab, Gij;         // [NG,Nv,No], [NG,Nv,Nv], [NG,No,No]
   OTen Vabij, Vx, Vaibj, Vijkl, Vijka;  // Vx[a,b,i,j] = Vabij[b,a,i,j]
   OTen fock_ai;               // HPFockMatrix as f[a,i] [Nv,No], if given
+  OTen Vabcd, Vabci;          // stored formulation: [Nv,Nv,Nv,Nv], [Nv,Nv,Nv,No]
 };
 
 // Upload eps and Gamma, slice the vertex blocks, upload or build the
 // integrals (CoulombIntegralsFromVertex.cxx:395-417).
 std::unique_ptr<CcsdInputs> upload_inputs(Context &ctx, const gbcc_ccsd_in &in,
-                                          int precision, bool need_vaibj);
+                                          int precision, bool need_vaibj,
+                                          bool stored = false);
 
 struct IterInfo {
   double energy = 0, direct = 0, exchange = 0, noncanonical = 0, dtdt = 0, tt = 0,
@@ -83,6 +85,7 @@ class Ccsd {
   std::vector<Graph> graphs_;
   uint64_t swaps_ = 0;
   void iteration_body();
+  void residual_stored(int it, const double *T, double *R);
   void energy_sums(const double *amp);
   void energy_from_sums(const double *h, IterInfo &info) const;
 };

@@ -191,7 +191,7 @@ gbcc_status gbcc_server_submit(gbcc_server *s, const gbcc_ccsd_in *in,
   if (!s || !in || !in->eps_h || !in->eps_p || !in->gamma) return GBCC_BAD_ARG;
   if (in->No <= 0 || in->Nv <= 0 || in->NG <= 0) return GBCC_BAD_ARG;
   if (in->Vabij || in->Vaibj || in->Vijkl || in->Vijka || in->init_T1 || in->init_T2 ||
-      in->gamma_imag || in->fock_hp)
+      in->gamma_imag || in->fock_hp || in->Vabcd || in->Vabci)
     return GBCC_BAD_ARG;  // requests carry the vertex only; integrals are built on device
   auto r = std::make_unique<Request>();
   const size_t Np = (size_t)in->No + in->Nv;

@@ -493,11 +493,23 @@ struct CoulombIntegralsFromVertex : Algorithm {
                                  pphh->re.data(), phph->re.data(), hhhh->re.data(),
                                  hhhp->re.data(), hhpp->re.data()),
           "CoulombIntegralsFromVertex");
+    // the particle blocks of the stored formulation, only when requested
+    // (PPPP alone is Nv^4 doubles)
+    std::shared_ptr<HTensor> pppp, ppph;
+    if (given("PPPPCoulombIntegrals") || given("PPPHCoulombIntegrals")) {
+      if (given("PPPPCoulombIntegrals")) pppp = mk({v, v, v, v});
+      if (given("PPPHCoulombIntegrals")) ppph = mk({v, v, v, o});
+      check(gbcc_coulomb_integrals_pp(gpu(), s.No, s.Nv, s.NG, g.re.data(),
+                                      pppp ? pppp->re.data() : nullptr,
+                                      ppph ? ppph->re.data() : nullptr),
+            "CoulombIntegralsFromVertex");
+    }
     Json list = Json::array();
     const std::pair<const char *, std::shared_ptr<HTensor>> built[] = {
         {"PPHHCoulombIntegrals", pphh}, {"PHPHCoulombIntegrals", phph},
         {"HHHHCoulombIntegrals", hhhh}, {"HHHPCoulombIntegrals", hhhp},
-        {"HHPPCoulombIntegrals", hhpp}};
+        {"HHPPCoulombIntegrals", hhpp}, {"PPPPCoulombIntegrals", pppp},
+        {"PPPHCoulombIntegrals", ppph}};
     for (auto &b : built)
       if (given(b.first)) {
         set_tensor(b.first, b.second);
@@ -559,6 +571,10 @@ std::shared_ptr<HTensor> complex_tensor(const std::vector<int64_t> &lens,
 
 // CcsdEnergyFromCoulombIntegrals (ClusterSinglesDoublesAlgorithm.cxx:25-128)
 struct CcsdEnergyFromCoulombIntegrals : Algorithm {
+  // 0: particle ladder from the vertex; 1: stored Vabcd / Vabci
+  // (CcsdEnergyFromCoulombIntegralsReference)
+  virtual int formulation() const { return 0; }
+
   // the complex branch, taken when the vertex is complex (:25-35); the
   // integrals are built from the vertex on the device
   void run_complex(const Sizes &s, const gbcc_ccsd_opts &o) {
@@ -617,9 +633,12 @@ struct CcsdEnergyFromCoulombIntegrals : Algorithm {
 
   void run() override {
     const Sizes s = sizes_of(*this);
-    if (!given("CoulombVertex")) throw StepError("CoulombVertex is required");
+    if (formulation() == 0 && !given("CoulombVertex"))
+      throw StepError("CoulombVertex is required");
     gbcc_ccsd_opts o;
     gbcc_ccsd_opts_default(&o);
+    o.formulation = formulation();
+    if (formulation() == 1) o.only_ppl = (int)integer("onlyPPL", 0);
     const std::string mixer = text("mixer", "LinearMixer");
     if (mixer == "LinearMixer") o.mixer = 0;
     else if (mixer == "DiisMixer") o.mixer = 1;
@@ -642,9 +661,10 @@ struct CcsdEnergyFromCoulombIntegrals : Algorithm {
     emit["amplitudesConvergence"] = std::abs(o.amplitudes_convergence);
     emit["energyConvergence"] = std::abs(o.energy_convergence);
     emit["precision"] = o.precision == GBCC_PREC_FP64 ? "fp64" : "emu";
-    if (has_imaginary_part(tensor("CoulombVertex"))) {
-      if (given("HPFockMatrix"))
-        throw StepError("HPFockMatrix is not supported for complex amplitudes");
+    if (given("CoulombVertex") && has_imaginary_part(tensor("CoulombVertex"))) {
+      if (given("HPFockMatrix") || formulation() != 0)
+        throw StepError("only CcsdEnergyFromCoulombIntegrals without HPFockMatrix has a "
+                        "complex branch here");
       run_complex(s, o);
       return;
     }
@@ -652,10 +672,16 @@ struct CcsdEnergyFromCoulombIntegrals : Algorithm {
     in.No = s.No; in.Nv = s.Nv; in.NG = s.NG;
     in.eps_h = tensor("HoleEigenEnergies").re.data();
     in.eps_p = tensor("ParticleEigenEnergies").re.data();
-    const HTensor &g = tensor("CoulombVertex");
-    in.gamma = g.re.data();
-    in.gamma_imag = g.complex ? g.im.data() : nullptr;
+    if (given("CoulombVertex")) {
+      const HTensor &g = tensor("CoulombVertex");
+      in.gamma = g.re.data();
+      in.gamma_imag = g.complex ? g.im.data() : nullptr;
+    }
     const int64_t o1 = s.No, v1 = s.Nv;
+    if (formulation() == 1) {
+      in.Vabcd = tensor_or_null("PPPPCoulombIntegrals", {v1, v1, v1, v1});
+      in.Vabci = tensor_or_null("PPPHCoulombIntegrals", {v1, v1, v1, o1});
+    }
     in.Vabij = tensor_or_null("PPHHCoulombIntegrals", {v1, v1, o1, o1});
     in.Vaibj = tensor_or_null("PHPHCoulombIntegrals", {v1, o1, v1, o1});
     in.Vijkl = tensor_or_null("HHHHCoulombIntegrals", {o1, o1, o1, o1});
@@ -706,6 +732,15 @@ struct CcsdEnergyFromCoulombIntegrals : Algorithm {
   }
 };
 REGISTER_ALGORITHM(CcsdEnergyFromCoulombIntegrals);
+
+// CcsdEnergyFromCoulombIntegralsReference
+// (src/algorithms/CcsdEnergyFromCoulombIntegralsReference.cxx:29-292): the
+// same driver and outputs, with the ladder from resident PPPP / PPPH
+// integrals; the vertex is optional when every integral is given.
+struct CcsdEnergyFromCoulombIntegralsReference : CcsdEnergyFromCoulombIntegrals {
+  int formulation() const override { return 1; }
+};
+REGISTER_ALGORITHM(CcsdEnergyFromCoulombIntegralsReference);
 
 // CcsdPerturbativeTriples (CcsdPerturbativeTriples.cxx:119-248)
 struct CcsdPerturbativeTriples : Algorithm {

@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "ccsd_complex.hpp"
+#include "ccsd_stored.hpp"
 
 namespace {
 
@@ -347,6 +348,36 @@ int cx_solve(int No, int Nv, int NG, const double *eh, const double *ep,
     const gbcc::cx::Layout L(Nv, No);
     rb.store_complex(gbcc::cx::t1_of(T, L), T1);
     rb.store_complex(gbcc::cx::t2_of(T, L), T2);
+    return 0;
+  } catch (const std::exception &e) {
+    g_err = e.what();
+    return 1;
+  }
+}
+
+// stored-integral residual (real buffers, first index fastest)
+int st_residual(int No, int Nv, int it, int init_doubles, int only_ppl, const double *Vabij,
+                const double *Vaibj, const double *Vijkl, const double *Vijka,
+                const double *Vabcd, const double *Vabci, const double *T1, const double *T2,
+                double *R1, double *R2) {
+  try {
+    HostBackend rb;
+    auto v = [](const double *p, std::initializer_list<int64_t> l) {
+      return gbcc::cx::view(const_cast<double *>(p), l);
+    };
+    const int64_t o = No, n = Nv;
+    gbcc::st::Ints I;
+    I.Vabij = v(Vabij, {n, n, o, o});
+    I.Vaibj = v(Vaibj, {n, o, n, o});
+    I.Vijkl = v(Vijkl, {o, o, o, o});
+    I.Vijka = v(Vijka, {o, o, o, n});
+    I.Vabcd = v(Vabcd, {n, n, n, n});
+    I.Vabci = v(Vabci, {n, n, n, o});
+    gbcc::st::Opts opts;
+    opts.init_doubles = init_doubles != 0;
+    opts.only_ppl = only_ppl != 0;
+    gbcc::st::residual(rb, I, it, opts, v(T1, {n, o}), v(T2, {n, n, o, o}), v(R1, {n, o}),
+                       v(R2, {n, n, o, o}));
     return 0;
   } catch (const std::exception &e) {
     g_err = e.what();

@@ -213,6 +213,9 @@ def _read_steps(names):
     ("CcsdEnergyFromCoulombIntegrals", "V",
      "PPHHCoulombIntegrals has lengths [3,3,2,3], expected [3,3,2,2]"),
     ("CcsdEnergyFromCoulombIntegrals", "F", "HPFockMatrix has lengths [2,4], expected [2,3]"),
+    ("CcsdEnergyFromCoulombIntegralsReference", None, None),
+    ("CcsdEnergyFromCoulombIntegralsReference", "P4",
+     "PPPPCoulombIntegrals has lengths [3,3,3,4], expected [3,3,3,3]"),
 ])
 def test_tensor_lengths_are_checked_before_the_library_is_called(tmp_path, step, bad, msg):
     # the C ABI takes bare pointers: a tensor of the wrong lengths must be
@@ -220,7 +223,8 @@ def test_tensor_lengths_are_checked_before_the_library_is_called(tmp_path, step,
     rng = np.random.default_rng(1)
     No, Nv, NG = 2, 3, 4
     good = {"Eh": (No,), "Ep": (Nv,), "G": (NG, No + Nv, No + Nv), "T1": (Nv, No),
-            "T2": (Nv, Nv, No, No), "V": (Nv, Nv, No, No), "F": (No, Nv)}
+            "T2": (Nv, Nv, No, No), "V": (Nv, Nv, No, No), "F": (No, Nv),
+            "P4": (Nv, Nv, Nv, Nv), "P3": (Nv, Nv, Nv, No)}
     for n, shape in good.items():
         if n == bad:
             shape = shape[:-1] + (shape[-1] + 1,)
@@ -232,6 +236,8 @@ def test_tensor_lengths_are_checked_before_the_library_is_called(tmp_path, step,
     HoleEigenEnergies: $Eh
     ParticleEigenEnergies: $Ep
     PPHHCoulombIntegrals: $V
+    PPPPCoulombIntegrals: $P4
+    PPPHCoulombIntegrals: $P3
     HPFockMatrix: $F
     CcsdEnergy: 0.0
     CcsdSinglesAmplitudes: $T1
@@ -329,7 +335,7 @@ def test_complex_vertex_takes_the_complex_branch(tmp_path):
 """
     r, out = _run(tmp_path, reads + "- name: CcsdEnergyFromCoulombIntegrals\n  in:\n" + common
                   + "    HPFockMatrix: $F\n  out: {}\n")
-    assert r.returncode == 1 and "not supported for complex" in out["error"], out
+    assert r.returncode == 1 and "without HPFockMatrix has a complex branch" in out["error"], out
     r, out = _run(tmp_path, reads + "- name: CcsdPerturbativeTriples\n  in:\n" + common
                   + "    CcsdEnergy: 0.0\n    CcsdSinglesAmplitudes: $T1\n"
                   "    CcsdDoublesAmplitudes: $T2\n  out: {}\n")

@@ -1,8 +1,11 @@
-"""The complex CCSD program of the library, run on the host (no GPU).
+"""The complex CCSD programs of the library, and its stored-integral
+residual, run on the host (no GPU).
 
 ``sisi4s_gb300/csrc/ccsd_complex.hpp`` holds the complex branch's statement
-sequence once, over a backend of real primitives; the library runs it with
-its CUDA backend.  Here the same source is compiled with the host backend in
+sequence once, over a backend of real primitives, and
+``sisi4s_gb300/csrc/ccsd_stored.hpp`` the stored-V_abcd residual
+(CcsdEnergyFromCoulombIntegralsReference); the library runs both with its
+CUDA backend.  Here the same source is compiled with the host backend in
 ``tests/harness/cx_host.cpp`` (naive loops restating each primitive, with the
 contraction engine's restrictions) and compared with the complex oracle,
 which is pinned to the reference's golden energies.
@@ -30,8 +33,8 @@ def lib():
     so = os.path.join(out, "libcx_host.so")
     src = os.path.join(HARNESS, "cx_host.cpp")
     hdr = os.path.join(ROOT, "sisi4s_gb300", "csrc", "ccsd_complex.hpp")
-    if not os.path.exists(so) or os.path.getmtime(so) < max(os.path.getmtime(src),
-                                                           os.path.getmtime(hdr)):
+    deps = [src, hdr, os.path.join(os.path.dirname(hdr), "ccsd_stored.hpp")]
+    if not os.path.exists(so) or os.path.getmtime(so) < max(map(os.path.getmtime, deps)):
         subprocess.run(["g++", "-std=c++17", "-O2", "-Wall", "-Wextra", "-Werror",
                         "-fPIC", "-shared", "-I", os.path.dirname(hdr), src, "-o", so],
                        check=True, capture_output=True, text=True)
@@ -136,3 +139,32 @@ def test_triples_program_matches_oracle(lib, No, Nv, NG):
                         _p(_flat(T2)), _p(et))
     assert st == 0, lib.cx_last_error()
     assert abs(complex(et[0], et[1]) - ref) < 1e-13 * abs(ref)
+
+
+@pytest.mark.parametrize("it,init,only_ppl", [(1, 1, 0), (0, 1, 0), (0, 0, 0), (1, 1, 1)])
+def test_stored_residual_program_matches_oracle(lib, it, init, only_ppl):
+    from oracle.ccsd import residual_reference
+    from oracle.coulomb import coulomb_integrals
+    No, Nv, NG = 3, 7, 12
+    s = make_system(No, Nv, NG, seed=8)
+    ints = coulomb_integrals(s.gamma, No, keys=("PPHH", "PHPH", "HHHH", "HHHP", "PPPP", "PPPH"))
+    rng = np.random.default_rng(2)
+    T1 = rng.normal(0, 0.05, (Nv, No))
+    T2 = rng.normal(0, 0.05, (Nv, Nv, No, No))
+    T2 = 0.5 * (T2 + T2.transpose(1, 0, 3, 2))
+    f = lambda a: np.ascontiguousarray(a.transpose(tuple(range(a.ndim - 1, -1, -1)))).ravel()
+    r1 = np.zeros(Nv * No)
+    r2 = np.zeros(Nv * Nv * No * No)
+    args = [f(ints[k]) for k in ("PPHH", "PHPH", "HHHH", "HHHP", "PPPP", "PPPH")]
+    st = lib.st_residual(No, Nv, it, init, only_ppl, *[_p(a) for a in args], _p(f(T1)),
+                         _p(f(T2)), _p(r1), _p(r2))
+    assert st == 0, lib.cx_last_error()
+    o1, o2 = residual_reference(it, T1, T2, ints, initial_doubles=bool(init),
+                                only_ppl=bool(only_ppl))
+    g1 = r1.reshape(No, Nv).T
+    g2 = r2.reshape(No, No, Nv, Nv).transpose(3, 2, 1, 0)
+    assert np.abs(g2 - o2).max() < 1e-13 * np.abs(o2).max()
+    if np.any(o1):
+        assert np.abs(g1 - o1).max() < 1e-13 * np.abs(o1).max()
+    else:
+        assert not np.any(g1)
