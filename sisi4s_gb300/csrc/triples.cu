@@ -299,6 +299,9 @@ __global__ void sum_rows_kernel(const double *__restrict__ partials, int nb,
 // E_(T) for device-resident inputs.
 double triples_energy(Context &ctx, const CcsdInputs &I, const double *T1,
                       const double *T2, int precision) {
+  // a solver of the stored formulation may have been set up without a vertex
+  require(I.Gab.p() && I.Gai.p() && I.Vabij.p() && I.Vijka.p(),
+          "(T) needs the CoulombVertex");
   const int64_t No = I.No, Nv = I.Nv;
   // Precision mode: W is produced as float-float by the emulated GEMMs and the
   // epilogue computes in float-float; FP64 mode computes in double.  Both
