@@ -1,6 +1,7 @@
 """Mixed vs FP64 CCSD(T) on one seeded synthetic system.
 
     python -m sisi4s_gb300.solve_bench No Nv NG [--iterations N] [--no-triples]
+        [--formulation vertex|stored]
 
 Runs N CCSD iterations (DIIS with 5 vectors, MP2 start) in precision mode and
 in FP64 on the GPU, then the (T) correction on each run's final amplitudes in
@@ -13,14 +14,15 @@ import json
 import time
 
 
-def run(ctx, s, precision, iterations, triples, triples_fp64=False):
+def run(ctx, s, precision, iterations, triples, triples_fp64=False, formulation="vertex"):
     import torch  # device synchronisation only
 
     from . import ccsd as gpu
 
     sol = gpu.Solver(ctx, s.eps_h, s.eps_p, s.gamma, mixer="DiisMixer", max_residua=5,
                      max_iterations=iterations + 1, energy_convergence=0.0,
-                     amplitudes_convergence=0.0, precision=precision)
+                     amplitudes_convergence=0.0, precision=precision,
+                     formulation=formulation)
     sol.step(1)  # first iteration (setup, graph capture)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -58,6 +60,9 @@ def main():
                     help="skip the FP64 run (compare against a recorded one)")
     ap.add_argument("--triples-fp64-on-emu", action="store_true",
                     help="also run the FP64 (T) on the precision-mode amplitudes")
+    ap.add_argument("--formulation", default="vertex", choices=["vertex", "stored"],
+                    help="vertex: CcsdEnergyFromCoulombIntegrals; stored: "
+                         "CcsdEnergyFromCoulombIntegralsReference (resident Vabcd)")
     args = ap.parse_args()
 
     from . import capi
@@ -67,15 +72,16 @@ def main():
     ctx = capi.Context(0)
     ctx.set_emulation(args.slices, 1e7)
     trip = not args.no_triples
-    emu = run(ctx, s, "emu", args.iterations, trip, trip and args.triples_fp64_on_emu)
+    emu = run(ctx, s, "emu", args.iterations, trip, trip and args.triples_fp64_on_emu,
+              args.formulation)
     line = {"No": args.No, "Nv": args.Nv, "NG": args.NG, "seed": args.seed,
             "iterations": args.iterations, "mixer": "DiisMixer(5), MP2 start",
-            "slices": args.slices, "emu": emu}
+            "slices": args.slices, "formulation": args.formulation, "emu": emu}
     if args.emu_only:
         print(json.dumps(line), flush=True)
         ctx.close()
         return
-    f64 = run(ctx, s, "fp64", args.iterations, trip)
+    f64 = run(ctx, s, "fp64", args.iterations, trip, formulation=args.formulation)
     line.update(fp64=f64, dE_ccsd_ha=emu["energy"] - f64["energy"],
                 speedup_iteration=f64["seconds_per_iteration"] / emu["seconds_per_iteration"])
     if trip:
