@@ -16,7 +16,9 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cctype>
 #include <cmath>
+#include <complex>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
@@ -400,28 +402,241 @@ struct Write : Algorithm {
 };
 REGISTER_ALGORITHM(Write);
 
-// TensorWriter (src/algorithms/TensorWriter.cxx:21-81): text by default,
-// one element per line, first index fastest; mode: binary writes raw doubles
+// ------------------------------------------------ TensorWriter / Reader
+// The formats of src/util/TensorIo.cxx and src/util/BinaryTensorFormat.hpp.
+//
+// Text (:158-226): a line "name<d>order<d>len0<d>len1...", a line
+// "rowIndexOrder<d>columnIndexOrder", then one line per row with the column
+// elements separated by the delimiter; index letters are 'i' + dim; without
+// orders every element is one row, first index fastest.  Numbers are written
+// with 16 significant digits, complex ones as "(re,im)".
+//
+// Binary (:120-155): a 32-byte header {"TENS", int32 version 0x9000, "IEEE",
+// int32 bytes per number, int32 numbers per element, int32 order, int32 flags,
+// int32 reserved}, one 8-byte header {int32 length, char index name 'a'+dim,
+// int8 flags, int16 reserved} per dimension, then the dense data (first index
+// fastest, complex as (re, im) pairs).
+
+// element offsets of the layout a text file is written in: dims of
+// columnIndexOrder (fastest first), then those of rowIndexOrder
+std::vector<int64_t> text_layout(const HTensor &t, const std::string &rows,
+                                 const std::string &cols, int64_t *ncols) {
+  const int order = (int)t.lens.size();
+  const std::string all = cols + rows;
+  std::vector<int> used(order, 0);
+  if ((int)all.size() != order)
+    throw StepError("rowIndexOrder and columnIndexOrder must hold the tensor's " +
+                    std::to_string(order) + " indices");
+  std::vector<int> dims;
+  for (char c : all) {
+    const int d = c - 'i';
+    if (d < 0 || d >= order || used[d]++)
+      throw StepError(std::string("bad index '") + c + "' in the index orders");
+    dims.push_back(d);
+  }
+  std::vector<int64_t> stride(order, 1);
+  for (int d = 1; d < order; ++d) stride[d] = stride[d - 1] * t.lens[d - 1];
+  *ncols = 1;
+  for (size_t q = 0; q < cols.size(); ++q) *ncols *= t.lens[dims[q]];
+  std::vector<int64_t> off((size_t)t.size());
+  std::vector<int64_t> idx(order, 0);
+  for (int64_t e = 0; e < t.size(); ++e) {
+    int64_t o = 0;
+    for (int q = 0; q < order; ++q) o += idx[q] * stride[dims[q]];
+    off[e] = o;
+    for (int q = 0; q < order; ++q) {
+      if (++idx[q] < t.lens[dims[q]]) break;
+      idx[q] = 0;
+    }
+  }
+  return off;
+}
+
+const char kMagic[4] = {'T', 'E', 'N', 'S'};
+const char kIeee[4] = {'I', 'E', 'E', 'E'};
+const int32_t kBinaryVersion = 0x09000;
+
+template <class T>
+void put(std::ostream &f, T v) {
+  f.write(reinterpret_cast<const char *>(&v), sizeof v);
+}
+template <class T>
+T get(std::istream &f, const std::string &file) {
+  T v;
+  if (!f.read(reinterpret_cast<char *>(&v), sizeof v)) throw StepError(file + ": truncated");
+  return v;
+}
+
+void write_tensor_binary(const std::string &file, const HTensor &t) {
+  std::ofstream f(file, std::ios::binary);
+  if (!f) throw StepError("cannot open " + file);
+  f.write(kMagic, 4);
+  put<int32_t>(f, kBinaryVersion);
+  f.write(kIeee, 4);
+  put<int32_t>(f, t.complex ? 16 : 8);
+  put<int32_t>(f, t.complex ? 2 : 1);
+  put<int32_t>(f, (int32_t)t.lens.size());
+  put<int32_t>(f, 0);
+  put<int32_t>(f, 0);
+  for (size_t d = 0; d < t.lens.size(); ++d) {
+    put<int32_t>(f, (int32_t)t.lens[d]);
+    put<char>(f, (char)('a' + d));
+    put<int8_t>(f, 0);
+    put<int16_t>(f, 0);
+  }
+  for (int64_t e = 0; e < t.size(); ++e) {
+    put<double>(f, t.re[e]);
+    if (t.complex) put<double>(f, t.im[e]);
+  }
+}
+
+std::shared_ptr<HTensor> read_tensor_binary(const std::string &file, bool complex) {
+  std::ifstream f(file, std::ios::binary);
+  if (!f) throw StepError("Failed to open file \"" + file + "\"");
+  char magic[4], type[4];
+  if (!f.read(magic, 4) || std::memcmp(magic, kMagic, 4) != 0)
+    throw StepError(file + ": invalid file format");
+  if (get<int32_t>(f, file) > kBinaryVersion)
+    throw StepError(file + ": incompatible file format version");
+  if (!f.read(type, 4)) throw StepError(file + ": truncated");
+  const int32_t bytes = get<int32_t>(f, file), per = get<int32_t>(f, file);
+  const int32_t order = get<int32_t>(f, file);
+  get<int32_t>(f, file);
+  get<int32_t>(f, file);
+  if (bytes != (complex ? 16 : 8) || per != (complex ? 2 : 1))
+    throw StepError(file + ": holds a " + (per == 2 ? "complex" : "real") +
+                    " tensor; set complexVersion accordingly");
+  if (order < 0 || order > 16) throw StepError(file + ": bad order");
+  auto t = std::make_shared<HTensor>();
+  int64_t n = 1;
+  for (int d = 0; d < order; ++d) {
+    const int32_t len = get<int32_t>(f, file);
+    get<char>(f, file);
+    get<int8_t>(f, file);
+    get<int16_t>(f, file);
+    if (len < 0 || (len > 0 && n > (INT64_MAX / 16) / len)) throw StepError(file + ": bad length");
+    n *= len;
+    t->lens.push_back(len);
+  }
+  t->complex = complex;
+  t->re.resize(n);
+  if (complex) t->im.resize(n);
+  for (int64_t e = 0; e < n; ++e) {
+    t->re[e] = get<double>(f, file);
+    if (complex) t->im[e] = get<double>(f, file);
+  }
+  return t;
+}
+
+void write_tensor_text(const std::string &file, const std::string &name, const HTensor &t,
+                       std::string rows, const std::string &cols, const std::string &delim) {
+  const int order = (int)t.lens.size();
+  if (rows.empty() && cols.empty())
+    for (int d = 0; d < order; ++d) rows += (char)('i' + d);
+  int64_t ncols = 1;
+  const std::vector<int64_t> off = text_layout(t, rows, cols, &ncols);
+  std::ofstream f(file);
+  if (!f) throw StepError("cannot open " + file);
+  f << name << delim << order;
+  for (auto l : t.lens) f << delim << l;
+  f << "\n" << rows << delim << cols << "\n";
+  f << std::setprecision(16);
+  auto value = [&](int64_t e) {
+    if (t.complex) f << std::complex<double>(t.re[off[e]], t.im[off[e]]);
+    else f << t.re[off[e]];
+  };
+  for (int64_t e = 0; e < t.size(); e += ncols) {
+    value(e);
+    for (int64_t c = 1; c < ncols; ++c) {
+      f << delim;
+      value(e + c);
+    }
+    f << "\n";
+  }
+}
+
+std::shared_ptr<HTensor> read_tensor_text(const std::string &file, bool complex) {
+  std::ifstream f(file);
+  if (!f) throw StepError("Failed to open file \"" + file + "\"");
+  std::string line, rows, cols;
+  std::getline(f, line);
+  const size_t sp = line.find(' ');
+  std::istringstream head(sp == std::string::npos ? "" : line.substr(sp + 1));
+  int order = -1;
+  head >> order;
+  if (order < 0 || order > 16) throw StepError(file + ": bad header");
+  auto t = std::make_shared<HTensor>();
+  for (int d = 0; d < order; ++d) {
+    long long l = -1;
+    head >> l;
+    if (l < 0) throw StepError(file + ": bad header");
+    t->lens.push_back(l);
+  }
+  std::getline(f, line);
+  const size_t sp2 = line.find(' ');
+  rows = line.substr(0, sp2);
+  cols = sp2 == std::string::npos ? "" : line.substr(sp2 + 1);
+  while (!cols.empty() && (cols.back() == '\r' || cols.back() == ' ')) cols.pop_back();
+  t->complex = complex;
+  t->re.assign((size_t)t->size(), 0.0);
+  if (complex) t->im.assign((size_t)t->size(), 0.0);
+  int64_t ncols = 1;
+  const std::vector<int64_t> off = text_layout(*t, rows, cols, &ncols);
+  // numbers as the reference's NumberScanner reads them (strtod; complex as
+  // "(re,im)"), skipping anything between them
+  std::stringstream ss;
+  ss << f.rdbuf();
+  const std::string body = ss.str();
+  const char *p = body.c_str();
+  auto number = [&]() {
+    while (*p && !(std::isdigit((unsigned char)*p) || *p == '-' || *p == '+' || *p == '.'))
+      ++p;
+    char *end = nullptr;
+    const double v = std::strtod(p, &end);
+    if (end == p) throw StepError(file + ": too few elements");
+    p = end;
+    return v;
+  };
+  for (int64_t e = 0; e < t->size(); ++e) {
+    t->re[off[e]] = number();
+    if (complex) t->im[off[e]] = number();
+  }
+  return t;
+}
+
+// TensorWriter (src/algorithms/TensorWriter.cxx:21-81)
 struct TensorWriter : Algorithm {
   void run() override {
     auto d = arg("Data");
     const bool binary = text("mode", "text") == "binary";
     const std::string file = text("file", d->name + (binary ? ".bin" : ".dat"));
     const HTensor &t = tensor("Data");
-    if (binary) {
-      std::ofstream f(file, std::ios::binary);
-      f.write(reinterpret_cast<const char *>(t.re.data()), 8 * t.size());
-    } else {
-      std::ofstream f(file);
-      f << std::setprecision(17);
-      for (int64_t i = 0; i < t.size(); ++i) f << t.re[i] << "\n";
-    }
+    if (binary) write_tensor_binary(file, t);
+    else write_tensor_text(file, d->name, t, text("rowIndexOrder", ""),
+                           text("columnIndexOrder", ""), text("delimiter", " "));
     emit["Data"] = d->name;
     emit["file"] = file;
     emit["elements"] = (long long)t.size();
   }
 };
 REGISTER_ALGORITHM(TensorWriter);
+
+// TensorReader (src/algorithms/TensorReader.cxx:14-63)
+struct TensorReader : Algorithm {
+  void run() override {
+    auto d = arg("Data");
+    const bool binary = text("mode", "text") == "binary";
+    const bool complex = integer("complexVersion", 0) == 1;
+    if (integer("precision", 64) != 64) throw StepError("only precision 64 is supported");
+    const std::string file = text("file", d->name + (binary ? ".bin" : ".dat"));
+    auto t = binary ? read_tensor_binary(file, complex) : read_tensor_text(file, complex);
+    emit["file"] = file;
+    emit["Data"] = d->name;
+    emit["elements"] = (long long)t->size();
+    set_tensor("Data", t);
+  }
+};
+REGISTER_ALGORITHM(TensorReader);
 
 // DefineHolesAndParticles (src/algorithms/cc4s/DefineHolesAndParticles.cxx:8-51)
 struct DefineHolesAndParticles : Algorithm {

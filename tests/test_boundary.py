@@ -115,8 +115,10 @@ def test_read_write_roundtrip_and_symbols(tmp_path):
     assert r.returncode == 0, r.stderr
     back = np.fromfile(tmp_path / "C.elements").reshape(5, 4, 3).transpose(2, 1, 0)
     assert np.array_equal(back, a)
-    txt = np.loadtxt(tmp_path / "B.dat")
-    assert np.allclose(txt, a[0].T.ravel(), rtol=0, atol=0)
+    lines = (tmp_path / "B.dat").read_text().split("\n")
+    assert lines[0] == "B 2 4 5" and lines[1] == "ij "   # name order lens; row / column orders
+    txt = np.array([float(x) for x in lines[2:] if x])
+    assert np.allclose(txt, a[0].T.ravel(), rtol=1e-15, atol=0)
     last = out["steps"][-1]["in"]
     assert last["a"] == 1e-8 and last["b"] == "DiisMixer" and last["c"] == 3
     assert last["d"] == "Undefined"
@@ -196,7 +198,7 @@ def test_list_algorithms():
     names = r.stdout.split()
     for n in ("CcsdEnergyFromCoulombIntegrals", "CcsdPerturbativeTriples",
               "CcsdPerturbativeTriplesComplex",
-              "CoulombIntegralsFromVertex", "Read", "Write", "TensorWriter",
+              "CoulombIntegralsFromVertex", "Read", "Write", "TensorWriter", "TensorReader",
               "DefineHolesAndParticles", "Nop"):
         assert n in names
 
@@ -344,3 +346,72 @@ def test_complex_vertex_takes_the_complex_branch(tmp_path):
                   + "    CcsdEnergy: 0.0\n    CcsdSinglesAmplitudes: $T1\n"
                   "    CcsdDoublesAmplitudes: $T2\n  out: {}\n")
     assert r.returncode == 0 or "GPU context: NO_DEVICE" in out["error"], out
+
+
+def test_tensor_writer_and_reader_formats(tmp_path):
+    """TensorWriter / TensorReader in the formats of src/util/TensorIo.cxx and
+    src/util/BinaryTensorFormat.hpp: text with a header line, index-order line
+    and row x column layout; binary with a 32-byte header and 8 bytes per
+    dimension."""
+    import struct
+    rng = np.random.default_rng(4)
+    a = rng.normal(size=(3, 4, 5))
+    z = rng.normal(size=(2, 3)) + 1j * rng.normal(size=(2, 3))
+    _write_tensor(tmp_path / "A.yaml", a)
+    _write_complex_tensor(tmp_path / "Z.yaml", z)
+    r, out = _run(tmp_path, _read_steps(["A", "Z"]) + """
+- name: TensorWriter
+  in: { Data: $A, rowIndexOrder: jk, columnIndexOrder: i }
+- name: TensorWriter
+  in: { Data: $A, mode: binary }
+- name: TensorWriter
+  in: { Data: $Z, file: Z.dat }
+- name: TensorWriter
+  in: { Data: $Z, mode: binary, file: Z.bin }
+- name: TensorReader
+  in: { file: A.dat }
+  out: { Data: $At }
+- name: TensorReader
+  in: { mode: binary, file: A.bin }
+  out: { Data: $Ab }
+- name: TensorReader
+  in: { file: Z.dat, complexVersion: 1 }
+  out: { Data: $Zt }
+- name: TensorReader
+  in: { mode: binary, file: Z.bin, complexVersion: 1 }
+  out: { Data: $Zb }
+- name: Write
+  in: { source: $At, fileName: At.yaml }
+- name: Write
+  in: { source: $Ab, fileName: Ab.yaml }
+- name: Write
+  in: { source: $Zt, fileName: Zt.yaml }
+- name: Write
+  in: { source: $Zb, fileName: Zb.yaml }
+""")
+    assert r.returncode == 0, (r.stderr, out)
+    # text: one line per (j, k) row, j fastest; the i column values in order
+    lines = (tmp_path / "A.dat").read_text().split("\n")
+    assert lines[0] == "A 3 3 4 5" and lines[1] == "jk i"
+    rows = [list(map(float, x.split(" "))) for x in lines[2:] if x]
+    want = [[a[i, j, k] for i in range(3)] for k in range(5) for j in range(4)]
+    assert np.allclose(rows, want, rtol=1e-15, atol=0)
+    # binary: header, dimension headers, then first-index-fastest data
+    raw = (tmp_path / "A.bin").read_bytes()
+    assert struct.unpack("<4si4siiiii", raw[:32]) == (b"TENS", 0x9000, b"IEEE", 8, 1, 3, 0, 0)
+    dims = [struct.unpack("<icbh", raw[32 + 8 * d:40 + 8 * d]) for d in range(3)]
+    assert dims == [(3, b"a", 0, 0), (4, b"b", 0, 0), (5, b"c", 0, 0)]
+    assert np.array_equal(np.frombuffer(raw[56:]), a.transpose(2, 1, 0).ravel())
+    zraw = (tmp_path / "Z.bin").read_bytes()
+    assert struct.unpack("<4si4siiiii", zraw[:32])[3:6] == (16, 2, 2)
+    assert np.array_equal(np.frombuffer(zraw[48:]).view(np.complex128), z.T.ravel())
+    zl = (tmp_path / "Z.dat").read_text().split("\n")
+    assert zl[0] == "Z 2 2 3" and zl[2].startswith("(") and "," in zl[2]
+    # the readers give the tensors back (the binary ones bit for bit)
+    back = lambda n, shape: np.fromfile(tmp_path / (n + ".elements")).reshape(
+        tuple(reversed(shape))).transpose(tuple(range(len(shape) - 1, -1, -1)))
+    assert np.array_equal(back("Ab", a.shape), a)
+    assert np.allclose(back("At", a.shape), a, rtol=1e-15, atol=0)
+    zb = np.fromfile(tmp_path / "Zb.elements").view(np.complex128).reshape(3, 2).T
+    zt = np.fromfile(tmp_path / "Zt.elements").view(np.complex128).reshape(3, 2).T
+    assert np.array_equal(zb, z) and np.allclose(zt, z, rtol=1e-15, atol=0)
