@@ -329,6 +329,13 @@ gbcc_status gbcc_coulomb_integrals(gbcc_ctx *ctx, int No, int Nv, int NG,
  * PPPH Vabci [Nv,Nv,Nv,No].  Any NULL output is skipped. */
 gbcc_status gbcc_coulomb_integrals_pp(gbcc_ctx *ctx, int No, int Nv, int NG,
                                       const double *gamma, double *Vabcd, double *Vabci);
+/* CoulombIntegralsFromVertex::calculateComplexIntegrals for the blocks the
+ * complex CCSD / (T) read (CoulombIntegralsFromVertex.cxx:767-809): complex
+ * gamma and outputs, interleaved (re, im).  Any NULL output is skipped. */
+gbcc_status gbcc_coulomb_integrals_complex(gbcc_ctx *ctx, int No, int Nv, int NG,
+                                           const double *gamma, double *Vabij,
+                                           double *Vaijb, double *Vijab, double *Vaibj,
+                                           double *Vijkl, double *Vijka, double *Vaijk);
 
 /* ------------------------------------------------------- building blocks */
 /* C[M,N] = alpha * op(A) op(B) + beta * C, column-major, device pointers,

@@ -64,16 +64,20 @@ def _flat(arr, shape, name):
 
 
 def _vertex(gamma, No, Nv):
-    """(real part, imaginary part or None) of the vertex Gamma[G, p, q].  The
-    imaginary part is handed to the library, which refuses it unless it is
-    zero (COMPLEX_UNSUPPORTED), as for the reference's complex CoulombVertex."""
+    """(column-major real vertex, its number of rows) for the real path.  The
+    reference's real CCSD and (T) read a complex vertex Gamma[G, p, q] as
+    Re.Re + Im.Im in every product of two vertex factors
+    (CcsdEnergyFromCoulombIntegrals.cxx:80-115,162-169; CcsdPerturbativeTriples
+    Complex.cxx:330-341), which is the real vertex [Re; Im] of 2 NG rows."""
     g = np.asarray(gamma)
     if g.ndim != 3 or g.shape[1:] != (No + Nv, No + Nv) or not g.shape[0]:
         raise ValueError("gamma has shape %s, expected (NG, %d, %d)"
                          % (g.shape, No + Nv, No + Nv))
     if np.iscomplexobj(g):
-        return fortran_flat(g.real), fortran_flat(g.imag)
-    return fortran_flat(g), None
+        if np.any(g.imag):
+            return fortran_flat(np.concatenate([g.real, g.imag], axis=0)), 2 * g.shape[0]
+        return fortran_flat(g.real), g.shape[0]
+    return fortran_flat(g), g.shape[0]
 
 
 _INTEGRAL_SHAPES = {"PPHH": "vvoo", "PHPH": "vovo", "HHHH": "oooo", "HHHP": "ooov",
@@ -93,16 +97,15 @@ class CcsdInput:
         eps_h, eps_p = _eigenenergies(eps_h, eps_p)
         No, Nv = eps_h.size, eps_p.size
         if gamma is None:
-            g, self.gamma_imag, NG = None, None, 0
+            g, NG = None, 0
         else:
-            g, self.gamma_imag = _vertex(gamma, No, Nv)
-            NG = np.shape(gamma)[0]
+            g, NG = _vertex(gamma, No, Nv)
         self.No, self.Nv, self.NG = No, Nv, NG
-        self._keep = [eps_h, eps_p, g, self.gamma_imag]
+        self._keep = [eps_h, eps_p, g]
         s = capi.CcsdIn()
         s.No, s.Nv, s.NG = self.No, self.Nv, self.NG
         s.eps_h, s.eps_p = ptr(eps_h), ptr(eps_p)
-        s.gamma, s.gamma_imag = ptr(g), ptr(self.gamma_imag)
+        s.gamma = ptr(g)
         ints = ints or {}
         for key, field in (("PPHH", "Vabij"), ("PHPH", "Vaibj"),
                            ("HHHH", "Vijkl"), ("HHHP", "Vijka"),
@@ -221,12 +224,12 @@ def triples(ctx, eps_h, eps_p, gamma, T1, T2, e_ccsd=0.0, Vabij=None,
     """Returns (E_(T), E_CCSD + E_(T))."""
     eps_h, eps_p = _eigenenergies(eps_h, eps_p)
     No, Nv = eps_h.size, eps_p.size
-    g, gi = _vertex(gamma, No, Nv)
+    g, NG = _vertex(gamma, No, Nv)
     s = capi.TriplesIn()
-    s.No, s.Nv, s.NG = No, Nv, np.shape(gamma)[0]
-    keep = [eps_h, eps_p, g, gi]
+    s.No, s.Nv, s.NG = No, Nv, NG
+    keep = [eps_h, eps_p, g]
     s.eps_h, s.eps_p = ptr(eps_h), ptr(eps_p)
-    s.gamma, s.gamma_imag = ptr(g), ptr(gi)
+    s.gamma = ptr(g)
     for name, arr, shape in (("T1", T1, (Nv, No)), ("T2", T2, (Nv, Nv, No, No)),
                              ("Vabij", Vabij, (Nv, Nv, No, No)),
                              ("Vijka", Vijka, (No, No, No, Nv))):
@@ -248,10 +251,7 @@ def coulomb_integrals(ctx, gamma, No):
     Nv = Np - No
     if not 0 < No < Np:
         raise ValueError("No must lie in 1..Np-1")
-    g, gi = _vertex(gamma, No, Nv)
-    if gi is not None and np.any(gi):
-        raise capi.GbccError(capi.COMPLEX_UNSUPPORTED,
-                             "the vertex has a non-zero imaginary part")
+    g, NG = _vertex(gamma, No, Nv)
     vabij = np.zeros(Nv * Nv * No * No)
     vaibj = np.zeros(Nv * Nv * No * No)
     vijkl = np.zeros(No ** 4)
@@ -274,10 +274,7 @@ def coulomb_integrals_pp(ctx, gamma, No):
     Nv = Np - No
     if not 0 < No < Np:
         raise ValueError("No must lie in 1..Np-1")
-    g, gi = _vertex(gamma, No, Nv)
-    if gi is not None and np.any(gi):
-        raise capi.GbccError(capi.COMPLEX_UNSUPPORTED,
-                             "the vertex has a non-zero imaginary part")
+    g, NG = _vertex(gamma, No, Nv)
     vabcd = np.zeros(Nv ** 4)
     vabci = np.zeros(Nv ** 3 * No)
     ctx.check(ctx.lib.gbcc_coulomb_integrals_pp(ctx.h, No, Nv, NG, ptr(g), ptr(vabcd),

@@ -15,6 +15,8 @@ void complex_residual(Context &ctx, const gbcc_ccsd_complex_in &in, const gbcc_c
                       int it, const double *T1, const double *T2, double *R1, double *R2);
 void complex_triples(Context &ctx, const gbcc_triples_complex_in &in, int precision,
                      double *e_total, double *e_t);
+void complex_integrals(Context &ctx, int No, int Nv, int NG, const double *gamma,
+                       double *const out[7]);
 }
 
 struct gbcc_ctx {
@@ -504,6 +506,19 @@ gbcc_status gbcc_coulomb_integrals_pp(gbcc_ctx *ctx, int No, int Nv, int NG,
     if (Vabcd) GBCC_CUDA(cudaMemcpyAsync(Vabcd, I->Vabcd.p(), 8 * v * v * v * v, cudaMemcpyDeviceToHost, st));
     if (Vabci) GBCC_CUDA(cudaMemcpyAsync(Vabci, I->Vabci.p(), 8 * v * v * v * o, cudaMemcpyDeviceToHost, st));
     GBCC_CUDA(cudaStreamSynchronize(st));
+    return GBCC_OK;
+  });
+}
+
+gbcc_status gbcc_coulomb_integrals_complex(gbcc_ctx *ctx, int No, int Nv, int NG,
+                                           const double *gamma, double *Vabij,
+                                           double *Vaijb, double *Vijab, double *Vaibj,
+                                           double *Vijkl, double *Vijka, double *Vaijk) {
+  if (!ctx || !gamma) return GBCC_BAD_ARG;
+  return guard(ctx, [&]() {
+    gbcc::require(No > 0 && Nv > 0 && NG > 0, "No, Nv, NG must be positive");
+    double *const out[7] = {Vabij, Vaijb, Vijab, Vaibj, Vijkl, Vijka, Vaijk};
+    gbcc::complex_integrals(ctx->c, No, Nv, NG, gamma, out);
     return GBCC_OK;
   });
 }

@@ -141,6 +141,25 @@ gbcc_status complex_solve(Context &ctx, const gbcc_ccsd_complex_in &in,
   return (r.converged || o.max_iterations == 0) ? GBCC_OK : GBCC_NOT_CONVERGED;
 }
 
+void complex_integrals(Context &ctx, int No, int Nv, int NG, const double *gamma,
+                       double *const out[7]) {
+  DeviceBackend rb{ctx, GBCC_PREC_FP64};
+  cx::Inputs<DeviceBackend> I;
+  cx::CBuf<DeviceBackend> T;
+  gbcc_ccsd_complex_in ci{};
+  ci.No = No; ci.Nv = Nv; ci.NG = NG;
+  std::vector<double> eh(No, 0.0), ep(Nv, 0.0);
+  ci.eps_h = eh.data();
+  ci.eps_p = ep.data();
+  ci.gamma = gamma;
+  cx::setup(rb, I, host_in(ci), T);
+  const cx::CBuf<DeviceBackend> *blocks[7] = {&I.Vabij, &I.Vaijb, &I.Vijab, &I.Vaibj,
+                                              &I.Vijkl, &I.Vijka, &I.Vaijk};
+  for (int q = 0; q < 7; ++q)
+    if (out[q]) rb.store_complex(blocks[q]->v(), out[q]);
+  ctx.check_device_errors();
+}
+
 void complex_triples(Context &ctx, const gbcc_triples_complex_in &in, int precision,
                      double *e_total, double *e_t) {
   require(in.T1 && in.T2, "CcsdSinglesAmplitudes and CcsdDoublesAmplitudes are required");

@@ -684,16 +684,114 @@ Sizes sizes_of(const Algorithm &a) {
   return s;
 }
 
+bool has_imaginary_part(const HTensor &t) {
+  if (!t.complex) return false;
+  for (double v : t.im)
+    if (v != 0.0) return true;
+  return false;
+}
+
+// interleaved (re, im) copy of a tensor, as CTF stores complex<double>
+std::vector<double> interleaved(const HTensor &t) {
+  std::vector<double> z(2 * (size_t)t.size(), 0.0);
+  for (int64_t e = 0; e < t.size(); ++e) {
+    z[2 * e] = t.re[e];
+    if (t.complex) z[2 * e + 1] = t.im[e];
+  }
+  return z;
+}
+
+// The real path reads a complex vertex as Re.Re + Im.Im in every product of
+// two vertex factors (CcsdEnergyFromCoulombIntegrals.cxx:80-115,162-169,...;
+// CcsdPerturbativeTriplesComplex.cxx:330-341): that is the real vertex with
+// the imaginary rows stacked under the real ones, [Re; Im] of 2 NG rows.
+const double *real_vertex(const HTensor &g, int *NG, std::vector<double> &buf) {
+  if (!has_imaginary_part(g)) return g.re.data();
+  const int64_t G = g.lens[0], pq = g.size() / G;
+  buf.resize(2 * (size_t)g.size());
+  for (int64_t e = 0; e < pq; ++e)
+    for (int64_t r = 0; r < G; ++r) {
+      buf[r + 2 * G * e] = g.re[r + G * e];
+      buf[G + r + 2 * G * e] = g.im[r + G * e];
+    }
+  *NG = (int)(2 * G);
+  return buf.data();
+}
+
+// the reference takes its complex branch when the PPHH integrals are complex
+// (ClusterSinglesDoublesAlgorithm.cxx:25-35, CcsdPerturbativeTriplesComplex.cxx:50-80)
+bool complex_integrals_given(const HTensor *pphh) { return pphh && pphh->complex; }
+
+std::shared_ptr<HTensor> complex_tensor(const std::vector<int64_t> &lens,
+                                        const std::vector<double> &z) {
+  auto t = std::make_shared<HTensor>();
+  t->lens = lens;
+  t->complex = true;
+  t->re.resize(t->size());
+  t->im.resize(t->size());
+  for (int64_t e = 0; e < t->size(); ++e) {
+    t->re[e] = z[2 * e];
+    t->im[e] = z[2 * e + 1];
+  }
+  return t;
+}
+
 // CoulombIntegralsFromVertex, real integrals (CoulombIntegralsFromVertex.cxx:203-558)
 struct CoulombIntegralsFromVertex : Algorithm {
-  void run() override {
-    if (integer("complex", 0)) throw StepError("complex integrals are not supported");
+  // complex: 1, calculateComplexIntegrals (CoulombIntegralsFromVertex.cxx:613-816)
+  void run_complex() {
     const Sizes s = sizes_of(*this);
-    const HTensor &g = tensor("CoulombVertex");
-    if (g.complex) {
-      for (double v : g.im)
-        if (v != 0.0) throw StepError("CoulombVertex has a non-zero imaginary part");
+    const std::vector<double> gz = interleaved(tensor("CoulombVertex"));
+    const int64_t o = s.No, v = s.Nv;
+    const std::pair<const char *, std::vector<int64_t>> blocks[7] = {
+        {"PPHHCoulombIntegrals", {v, v, o, o}}, {"PHHPCoulombIntegrals", {v, o, o, v}},
+        {"HHPPCoulombIntegrals", {o, o, v, v}}, {"PHPHCoulombIntegrals", {v, o, v, o}},
+        {"HHHHCoulombIntegrals", {o, o, o, o}}, {"HHHPCoulombIntegrals", {o, o, o, v}},
+        {"PHHHCoulombIntegrals", {v, o, o, o}}};
+    std::vector<std::vector<double>> bufs(7);
+    double *out[7];
+    for (int q = 0; q < 7; ++q) {
+      out[q] = nullptr;
+      if (!given(blocks[q].first)) continue;
+      size_t n = 2;
+      for (auto l : blocks[q].second) n *= (size_t)l;
+      bufs[q].assign(n, 0.0);
+      out[q] = bufs[q].data();
     }
+    check(gbcc_coulomb_integrals_complex(gpu(), s.No, s.Nv, s.NG, gz.data(), out[0], out[1],
+                                         out[2], out[3], out[4], out[5], out[6]),
+          "CoulombIntegralsFromVertex");
+    Json list = Json::array();
+    for (int q = 0; q < 7; ++q)
+      if (out[q]) {
+        set_tensor(blocks[q].first, complex_tensor(blocks[q].second, bufs[q]));
+        list.push(blocks[q].first);
+      }
+    for (auto &a : args)
+      if (a.first.find("CoulombIntegrals") != std::string::npos) {
+        bool ok = false;
+        for (auto &b : blocks) ok |= a.first == b.first;
+        if (!ok)
+          log(0, "CoulombIntegralsFromVertex",
+              "WARNING: " + a.first + " is not built (not used by the complex CCSD/(T))");
+      }
+    emit["NG"] = s.NG;
+    emit["No"] = s.No;
+    emit["Nv"] = s.Nv;
+    emit["complex"] = 1;
+    emit["integrals"] = list;
+  }
+
+  void run() override {
+    if (integer("antisymmetrize", 0))
+      throw StepError("antisymmetrized integrals are not supported");
+    if (integer("complex", 0)) {
+      run_complex();
+      return;
+    }
+    Sizes s = sizes_of(*this);
+    std::vector<double> stacked;
+    const double *gre = real_vertex(tensor("CoulombVertex"), &s.NG, stacked);
     const int64_t o = s.No, v = s.Nv;
     auto mk = [&](std::initializer_list<int64_t> l) {
       auto t = std::make_shared<HTensor>();
@@ -704,7 +802,7 @@ struct CoulombIntegralsFromVertex : Algorithm {
     std::shared_ptr<HTensor> pphh = mk({v, v, o, o}), phph = mk({v, o, v, o}),
                              hhhh = mk({o, o, o, o}), hhhp = mk({o, o, o, v}),
                              hhpp = mk({o, o, v, v});
-    check(gbcc_coulomb_integrals(gpu(), s.No, s.Nv, s.NG, g.re.data(),
+    check(gbcc_coulomb_integrals(gpu(), s.No, s.Nv, s.NG, gre,
                                  pphh->re.data(), phph->re.data(), hhhh->re.data(),
                                  hhhp->re.data(), hhpp->re.data()),
           "CoulombIntegralsFromVertex");
@@ -714,7 +812,7 @@ struct CoulombIntegralsFromVertex : Algorithm {
     if (given("PPPPCoulombIntegrals") || given("PPPHCoulombIntegrals")) {
       if (given("PPPPCoulombIntegrals")) pppp = mk({v, v, v, v});
       if (given("PPPHCoulombIntegrals")) ppph = mk({v, v, v, o});
-      check(gbcc_coulomb_integrals_pp(gpu(), s.No, s.Nv, s.NG, g.re.data(),
+      check(gbcc_coulomb_integrals_pp(gpu(), s.No, s.Nv, s.NG, gre,
                                       pppp ? pppp->re.data() : nullptr,
                                       ppph ? ppph->re.data() : nullptr),
             "CoulombIntegralsFromVertex");
@@ -751,37 +849,6 @@ int precision_of(const Algorithm &a) {
   if (p == "fp64") return GBCC_PREC_FP64;
   if (p == "emu" || p == "mixed") return GBCC_PREC_EMU;
   throw StepError("precision must be fp64 or emu");
-}
-
-bool has_imaginary_part(const HTensor &t) {
-  if (!t.complex) return false;
-  for (double v : t.im)
-    if (v != 0.0) return true;
-  return false;
-}
-
-// interleaved (re, im) copy of a tensor, as CTF stores complex<double>
-std::vector<double> interleaved(const HTensor &t) {
-  std::vector<double> z(2 * (size_t)t.size(), 0.0);
-  for (int64_t e = 0; e < t.size(); ++e) {
-    z[2 * e] = t.re[e];
-    if (t.complex) z[2 * e + 1] = t.im[e];
-  }
-  return z;
-}
-
-std::shared_ptr<HTensor> complex_tensor(const std::vector<int64_t> &lens,
-                                        const std::vector<double> &z) {
-  auto t = std::make_shared<HTensor>();
-  t->lens = lens;
-  t->complex = true;
-  t->re.resize(t->size());
-  t->im.resize(t->size());
-  for (int64_t e = 0; e < t->size(); ++e) {
-    t->re[e] = z[2 * e];
-    t->im[e] = z[2 * e + 1];
-  }
-  return t;
 }
 
 // CcsdEnergyFromCoulombIntegrals (ClusterSinglesDoublesAlgorithm.cxx:25-128)
@@ -876,10 +943,12 @@ struct CcsdEnergyFromCoulombIntegrals : Algorithm {
     emit["amplitudesConvergence"] = std::abs(o.amplitudes_convergence);
     emit["energyConvergence"] = std::abs(o.energy_convergence);
     emit["precision"] = o.precision == GBCC_PREC_FP64 ? "fp64" : "emu";
-    if (given("CoulombVertex") && has_imaginary_part(tensor("CoulombVertex"))) {
+    if (complex_integrals_given(given("PPHHCoulombIntegrals") ? &tensor("PPHHCoulombIntegrals")
+                                                              : nullptr)) {
       if (given("HPFockMatrix") || formulation() != 0)
         throw StepError("only CcsdEnergyFromCoulombIntegrals without HPFockMatrix has a "
                         "complex branch here");
+      if (!given("CoulombVertex")) throw StepError("CoulombVertex is required");
       run_complex(s, o);
       return;
     }
@@ -887,11 +956,8 @@ struct CcsdEnergyFromCoulombIntegrals : Algorithm {
     in.No = s.No; in.Nv = s.Nv; in.NG = s.NG;
     in.eps_h = tensor("HoleEigenEnergies").re.data();
     in.eps_p = tensor("ParticleEigenEnergies").re.data();
-    if (given("CoulombVertex")) {
-      const HTensor &g = tensor("CoulombVertex");
-      in.gamma = g.re.data();
-      in.gamma_imag = g.complex ? g.im.data() : nullptr;
-    }
+    std::vector<double> stacked;
+    if (given("CoulombVertex")) in.gamma = real_vertex(tensor("CoulombVertex"), &in.NG, stacked);
     const int64_t o1 = s.No, v1 = s.Nv;
     if (formulation() == 1) {
       in.Vabcd = tensor_or_null("PPPPCoulombIntegrals", {v1, v1, v1, v1});
@@ -966,9 +1032,8 @@ struct CcsdPerturbativeTriples : Algorithm {
     in.No = s.No; in.Nv = s.Nv; in.NG = s.NG;
     in.eps_h = tensor("HoleEigenEnergies").re.data();
     in.eps_p = tensor("ParticleEigenEnergies").re.data();
-    const HTensor &g = tensor("CoulombVertex");
-    in.gamma = g.re.data();
-    in.gamma_imag = g.complex ? g.im.data() : nullptr;
+    std::vector<double> stacked;
+    in.gamma = real_vertex(tensor("CoulombVertex"), &in.NG, stacked);
     const int64_t o1 = s.No, v1 = s.Nv;
     in.Vabij = tensor_or_null("PPHHCoulombIntegrals", {v1, v1, o1, o1});
     in.Vijka = tensor_or_null("HHHPCoulombIntegrals", {o1, o1, o1, v1});
@@ -1007,7 +1072,12 @@ struct CcsdPerturbativeTriplesComplex : Algorithm {
     const HTensor &t2 = tensor("CcsdDoublesAmplitudes", {v1, v1, o1, o1});
     const double e_ccsd = real("CcsdEnergy");
     double etot = 0, et[2] = {0, 0};
-    if (t1.complex || t2.complex) {
+    // Calculator<complex> for complex integrals (:50-80); without integrals,
+    // for complex amplitudes
+    const bool cplx = given("PPHHCoulombIntegrals")
+                          ? complex_integrals_given(&tensor("PPHHCoulombIntegrals"))
+                          : (t1.complex || t2.complex);
+    if (cplx) {
       const std::vector<double> gz = interleaved(g), t1z = interleaved(t1),
                                 t2z = interleaved(t2);
       gbcc_triples_complex_in in{};
@@ -1021,12 +1091,14 @@ struct CcsdPerturbativeTriplesComplex : Algorithm {
       check(gbcc_triples_complex(gpu(), &in, precision_of(*this), &etot, et),
             "CcsdPerturbativeTriplesComplex");
     } else {
+      if (has_imaginary_part(t1) || has_imaginary_part(t2))
+        throw StepError("complex amplitudes with real integrals");
       gbcc_triples_in in{};
       in.No = s.No; in.Nv = s.Nv; in.NG = s.NG;
       in.eps_h = tensor("HoleEigenEnergies").re.data();
       in.eps_p = tensor("ParticleEigenEnergies").re.data();
-      in.gamma = g.re.data();
-      in.gamma_imag = g.complex ? g.im.data() : nullptr;
+      std::vector<double> stacked;
+      in.gamma = real_vertex(g, &in.NG, stacked);  // Calculator<double> (:330-341)
       in.T1 = t1.re.data();
       in.T2 = t2.re.data();
       in.e_ccsd = e_ccsd;

@@ -74,12 +74,6 @@ class Server:
 
     def submit(self, system, triples=True, **opts):
         inp = CcsdInput(system.eps_h, system.eps_p, system.gamma)
-        if inp.gamma_imag is not None:
-            # requests carry the real vertex only; a zero imaginary part is dropped
-            if np.any(inp.gamma_imag):
-                raise capi.GbccError(capi.COMPLEX_UNSUPPORTED,
-                                     "the vertex has a non-zero imaginary part")
-            inp.s.gamma_imag = None
         o = make_opts(**opts)
         rid = C.c_int64()
         st = self.lib.gbcc_server_submit(self.h, C.byref(inp.s), C.byref(o),

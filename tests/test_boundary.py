@@ -316,36 +316,42 @@ def _write_complex_tensor(path, arr):
     z.view(np.float64).tofile(str(path)[:-5] + ".elements")
 
 
-def test_complex_vertex_takes_the_complex_branch(tmp_path):
-    # a vertex with a non-zero imaginary part selects the complex branch
-    # (ClusterSinglesDoublesAlgorithm.cxx:25-35); it has no noncanonical term
-    # and its amplitudes cannot enter the real (T)
+def test_complex_branch_is_chosen_by_the_integrals(tmp_path):
+    # as in the reference (ClusterSinglesDoublesAlgorithm.cxx:25-35), complex
+    # PPHH integrals select the complex branch; a complex vertex alone is read
+    # by the real path as Re.Re + Im.Im; the real (T) refuses complex amplitudes
     rng = np.random.default_rng(2)
     No, Nv, NG = 2, 3, 4
     _write_tensor(tmp_path / "Eh.yaml", rng.normal(size=No))
     _write_tensor(tmp_path / "Ep.yaml", rng.normal(size=Nv))
     _write_tensor(tmp_path / "F.yaml", rng.normal(size=(No, Nv)))
-    g = rng.normal(size=(NG, No + Nv, No + Nv)) + 1j * rng.normal(size=(NG, No + Nv, No + Nv))
-    _write_complex_tensor(tmp_path / "G.yaml", g)
-    t1 = rng.normal(size=(Nv, No)) + 1j * rng.normal(size=(Nv, No))
-    _write_complex_tensor(tmp_path / "T1.yaml", t1)
+    c = lambda *shape: rng.normal(size=shape) + 1j * rng.normal(size=shape)
+    _write_complex_tensor(tmp_path / "G.yaml", c(NG, No + Nv, No + Nv))
+    _write_complex_tensor(tmp_path / "V.yaml", c(Nv, Nv, No, No))
+    _write_complex_tensor(tmp_path / "T1.yaml", c(Nv, No))
     _write_tensor(tmp_path / "T2.yaml", rng.normal(size=(Nv, Nv, No, No)))
-    reads = _read_steps(["Eh", "Ep", "F", "G", "T1", "T2"])
+    reads = _read_steps(["Eh", "Ep", "F", "G", "V", "T1", "T2"])
     common = """    CoulombVertex: $G
     HoleEigenEnergies: $Eh
     ParticleEigenEnergies: $Ep
 """
-    r, out = _run(tmp_path, reads + "- name: CcsdEnergyFromCoulombIntegrals\n  in:\n" + common
-                  + "    HPFockMatrix: $F\n  out: {}\n")
+    reaches_library = lambda r, out: r.returncode == 0 or "GPU context: NO_DEVICE" in out["error"]
+    step = lambda name, extra: (reads + "- name: %s\n  in:\n" % name + common + extra
+                                + "  out: {}\n")
+    r, out = _run(tmp_path, step("CcsdEnergyFromCoulombIntegrals",
+                                 "    HPFockMatrix: $F\n    PPHHCoulombIntegrals: $V\n"))
     assert r.returncode == 1 and "without HPFockMatrix has a complex branch" in out["error"], out
-    r, out = _run(tmp_path, reads + "- name: CcsdPerturbativeTriples\n  in:\n" + common
-                  + "    CcsdEnergy: 0.0\n    CcsdSinglesAmplitudes: $T1\n"
-                  "    CcsdDoublesAmplitudes: $T2\n  out: {}\n")
+    r, out = _run(tmp_path, step("CcsdEnergyFromCoulombIntegrals", "    HPFockMatrix: $F\n"))
+    assert reaches_library(r, out), out
+    amps = "    CcsdEnergy: 0.0\n    CcsdSinglesAmplitudes: $T1\n    CcsdDoublesAmplitudes: $T2\n"
+    r, out = _run(tmp_path, step("CcsdPerturbativeTriples", amps))
     assert r.returncode == 1 and "CcsdPerturbativeTriplesComplex" in out["error"], out
-    r, out = _run(tmp_path, reads + "- name: CcsdPerturbativeTriplesComplex\n  in:\n" + common
-                  + "    CcsdEnergy: 0.0\n    CcsdSinglesAmplitudes: $T1\n"
-                  "    CcsdDoublesAmplitudes: $T2\n  out: {}\n")
-    assert r.returncode == 0 or "GPU context: NO_DEVICE" in out["error"], out
+    r, out = _run(tmp_path, step("CcsdPerturbativeTriplesComplex", amps))
+    assert reaches_library(r, out), out
+    r, out = _run(tmp_path, step("CoulombIntegralsFromVertex",
+                                 "    complex: 1\n  out:\n    PPHHCoulombIntegrals: $W\n")
+                  .replace("  out: {}\n", ""))
+    assert reaches_library(r, out), out
 
 
 def test_tensor_writer_and_reader_formats(tmp_path):

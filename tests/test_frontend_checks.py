@@ -1,9 +1,10 @@
 """Host-side argument checks of the Python front end (no GPU).
 
 The C ABI takes bare pointers and sizes, so the front end refuses arrays of
-the wrong shape before anything reaches the library, and hands a complex
-vertex's imaginary part to the library (which refuses it unless it is zero)
-instead of dropping it in a float64 cast.
+the wrong shape before anything reaches the library.  A complex vertex is
+not dropped to its real part in a float64 cast: the real path reads it as
+the reference's real CCSD does, Re.Re + Im.Im, i.e. as the real vertex with
+the imaginary rows stacked under the real ones.
 """
 import numpy as np
 import pytest
@@ -21,19 +22,40 @@ def system():
 
 def test_real_vertex_passes_no_imaginary_part(system):
     inp = gpu.CcsdInput(system.eps_h, system.eps_p, system.gamma)
-    assert inp.gamma_imag is None and not inp.s.gamma_imag
+    assert not inp.s.gamma_imag
     assert (inp.No, inp.Nv, inp.NG) == (No, Nv, NG)
+    zero_im = gpu.CcsdInput(system.eps_h, system.eps_p, system.gamma.astype(complex))
+    assert zero_im.NG == NG and np.array_equal(zero_im._keep[2], inp._keep[2])
 
 
-def test_complex_vertex_keeps_its_imaginary_part(system):
+def test_complex_vertex_is_stacked_for_the_real_path(system):
     g = system.gamma.astype(np.complex128)
     g[1, 2, 3] += 1e-3j
     inp = gpu.CcsdInput(system.eps_h, system.eps_p, g)
-    assert inp.s.gamma_imag
-    # column-major: element (G, p, q) sits at G + p*NG + q*NG*Np
+    assert not inp.s.gamma_imag and inp.NG == 2 * NG and inp.s.NG == 2 * NG
+    # column-major [Re; Im]: element (G', p, q) at G' + p*2NG + q*2NG*Np
     Np = No + Nv
-    assert inp.gamma_imag[1 + 2 * NG + 3 * NG * Np] == 1e-3
-    assert np.count_nonzero(inp.gamma_imag) == 1
+    flat = inp._keep[2]
+    assert flat[NG + 1 + 2 * (2 * NG) + 3 * (2 * NG) * Np] == 1e-3
+    assert flat[1 + 2 * (2 * NG) + 3 * (2 * NG) * Np] == g[1, 2, 3].real
+
+
+def test_stacked_vertex_is_the_reference_real_path():
+    # the oracle's real residual reads a complex vertex as Re.Re + Im.Im
+    # (CcsdEnergyFromCoulombIntegrals.cxx:80-115); so does the stacked vertex
+    from oracle.ccsd import residual
+    from oracle.coulomb import coulomb_integrals
+    s = make_system(No, Nv, NG, seed=7)
+    rng = np.random.default_rng(8)
+    g = s.gamma + 1j * 0.02 * rng.normal(size=s.gamma.shape)
+    stacked = np.concatenate([g.real, g.imag], axis=0)
+    T1 = rng.normal(0, 0.05, (Nv, No))
+    T2 = rng.normal(0, 0.05, (Nv, Nv, No, No))
+    T2 = 0.5 * (T2 + T2.transpose(1, 0, 3, 2))
+    a = residual(1, T1, T2, coulomb_integrals(g, No), g, slice_size=2)
+    b = residual(1, T1, T2, coulomb_integrals(stacked, No), stacked, slice_size=2)
+    for x, y in zip(a, b):
+        assert np.abs(x - y).max() < 1e-14 * np.abs(y).max()
 
 
 @pytest.mark.parametrize("key,shape", [("PPHH", (Nv, Nv, No, No + 1)),
