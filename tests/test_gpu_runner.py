@@ -119,5 +119,9 @@ def test_ueg_pipeline_through_runner(tmp_path):
     assert abs(e_ccsd - g["ccsd"]) < 2e-9
     assert abs(t["energy"]["triples"] - g["triples"]) < 1e-10
     assert abs(t["energy"]["value"] - (e_ccsd + t["energy"]["triples"])) < 1e-14
-    written = float(open(tmp_path / "CcsdPerturbativeTriplesEnergy.dat").read())
-    assert written == t["energy"]["value"]
+    # TensorWriter's text format (src/util/TensorIo.cxx:158-226): a name/order
+    # line, an index-order line, then the value with 16 significant digits
+    lines = open(tmp_path / "CcsdPerturbativeTriplesEnergy.dat").read().split("\n")
+    assert lines[0] == "CcsdPerturbativeTriplesEnergy 0"
+    written = float(lines[2])
+    assert abs(written - t["energy"]["value"]) <= 1e-15 * abs(t["energy"]["value"])
