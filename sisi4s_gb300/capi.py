@@ -119,6 +119,8 @@ _SIGS = {
                                          _dp]),
     "gbcc_coulomb_integrals_pp": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int,
                                             _dp, _dp, _dp]),
+    "gbcc_coulomb_integrals_complex": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int,
+                                                 _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp]),
     "gbcc_dgemm": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int64,
                              C.c_int64, C.c_int64, C.c_double, C.c_void_p,
                              C.c_int64, C.c_void_p, C.c_int64, C.c_double,

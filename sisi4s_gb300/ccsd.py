@@ -14,7 +14,7 @@ from .capi import fortran_flat, from_fortran_flat, ptr
 __all__ = ["make_opts", "CcsdInput", "ccsd_solve", "ccsd_residual", "Solver",
            "triples", "coulomb_integrals", "energy", "ComplexInput",
            "ccsd_solve_complex", "ccsd_residual_complex", "triples_complex",
-           "coulomb_integrals_pp"]
+           "coulomb_integrals_pp", "coulomb_integrals_complex"]
 
 
 def make_opts(mixer="LinearMixer", max_residua=4, mixing_ratio=1.0,
@@ -389,3 +389,21 @@ def triples_complex(ctx, eps_h, eps_p, gamma, T1, T2, e_ccsd=0.0, precision="fp6
     ctx.check(ctx.lib.gbcc_triples_complex(ctx.h, C.byref(s), p, C.byref(etot), ptr(et)))
     del keep
     return complex(et[0], et[1]), etot.value
+
+
+def coulomb_integrals_complex(ctx, gamma, No):
+    """Complex integrals of CoulombIntegralsFromVertex with complex: 1 (PPHH,
+    PHHP, HHPP, PHPH, HHHH, HHHP, PHHH) from a complex vertex."""
+    g = np.asarray(gamma)
+    NG, Np = g.shape[0], g.shape[1]
+    Nv = Np - No
+    if g.ndim != 3 or not 0 < No < Np:
+        raise ValueError("gamma must be [NG, Np, Np] with 0 < No < Np")
+    gf = complex_flat(g, (NG, Np, Np), "gamma")
+    shapes = {"PPHH": (Nv, Nv, No, No), "PHHP": (Nv, No, No, Nv), "HHPP": (No, No, Nv, Nv),
+              "PHPH": (Nv, No, Nv, No), "HHHH": (No, No, No, No), "HHHP": (No, No, No, Nv),
+              "PHHH": (Nv, No, No, No)}
+    bufs = {k: np.zeros(2 * int(np.prod(v))) for k, v in shapes.items()}
+    ctx.check(ctx.lib.gbcc_coulomb_integrals_complex(
+        ctx.h, No, Nv, NG, ptr(gf), *[ptr(bufs[k]) for k in shapes]))
+    return {k: from_complex_flat(bufs[k], shapes[k]) for k in shapes}

@@ -130,3 +130,11 @@ def test_complex_triples_matches_oracle(ctx, No, Nv, NG, precision):
         ctx.set_emulation(6, 1e7)
     tol = 1e-12 if precision == "fp64" else 1e-10
     assert abs(et - ref) < tol * abs(ref)
+
+
+def test_complex_integrals_match_oracle(ctx):
+    s, g, _, _ = _system(3, 7, 11, seed=2)
+    ref = coulomb_integrals_complex(g, 3)
+    got = gpu.coulomb_integrals_complex(ctx, g, 3)
+    for k in ("PPHH", "PHHP", "HHPP", "PHPH", "HHHH", "HHHP", "PHHH"):
+        assert _rel(got[k], ref[k]) < 1e-13, k
