@@ -945,9 +945,9 @@ struct CcsdEnergyFromCoulombIntegrals : Algorithm {
     emit["precision"] = o.precision == GBCC_PREC_FP64 ? "fp64" : "emu";
     if (complex_integrals_given(given("PPHHCoulombIntegrals") ? &tensor("PPHHCoulombIntegrals")
                                                               : nullptr)) {
-      if (given("HPFockMatrix") || formulation() != 0)
-        throw StepError("only CcsdEnergyFromCoulombIntegrals without HPFockMatrix has a "
-                        "complex branch here");
+      if (given("HPFockMatrix") || given("PairEnergy") || formulation() != 0)
+        throw StepError("only CcsdEnergyFromCoulombIntegrals without HPFockMatrix and "
+                        "PairEnergy has a complex branch here");
       if (!given("CoulombVertex")) throw StepError("CoulombVertex is required");
       run_complex(s, o);
       return;
