@@ -939,9 +939,11 @@ struct CcsdEnergyFromCoulombIntegrals : Algorithm {
     o.emu_slices = (int)integer("emulationDigits", 0);
     if (integer("unrestricted", 0) || integer("antisymmetrize", 0))
       throw StepError("unrestricted / antisymmetrized amplitudes are not supported");
-    emit["maxIterations"] = o.max_iterations;
+    emit["maxIterations"] = o.max_iterations;                     // :65-70
     emit["amplitudesConvergence"] = std::abs(o.amplitudes_convergence);
     emit["energyConvergence"] = std::abs(o.energy_convergence);
+    for (const char *k : {"distinguishable", "PPL", "OnlyPPL", "integralsSliceSize"})  // :72-87
+      if (given(k)) emit[k] = integer(k, 0);
     emit["precision"] = o.precision == GBCC_PREC_FP64 ? "fp64" : "emu";
     if (complex_integrals_given(given("PPHHCoulombIntegrals") ? &tensor("PPHHCoulombIntegrals")
                                                               : nullptr)) {
