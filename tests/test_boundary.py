@@ -421,3 +421,38 @@ def test_tensor_writer_and_reader_formats(tmp_path):
     zb = np.fromfile(tmp_path / "Zb.elements").view(np.complex128).reshape(3, 2).T
     zt = np.fromfile(tmp_path / "Zt.elements").view(np.complex128).reshape(3, 2).T
     assert np.array_equal(zb, z) and np.allclose(zt, z, rtol=1e-15, atol=0)
+
+
+def test_yaml_subset_of_the_step_files(tmp_path):
+    """The YAML the reference's step files use: comments (also after values,
+    not inside quotes), anchors and aliases, flow maps and sequences, quoted
+    scalars, enable / disable, and typed anonymous constants."""
+    r, out = _run(tmp_path, """
+# leading comment
+- name: Nop            # trailing comment
+  in:
+    text: "a # not a comment"
+    single: 'x: y'
+    int: 42
+    neg: -7
+    real: 2.5e-3
+    word: DiisMixer
+    anchored: &anc 17
+    alias: *anc
+- name: Nop
+  disable: true
+  in: { never: 1 }
+- name: Nop
+  enable: false
+- name: Nop
+  in: {flow: 3, other: "q,r"}
+  note: "kept"
+""")
+    assert r.returncode == 0, (r.stderr, out)
+    steps = out["steps"]
+    assert len(steps) == 2                      # the disabled steps are skipped
+    first = steps[0]["in"]
+    assert first["text"] == "a # not a comment" and first["single"] == "x: y"
+    assert first["int"] == 42 and first["neg"] == -7 and first["real"] == 2.5e-3
+    assert first["word"] == "DiisMixer" and first["alias"] == 17
+    assert steps[1]["in"] == {"flow": 3, "other": "q,r"} and steps[1]["note"] == "kept"
