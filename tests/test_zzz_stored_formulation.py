@@ -90,3 +90,77 @@ def test_particle_integrals_match_oracle(ctx):
     got = gpu.coulomb_integrals_pp(ctx, s.gamma, 3)
     for k in ("PPPP", "PPPH"):
         assert _rel(got[k], ref[k]) < 1e-13
+
+
+REFERENCE_STEPS = """
+- name: DefineHolesAndParticles
+  in: { fileName: "EigenEnergies.yaml" }
+  out: { HoleEigenEnergies: $HoleEigenEnergies, ParticleEigenEnergies: $ParticleEigenEnergies }
+- name: Read
+  in: { fileName: "CoulombVertex.yaml" }
+  out: { destination: $CoulombVertex }
+- name: CoulombIntegralsFromVertex
+  in:
+    CoulombVertex: $CoulombVertex
+    HoleEigenEnergies: $HoleEigenEnergies
+    ParticleEigenEnergies: $ParticleEigenEnergies
+  out:
+    PPHHCoulombIntegrals: $PPHHCoulombIntegrals
+    PHPHCoulombIntegrals: $PHPHCoulombIntegrals
+    HHHHCoulombIntegrals: $HHHHCoulombIntegrals
+    HHHPCoulombIntegrals: $HHHPCoulombIntegrals
+    PPPPCoulombIntegrals: $PPPPCoulombIntegrals
+    PPPHCoulombIntegrals: $PPPHCoulombIntegrals
+- name: CcsdEnergyFromCoulombIntegralsReference
+  in:
+    mixer: DiisMixer
+    maxResidua: 4
+    maxIterations: 20
+    energyConvergence: 1e-8
+    amplitudesConvergence: 1e-8
+    HoleEigenEnergies: $HoleEigenEnergies
+    ParticleEigenEnergies: $ParticleEigenEnergies
+    PPHHCoulombIntegrals: $PPHHCoulombIntegrals
+    PHPHCoulombIntegrals: $PHPHCoulombIntegrals
+    HHHHCoulombIntegrals: $HHHHCoulombIntegrals
+    HHHPCoulombIntegrals: $HHHPCoulombIntegrals
+    PPPPCoulombIntegrals: $PPPPCoulombIntegrals
+    PPPHCoulombIntegrals: $PPPHCoulombIntegrals
+  out:
+    CcsdEnergy: $CcsdEnergyReference
+"""
+
+
+def test_ueg_golden_through_the_stored_formulation_in_the_runner(tmp_path):
+    """The reference's UEG input runs CcsdEnergyFromCoulombIntegralsReference
+    on the integrals alone (no vertex); its CCSD energy is the golden one."""
+    import json
+    import os
+    import subprocess
+
+    from oracle.ueg import UEG_GOLDEN, ueg_real_vertex
+    from sisi4s_gb300 import build
+    build.build()
+    runner = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                          "sisi4s_gb300", "_lib", "sisi4s-gb300")
+    g = UEG_GOLDEN
+    gamma, eh, ep = ueg_real_vertex(g["No"], g["Nv"], g["rs"])
+    fermi = 0.5 * (eh.max() + ep.min())
+    (tmp_path / "EigenEnergies.yaml").write_text(
+        "metaData:\n  fermiEnergy: %.17g\n  energies: [%s]\n"
+        % (fermi, ", ".join("%.17g" % e for e in np.concatenate([eh, ep]))))
+    NG, Np, _ = gamma.shape
+    (tmp_path / "CoulombVertex.yaml").write_text(
+        "version: 100\ntype: Tensor\ndimensions:\n"
+        "  - length: %d\n    type: AuxiliaryField\n"
+        "  - length: %d\n    type: State\n  - length: %d\n    type: State\n"
+        "scalarType: Real64\nelements:\n  type: IeeeBinaryFile\nunit: 1.0\n" % (NG, Np, Np))
+    gamma.transpose(2, 1, 0).copy().tofile(tmp_path / "CoulombVertex.elements")
+    (tmp_path / "in.yaml").write_text(REFERENCE_STEPS)
+    r = subprocess.run([runner, "-i", "in.yaml", "-o", "out.yaml"], cwd=tmp_path,
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    out = json.loads((tmp_path / "out.yaml").read_text())
+    step = [s for s in out["steps"] if s["name"] == "CcsdEnergyFromCoulombIntegralsReference"][0]
+    assert step["convergenceReached"] == 1
+    assert abs(step["energy"]["value"] - g["ccsd"]) < 2e-9
