@@ -220,6 +220,8 @@ typedef struct {
   const double *gamma;        /* CoulombVertex, complex [NG,Np,Np] */
   const double *init_T1;      /* initialSinglesAmplitudes, complex [Nv,No] or NULL */
   const double *init_T2;      /* initialDoublesAmplitudes, complex [Nv,Nv,No,No] or NULL */
+  const double *fock_hp;      /* HPFockMatrix, complex [No,Nv] or NULL: adds the
+                                 noncanonical spins * T1_ai f_ia (:199-209) */
 } gbcc_ccsd_complex_in;
 
 typedef struct {

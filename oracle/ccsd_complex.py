@@ -210,18 +210,24 @@ def residual_complex(it, T1, T2, ints, gamma, distinguishable=0, ppl=1,
     return R1, R2
 
 
-def energy_complex(T1, T2, Vijab, spins=2.0):
+def energy_complex(T1, T2, Vijab, spins=2.0, fock_hp=None):
     """``getEnergy<complex>`` non-antisymmetrized branch
-    (ClusterSinglesDoublesAlgorithm.cxx:131-197) with the given HHPP integrals
+    (ClusterSinglesDoublesAlgorithm.cxx:131-209) with the given HHPP integrals
     (:137-139): direct = 0.5 s^2 (T2 + T1T1).Vijab["ijab"] (:170-172),
-    exchange = -0.5 s (T2 + T1T1).Vijab["ijba"] (:175-177).  Complex values;
-    the emitted energies are their real parts (:189-196)."""
+    exchange = -0.5 s (T2 + T1T1).Vijab["ijba"] (:175-177), and with
+    HPFockMatrix f[i,a] the noncanonical s T1["ai"] f["ia"] (:199-206).
+    Complex values; the emitted energies are their real parts (:189-196)."""
     d = 0.5 * spins * spins * _e("abij,ijab->", T2, Vijab)
     d = d + 0.5 * spins * spins * _e("ai,bj,ijab->", T1, T1, Vijab)
     x = (-0.5) * spins * _e("abij,ijba->", T2, Vijab)
     x = x + (-0.5) * spins * _e("ai,bj,ijba->", T1, T1, Vijab)
     d, x = complex(d), complex(x)
-    return {"direct": d, "exchange": x, "value": d + x}
+    out = {"direct": d, "exchange": x, "value": d + x}
+    if fock_hp is not None:
+        nc = complex(spins * _e("ai,ia->", T1, fock_hp))
+        out["noncanonical"] = nc
+        out["value"] = out["value"] + nc
+    return out
 
 
 def _fv_dot(x, y):
@@ -234,7 +240,7 @@ def ccsd_complex(eps_h, eps_p, ints, gamma, *, mixer="LinearMixer",
                  mixing_ratio=1.0, max_iterations=16, energy_convergence=1e-6,
                  amplitudes_convergence=1e-5, level_shift=0.0,
                  distinguishable=0, ppl=1, slice_size=-1, slice_factor=None,
-                 initial=None):
+                 initial=None, fock_hp=None):
     """``run<complex>`` (ClusterSinglesDoublesAlgorithm.cxx:37-128).  Returns
     dict(energy (real part, :32), energy_complex, T1, T2, iterations,
     converged, history)."""
@@ -279,7 +285,7 @@ def ccsd_complex(eps_h, eps_p, ints, gamma, *, mixer="LinearMixer",
                 dT[c] = dT[c] * r + last[1][c]
         last = (N, dT)
         amp = (N[0], N[1])
-        en = energy_complex(amp[0], amp[1], ints["HHPP"])         # :102
+        en = energy_complex(amp[0], amp[1], ints["HHPP"], fock_hp=fock_hp)  # :102
         e = en["value"]
         history.append({"iteration": it + 1, "energy": en})
         if (abs((e - prev) / e) < abs(energy_convergence)

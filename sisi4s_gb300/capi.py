@@ -50,7 +50,7 @@ class CcsdOut(C.Structure):
 class ComplexIn(C.Structure):
     _fields_ = [("No", C.c_int), ("Nv", C.c_int), ("NG", C.c_int),
                 ("eps_h", _dp), ("eps_p", _dp), ("gamma", _dp),
-                ("init_T1", _dp), ("init_T2", _dp)]
+                ("init_T1", _dp), ("init_T2", _dp), ("fock_hp", _dp)]
 
 
 class ComplexOut(C.Structure):

@@ -304,7 +304,7 @@ def from_complex_flat(flat, shape):
 class ComplexInput:
     """Owns the host buffers behind a ``gbcc_ccsd_complex_in``."""
 
-    def __init__(self, eps_h, eps_p, gamma, initial=None):
+    def __init__(self, eps_h, eps_p, gamma, initial=None, fock_hp=None):
         eps_h, eps_p = _eigenenergies(eps_h, eps_p)
         No, Nv = eps_h.size, eps_p.size
         g = np.asarray(gamma)
@@ -322,13 +322,17 @@ class ComplexInput:
             t2 = complex_flat(initial[1], (Nv, Nv, No, No), "initial T2")
             self._keep += [t1, t2]
             s.init_T1, s.init_T2 = ptr(t1), ptr(t2)
+        if fock_hp is not None:  # HPFockMatrix f[i, a]
+            f = complex_flat(fock_hp, (No, Nv), "fock_hp")
+            self._keep.append(f)
+            s.fock_hp = ptr(f)
         self.s = s
 
 
-def ccsd_solve_complex(ctx, eps_h, eps_p, gamma, initial=None, **opts):
+def ccsd_solve_complex(ctx, eps_h, eps_p, gamma, initial=None, fock_hp=None, **opts):
     """Complex CCSD (linear mixer).  Returns complex energies, the complex
     per-iteration history and the complex amplitudes."""
-    inp = ComplexInput(eps_h, eps_p, gamma, initial)
+    inp = ComplexInput(eps_h, eps_p, gamma, initial, fock_hp)
     o = make_opts(**opts)
     No, Nv = inp.No, inp.Nv
     out = capi.ComplexOut()

@@ -55,6 +55,7 @@ cx::HostIn host_in(const gbcc_ccsd_complex_in &in) {
   h.gamma = in.gamma;
   h.init_T1 = in.init_T1;
   h.init_T2 = in.init_T2;
+  h.fock_hp = in.fock_hp;
   return h;
 }
 

@@ -161,6 +161,9 @@ struct Inputs {
   CBuf<RB> Gij, Gia, Gai, Gab;     // vertex blocks [NG,No,No] ... [NG,Nv,Nv]
   // integrals of calculateComplexIntegrals (CoulombIntegralsFromVertex.cxx:767-809)
   CBuf<RB> Vabij, Vaijb, Vijab, Vaibj, Vijkl, Vijka, Vaijk;
+  // HPFockMatrix f[i,a] [No,Nv], if given
+  bool has_fock = false;
+  CBuf<RB> fock;
 };
 
 // Gamma planes [NG, Np, Np] -> blocks and integrals
@@ -390,7 +393,7 @@ void residual(RB &rb, const Inputs<RB> &I, int it, const ResidualOpts &o,
 
 // ------------------------------------------------------------------ energy
 struct Energy {
-  std::complex<double> direct, exchange, value;
+  std::complex<double> direct, exchange, noncanonical, value;
 };
 
 // getEnergy<complex> with Vijab (ClusterSinglesDoublesAlgorithm.cxx:131-189)
@@ -416,6 +419,10 @@ Energy energy(RB &rb, const Inputs<RB> &I, const CView &T1, const CView &T2) {
   e.direct = d;
   e.exchange = x;
   e.value = d + x;                                                  // :189
+  if (I.has_fock) {                                                 // :199-206
+    e.noncanonical = spins * dot(T1, "ai", I.fock.v(), "ia");
+    e.value += e.noncanonical;
+  }
   return e;
 }
 
@@ -597,6 +604,7 @@ struct HostIn {
   const double *gamma = nullptr;                    // CoulombVertex [NG,Np,Np]
   const double *init_T1 = nullptr;                  // [Nv,No] or null
   const double *init_T2 = nullptr;                  // [Nv,Nv,No,No] or null
+  const double *fock_hp = nullptr;                  // HPFockMatrix [No,Nv] or null
 };
 
 // Backend host transfers used here:
@@ -635,6 +643,11 @@ bool setup(RB &rb, Inputs<RB> &I, const HostIn &h, CBuf<RB> &T) {
   czero(rb, T.v());
   if (h.init_T1) rb.load_complex(h.init_T1, t1_of(T, L));
   if (h.init_T2) rb.load_complex(h.init_T2, t2_of(T, L));
+  if (h.fock_hp) {
+    I.has_fock = true;
+    I.fock = cbuf(rb, {h.No, h.Nv});
+    rb.load_complex(h.fock_hp, I.fock.v());
+  }
   return h.init_T2 != nullptr;                   // createAmplitudes: initial doubles given
 }
 

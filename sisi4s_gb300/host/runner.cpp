@@ -876,6 +876,11 @@ struct CcsdEnergyFromCoulombIntegrals : Algorithm {
       t2i = interleaved(tensor("initialDoublesAmplitudes", {v1, v1, o1, o1}));
       in.init_T2 = t2i.data();
     }
+    std::vector<double> fi;
+    if (given("HPFockMatrix")) {
+      fi = interleaved(tensor("HPFockMatrix", {o1, v1}));
+      in.fock_hp = fi.data();
+    }
     std::vector<double> t1(2 * v1 * o1), t2(2 * v1 * v1 * o1 * o1);
     std::vector<double> hist(2 * std::max(o.max_iterations, 1));
     gbcc_ccsd_complex_out out{};
@@ -947,9 +952,9 @@ struct CcsdEnergyFromCoulombIntegrals : Algorithm {
     emit["precision"] = o.precision == GBCC_PREC_FP64 ? "fp64" : "emu";
     if (complex_integrals_given(given("PPHHCoulombIntegrals") ? &tensor("PPHHCoulombIntegrals")
                                                               : nullptr)) {
-      if (given("HPFockMatrix") || given("PairEnergy") || formulation() != 0)
-        throw StepError("only CcsdEnergyFromCoulombIntegrals without HPFockMatrix and "
-                        "PairEnergy has a complex branch here");
+      if (given("PairEnergy") || formulation() != 0)
+        throw StepError("only CcsdEnergyFromCoulombIntegrals without PairEnergy has a "
+                        "complex branch here");
       if (!given("CoulombVertex")) throw StepError("CoulombVertex is required");
       run_complex(s, o);
       return;

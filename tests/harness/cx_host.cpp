@@ -274,11 +274,13 @@ struct HostBackend {
 std::string g_err;
 
 gbcc::cx::HostIn host_in(int No, int Nv, int NG, const double *eh, const double *ep,
-                         const double *gamma, const double *T1, const double *T2) {
+                         const double *gamma, const double *T1, const double *T2,
+                         const double *fock = nullptr) {
   gbcc::cx::HostIn h;
   h.No = No; h.Nv = Nv; h.NG = NG;
   h.eps_h = eh; h.eps_p = ep; h.gamma = gamma;
   h.init_T1 = T1; h.init_T2 = T2;
+  h.fock_hp = fock;
   return h;
 }
 
@@ -320,14 +322,14 @@ int cx_solve(int No, int Nv, int NG, const double *eh, const double *ep,
              const double *gamma, const double *T1in, const double *T2in, int max_it,
              double econv, double aconv, double shift, double ratio, int dist, int ppl,
              int slice, double *energy, int *iterations, int *converged,
-             double *history, double *T1, double *T2) {
+             double *history, double *T1, double *T2, const double *fock) {
   try {
     HostBackend rb;
     gbcc::cx::Inputs<HostBackend> I;
     gbcc::cx::CBuf<HostBackend> T;
     gbcc::cx::SolveOpts o;
     o.res.init_doubles =
-        gbcc::cx::setup(rb, I, host_in(No, Nv, NG, eh, ep, gamma, T1in, T2in), T);
+        gbcc::cx::setup(rb, I, host_in(No, Nv, NG, eh, ep, gamma, T1in, T2in, fock), T);
     o.res.distinguishable = dist != 0;
     o.res.ppl = ppl != 0;
     o.res.slice = slice > 0 ? slice : No;

@@ -340,6 +340,10 @@ def test_complex_branch_is_chosen_by_the_integrals(tmp_path):
                                 + "  out: {}\n")
     r, out = _run(tmp_path, step("CcsdEnergyFromCoulombIntegrals",
                                  "    HPFockMatrix: $F\n    PPHHCoulombIntegrals: $V\n"))
+    assert reaches_library(r, out), out    # the complex branch with its Fock term
+    r, out = _run(tmp_path, step("CcsdEnergyFromCoulombIntegrals",
+                                 "    PPHHCoulombIntegrals: $V\n  out:\n    PairEnergy: $P\n")
+                  .replace("  out: {}\n", ""))
     assert r.returncode == 1 and "has a complex branch here" in out["error"], out
     r, out = _run(tmp_path, step("CcsdEnergyFromCoulombIntegrals", "    HPFockMatrix: $F\n"))
     assert reaches_library(r, out), out

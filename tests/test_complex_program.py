@@ -98,11 +98,14 @@ def test_residual_program_matches_oracle(lib, it, init, dist, ppl, slice_size):
         assert not np.any(g1) and not np.any(o1)
 
 
-@pytest.mark.parametrize("ratio,shift", [(1.0, 0.0), (0.7, 0.0), (1.0, 0.3)])
-def test_solve_program_matches_oracle(lib, ratio, shift):
+@pytest.mark.parametrize("ratio,shift,fock", [(1.0, 0.0, False), (0.7, 0.0, False),
+                                              (1.0, 0.3, False), (1.0, 0.0, True)])
+def test_solve_program_matches_oracle(lib, ratio, shift, fock):
     No, Nv, NG = 3, 7, 11
     s, g, _, _ = _system(No, Nv, NG, seed=6)
     ci = coulomb_integrals_complex(g, No)
+    rng = np.random.default_rng(12)
+    f = (rng.normal(0, 0.05, (No, Nv)) + 1j * rng.normal(0, 0.05, (No, Nv))) if fock else None
     n = 40
     e = np.zeros(2)
     hist = np.zeros(2 * n)
@@ -112,11 +115,11 @@ def test_solve_program_matches_oracle(lib, ratio, shift):
     st = lib.cx_solve(No, Nv, NG, _p(s.eps_h), _p(s.eps_p), _p(_flat(g)), None, None, n,
                       C.c_double(1e-10), C.c_double(1e-8), C.c_double(shift),
                       C.c_double(ratio), 0, 1, 2, _p(e), C.byref(it), C.byref(conv),
-                      _p(hist), _p(t1), _p(t2))
+                      _p(hist), _p(t1), _p(t2), _p(None if f is None else _flat(f)))
     assert st == 0, lib.cx_last_error()
     ref = ccsd_complex(s.eps_h, s.eps_p, ci, g, mixing_ratio=ratio, level_shift=shift,
                        max_iterations=n, energy_convergence=1e-10,
-                       amplitudes_convergence=1e-8, slice_size=2)
+                       amplitudes_convergence=1e-8, slice_size=2, fock_hp=f)
     assert it.value == ref["iterations"] and bool(conv.value) == ref["converged"]
     h = hist[:2 * it.value].view(np.complex128)
     rh = np.array([x["energy"]["value"] for x in ref["history"]])

@@ -138,3 +138,17 @@ def test_complex_integrals_match_oracle(ctx):
     got = gpu.coulomb_integrals_complex(ctx, g, 3)
     for k in ("PPHH", "PHHP", "HHPP", "PHPH", "HHHH", "HHHP", "PHHH"):
         assert _rel(got[k], ref[k]) < 1e-13, k
+
+
+def test_complex_noncanonical_fock_term(ctx):
+    No, Nv, NG = 3, 8, 12
+    s, g, _, _ = _system(No, Nv, NG, seed=4)
+    ci = coulomb_integrals_complex(g, No)
+    rng = np.random.default_rng(12)
+    f = rng.normal(0, 0.05, (No, Nv)) + 1j * rng.normal(0, 0.05, (No, Nv))
+    kw = dict(max_iterations=6, energy_convergence=0.0, amplitudes_convergence=0.0,
+              slice_size=3)
+    ref = ccsd_complex(s.eps_h, s.eps_p, ci, g, fock_hp=f, **kw)
+    got = gpu.ccsd_solve_complex(ctx, s.eps_h, s.eps_p, g, fock_hp=f, **kw)
+    rh = np.array([h["energy"]["value"] for h in ref["history"]])
+    assert np.abs(got["history"] - rh).max() < 1e-12
