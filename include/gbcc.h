@@ -232,6 +232,7 @@ typedef struct {
   double *T1;                 /* optional caller buffer, complex [Nv,No] */
   double *T2;                 /* optional caller buffer, complex [Nv,Nv,No,No] */
   double *energy_history;     /* optional [2*max_iterations]: (re, im) per iteration */
+  double *pair_energy;        /* optional caller buffer, complex [No,No] (PairEnergy) */
 } gbcc_ccsd_complex_out;
 
 gbcc_status gbcc_ccsd_solve_complex(gbcc_ctx *ctx, const gbcc_ccsd_complex_in *in,

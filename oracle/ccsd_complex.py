@@ -32,8 +32,8 @@ build their vertices that way.
 import numpy as np
 
 __all__ = ["cvertex", "coulomb_integrals_complex", "residual_complex",
-           "energy_complex", "ccsd_complex", "triples_complex_loop",
-           "ComplexDiisUnsupported"]
+           "energy_complex", "pair_energy_complex", "ccsd_complex",
+           "triples_complex_loop", "ComplexDiisUnsupported"]
 
 
 class ComplexDiisUnsupported(NotImplementedError):
@@ -228,6 +228,16 @@ def energy_complex(T1, T2, Vijab, spins=2.0, fock_hp=None):
         out["noncanonical"] = nc
         out["value"] = out["value"] + nc
     return out
+
+
+def pair_energy_complex(T1, T2, Vijab):
+    """PairEnergy[i,j] of ``getEnergy<complex>`` (ClusterSinglesDoublesAlgorithm.cxx:227-232):
+    2 T2.V["ijab"] - T2.V["ijba"] + 2 T1T1.V["ijab"] - T1T1.V["ijba"]."""
+    p = 2.0 * _e("abij,ijab->ij", T2, Vijab)
+    p = p + (-1.0) * _e("abij,ijba->ij", T2, Vijab)
+    p = p + 2.0 * _e("ai,bj,ijab->ij", T1, T1, Vijab)
+    p = p + (-1.0) * _e("ai,bj,ijba->ij", T1, T1, Vijab)
+    return p
 
 
 def _fv_dot(x, y):

@@ -57,7 +57,7 @@ class ComplexOut(C.Structure):
     _fields_ = [("energy", C.c_double * 2), ("direct", C.c_double * 2),
                 ("exchange", C.c_double * 2), ("iterations", C.c_int),
                 ("converged", C.c_int), ("T1", _dp), ("T2", _dp),
-                ("energy_history", _dp)]
+                ("energy_history", _dp), ("pair_energy", _dp)]
 
 
 class TriplesComplexIn(C.Structure):

@@ -329,9 +329,11 @@ class ComplexInput:
         self.s = s
 
 
-def ccsd_solve_complex(ctx, eps_h, eps_p, gamma, initial=None, fock_hp=None, **opts):
+def ccsd_solve_complex(ctx, eps_h, eps_p, gamma, initial=None, fock_hp=None,
+                       pair_energy=False, **opts):
     """Complex CCSD (linear mixer).  Returns complex energies, the complex
-    per-iteration history and the complex amplitudes."""
+    per-iteration history, the complex amplitudes and, on request, the
+    complex pair energies."""
     inp = ComplexInput(eps_h, eps_p, gamma, initial, fock_hp)
     o = make_opts(**opts)
     No, Nv = inp.No, inp.Nv
@@ -339,7 +341,9 @@ def ccsd_solve_complex(ctx, eps_h, eps_p, gamma, initial=None, fock_hp=None, **o
     t1 = np.zeros(2 * Nv * No)
     t2 = np.zeros(2 * Nv * Nv * No * No)
     hist = np.zeros(2 * max(o.max_iterations, 1))
+    pe = np.zeros(2 * No * No) if pair_energy else None
     out.T1, out.T2, out.energy_history = ptr(t1), ptr(t2), ptr(hist)
+    out.pair_energy = ptr(pe)
     st = ctx.check(ctx.lib.gbcc_ccsd_solve_complex(ctx.h, C.byref(inp.s), C.byref(o),
                                                    C.byref(out)),
                    allow=(capi.OK, capi.NOT_CONVERGED))
@@ -350,7 +354,8 @@ def ccsd_solve_complex(ctx, eps_h, eps_p, gamma, initial=None, fock_hp=None, **o
             "iterations": n, "converged": bool(out.converged), "status": st,
             "history": hist[:2 * n].view(np.complex128).copy(),
             "T1": from_complex_flat(t1, (Nv, No)),
-            "T2": from_complex_flat(t2, (Nv, Nv, No, No))}
+            "T2": from_complex_flat(t2, (Nv, Nv, No, No)),
+            "pair_energy": None if pe is None else from_complex_flat(pe, (No, No))}
 
 
 def ccsd_residual_complex(ctx, it, T1, T2, eps_h, eps_p, gamma,

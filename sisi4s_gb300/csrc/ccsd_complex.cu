@@ -137,6 +137,13 @@ gbcc_status complex_solve(Context &ctx, const gbcc_ccsd_complex_in &in,
         out->energy_history[2 * q] = r.history[q].real();
         out->energy_history[2 * q + 1] = r.history[q].imag();
       }
+    if (out->pair_energy) {
+      const auto p = cx::pair_energy(rb, I, cx::t1_of(T, L), cx::t2_of(T, L));
+      for (size_t q = 0; q < p.size(); ++q) {
+        out->pair_energy[2 * q] = p[q].real();
+        out->pair_energy[2 * q + 1] = p[q].imag();
+      }
+    }
   }
   ctx.check_device_errors();
   return (r.converged || o.max_iterations == 0) ? GBCC_OK : GBCC_NOT_CONVERGED;

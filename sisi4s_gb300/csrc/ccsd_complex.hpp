@@ -83,6 +83,7 @@ struct Layout {
 //   linear_mix(next, nres, last, lres, r, sums)      LinearMixer::append
 //   vertex_block(dst, src, p0, np, q0, nq)            Gamma sub-block
 //   double scalar(x)                      read an order-0 tensor (synchronises)
+//   read(x, host)                         copy a tensor to host memory (synchronises)
 //   conj_over_denominator(re, im, eps_h, eps_p, i, j, k)
 //                                         z[a,b,c] = conj(z / D^{ijk}_{abc}) for
 //                                         the (T) denominator of the reference
@@ -424,6 +425,36 @@ Energy energy(RB &rb, const Inputs<RB> &I, const CView &T1, const CView &T2) {
     e.value += e.noncanonical;
   }
   return e;
+}
+
+// PairEnergy[i,j] (ClusterSinglesDoublesAlgorithm.cxx:227-232) for complex
+// amplitudes: 2 X.V["ijab"] - X.V["ijba"] with X = T2 + T1T1, per (i, j).
+// Both operands carry i and j, which the contraction engine does not take as
+// batch indices, so the full [i,j,k,l] products are formed (No^4 entries) and
+// their diagonal k = i, l = j is read on the host.  Returns p[i + No j].
+template <class RB>
+std::vector<std::complex<double>> pair_energy(RB &rb, const Inputs<RB> &I, const CView &T1,
+                                              const CView &T2) {
+  const int64_t No = I.No, Nv = I.Nv;
+  CBuf<RB> X = cbuf(rb, {Nv, Nv, No, No});
+  couter(rb, X.v(), T2, T1, 1.0);
+  CBuf<RB> P1 = cbuf(rb, {No, No, No, No}), P2 = cbuf(rb, {No, No, No, No});
+  ccontract(rb, 1.0, X.v(), "abij", false, I.Vijab.v(), "klab", false, 0.0, P1.v(), "ijkl");
+  ccontract(rb, 1.0, X.v(), "abij", false, I.Vijab.v(), "klba", false, 0.0, P2.v(), "ijkl");
+  const size_t n = (size_t)(No * No * No * No);
+  std::vector<double> h1r(n), h1i(n), h2r(n), h2i(n);
+  rb.read(P1.re.v, h1r.data());
+  rb.read(P1.im.v, h1i.data());
+  rb.read(P2.re.v, h2r.data());
+  rb.read(P2.im.v, h2i.data());
+  std::vector<std::complex<double>> p((size_t)(No * No));
+  for (int64_t j = 0; j < No; ++j)
+    for (int64_t i = 0; i < No; ++i) {
+      const size_t d = (size_t)(i + No * (j + No * (i + No * j)));
+      p[i + No * j] = 2.0 * std::complex<double>(h1r[d], h1i[d]) -
+                      std::complex<double>(h2r[d], h2i[d]);
+    }
+  return p;
 }
 
 // ------------------------------------------------------------------ driver

@@ -70,7 +70,7 @@ struct DeviceBackend {
     require(p0 + np <= src.lens[1] && q0 + nq <= src.lens[2], "vertex_block: out of range");
     gbcc::vertex_block(ctx, dst.p, src.p, src.lens[0], src.lens[1], p0, np, q0, nq);
   }
-  void read_sums(const double *dev, double *host, int n) {
+  void read_sums(const double *dev, double *host, int64_t n) {
     GBCC_CUDA(cudaMemcpyAsync(host, dev, sizeof(double) * n, cudaMemcpyDeviceToHost,
                               ctx.stream));
     ctx.check_device_errors();
@@ -102,6 +102,7 @@ struct DeviceBackend {
             "conj_over_denominator: bad shape");
     gbcc::conj_over_denominator(ctx, re.p, im.p, eh.p, ep.p, i0, i1, i2, Nv);
   }
+  void read(const cx::View &x, double *h) { read_sums(x.p, h, x.size()); }
   double scalar(const cx::View &x) {
     double h = 0.0;
     read_sums(x.p, &h, 1);

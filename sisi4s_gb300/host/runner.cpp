@@ -882,11 +882,12 @@ struct CcsdEnergyFromCoulombIntegrals : Algorithm {
       in.fock_hp = fi.data();
     }
     std::vector<double> t1(2 * v1 * o1), t2(2 * v1 * v1 * o1 * o1);
-    std::vector<double> hist(2 * std::max(o.max_iterations, 1));
+    std::vector<double> hist(2 * std::max(o.max_iterations, 1)), pe(2 * o1 * o1);
     gbcc_ccsd_complex_out out{};
     out.T1 = t1.data();
     out.T2 = t2.data();
     out.energy_history = hist.data();
+    out.pair_energy = given("PairEnergy") ? pe.data() : nullptr;
     emit["complex"] = 1;
     const gbcc_status st = gbcc_ccsd_solve_complex(gpu(), &in, &o, &out);
     check(st, "CcsdEnergyFromCoulombIntegrals (complex)", true);
@@ -916,6 +917,7 @@ struct CcsdEnergyFromCoulombIntegrals : Algorithm {
       set_tensor("CcsdSinglesAmplitudes", complex_tensor({v1, o1}, t1));
     if (given("CcsdDoublesAmplitudes"))
       set_tensor("CcsdDoublesAmplitudes", complex_tensor({v1, v1, o1, o1}, t2));
+    if (given("PairEnergy")) set_tensor("PairEnergy", complex_tensor({o1, o1}, pe));
   }
 
   void run() override {
@@ -952,9 +954,8 @@ struct CcsdEnergyFromCoulombIntegrals : Algorithm {
     emit["precision"] = o.precision == GBCC_PREC_FP64 ? "fp64" : "emu";
     if (complex_integrals_given(given("PPHHCoulombIntegrals") ? &tensor("PPHHCoulombIntegrals")
                                                               : nullptr)) {
-      if (given("PairEnergy") || formulation() != 0)
-        throw StepError("only CcsdEnergyFromCoulombIntegrals without PairEnergy has a "
-                        "complex branch here");
+      if (formulation() != 0)
+        throw StepError("only CcsdEnergyFromCoulombIntegrals has a complex branch here");
       if (!given("CoulombVertex")) throw StepError("CoulombVertex is required");
       run_complex(s, o);
       return;

@@ -235,6 +235,7 @@ struct HostBackend {
   }
 
   double scalar(const View &x) { return x.p[0]; }
+  void read(const View &x, double *h) { std::memcpy(h, x.p, sizeof(double) * x.size()); }
 
   // z = conj(z / D), D = (((e_i + e_j) + e_k) - e_a) - e_b) - e_c in the
   // reference's order (CcsdPerturbativeTriplesComplex.cxx:156-161, 224-229)
@@ -380,6 +381,27 @@ int st_residual(int No, int Nv, int it, int init_doubles, int only_ppl, const do
     opts.only_ppl = only_ppl != 0;
     gbcc::st::residual(rb, I, it, opts, v(T1, {n, o}), v(T2, {n, n, o, o}), v(R1, {n, o}),
                        v(R2, {n, n, o, o}));
+    return 0;
+  } catch (const std::exception &e) {
+    g_err = e.what();
+    return 1;
+  }
+}
+
+// complex pair energies [No,No] (interleaved) of the given complex amplitudes
+int cx_pair_energy(int No, int Nv, int NG, const double *eh, const double *ep,
+                   const double *gamma, const double *T1, const double *T2, double *pe) {
+  try {
+    HostBackend rb;
+    gbcc::cx::Inputs<HostBackend> I;
+    gbcc::cx::CBuf<HostBackend> T;
+    gbcc::cx::setup(rb, I, host_in(No, Nv, NG, eh, ep, gamma, T1, T2), T);
+    const gbcc::cx::Layout L(Nv, No);
+    const auto p = gbcc::cx::pair_energy(rb, I, gbcc::cx::t1_of(T, L), gbcc::cx::t2_of(T, L));
+    for (size_t q = 0; q < p.size(); ++q) {
+      pe[2 * q] = p[q].real();
+      pe[2 * q + 1] = p[q].imag();
+    }
     return 0;
   } catch (const std::exception &e) {
     g_err = e.what();

@@ -344,6 +344,9 @@ def test_complex_branch_is_chosen_by_the_integrals(tmp_path):
     r, out = _run(tmp_path, step("CcsdEnergyFromCoulombIntegrals",
                                  "    PPHHCoulombIntegrals: $V\n  out:\n    PairEnergy: $P\n")
                   .replace("  out: {}\n", ""))
+    assert reaches_library(r, out), out
+    r, out = _run(tmp_path, step("CcsdEnergyFromCoulombIntegralsReference",
+                                 "    PPHHCoulombIntegrals: $V\n"))
     assert r.returncode == 1 and "has a complex branch here" in out["error"], out
     r, out = _run(tmp_path, step("CcsdEnergyFromCoulombIntegrals", "    HPFockMatrix: $F\n"))
     assert reaches_library(r, out), out

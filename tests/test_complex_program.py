@@ -17,8 +17,8 @@ import subprocess
 import numpy as np
 import pytest
 
-from oracle.ccsd_complex import (ccsd_complex, coulomb_integrals_complex, residual_complex,
-                                 triples_complex_loop)
+from oracle.ccsd_complex import (ccsd_complex, coulomb_integrals_complex, pair_energy_complex,
+                                 residual_complex, triples_complex_loop)
 from sisi4s_gb300.inputs import make_system
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -171,3 +171,16 @@ def test_stored_residual_program_matches_oracle(lib, it, init, only_ppl):
         assert np.abs(g1 - o1).max() < 1e-13 * np.abs(o1).max()
     else:
         assert not np.any(g1)
+
+
+def test_pair_energy_program_matches_oracle(lib):
+    No, Nv, NG = 3, 6, 9
+    s, g, T1, T2 = _system(No, Nv, NG, seed=3)
+    ci = coulomb_integrals_complex(g, No)
+    ref = pair_energy_complex(T1, T2, ci["HHPP"])
+    pe = np.zeros(2 * No * No)
+    st = lib.cx_pair_energy(No, Nv, NG, _p(s.eps_h), _p(s.eps_p), _p(_flat(g)), _p(_flat(T1)),
+                            _p(_flat(T2)), _p(pe))
+    assert st == 0, lib.cx_last_error()
+    got = _unflat(pe, (No, No))
+    assert np.abs(got - ref).max() < 1e-13 * np.abs(ref).max()

@@ -10,8 +10,8 @@ import ctypes as C
 import numpy as np
 import pytest
 
-from oracle.ccsd_complex import (ccsd_complex, coulomb_integrals_complex, residual_complex,
-                                 triples_complex_loop)
+from oracle.ccsd_complex import (ccsd_complex, coulomb_integrals_complex, pair_energy_complex,
+                                 residual_complex, triples_complex_loop)
 from oracle.ueg import UEG_GOLDEN, ueg_planewave
 from sisi4s_gb300 import capi
 from sisi4s_gb300 import ccsd as gpu
@@ -152,3 +152,15 @@ def test_complex_noncanonical_fock_term(ctx):
     got = gpu.ccsd_solve_complex(ctx, s.eps_h, s.eps_p, g, fock_hp=f, **kw)
     rh = np.array([h["energy"]["value"] for h in ref["history"]])
     assert np.abs(got["history"] - rh).max() < 1e-12
+
+
+def test_complex_pair_energies(ctx):
+    No, Nv, NG = 3, 8, 12
+    s, g, _, _ = _system(No, Nv, NG, seed=5)
+    ci = coulomb_integrals_complex(g, No)
+    r = gpu.ccsd_solve_complex(ctx, s.eps_h, s.eps_p, g, pair_energy=True, max_iterations=4,
+                               energy_convergence=0.0, amplitudes_convergence=0.0)
+    ref = pair_energy_complex(r["T1"], r["T2"], ci["HHPP"])
+    assert np.abs(r["pair_energy"] - ref).max() < 1e-12 * np.abs(ref).max()
+    # the pair energies sum to the correlation energy (:189, :227-232)
+    assert abs(r["pair_energy"].sum() - r["energy"]) < 1e-12 * abs(r["energy"])
