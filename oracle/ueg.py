@@ -29,8 +29,9 @@ __all__ = ["eval_madelung", "ueg_planewave", "ueg_real_vertex", "UEG_GOLDEN"]
 
 #: golden energies of the reference integration test
 #: integration-tests/tests/cc4s/ueg/rs1.0-7occ-26virt/cc4s.correct.out.yaml:
-#: secondOrder :148, CCSD correlation :153 (DIIS, maxResidua 4, energy and
-#: amplitude convergence 1e-8, maxIterations 20, :132-146), (T) :169.
+#: CCSD correlation :153 (direct :154, exchange :155), its secondOrder :156
+#: (DIIS, maxResidua 4, energy and amplitude convergence 1e-8, maxIterations
+#: 20, :134-147), (T) :169.
 UEG_GOLDEN = {
     "No": 7, "Nv": 26, "rs": 1.0,
     "mp2": -0.36143028565969504,

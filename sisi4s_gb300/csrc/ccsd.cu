@@ -124,6 +124,8 @@ std::unique_ptr<CcsdInputs> upload_inputs(Context &ctx, const gbcc_ccsd_in &in,
     for (int64_t i = 0; i < No; ++i)
       for (int64_t a = 0; a < Nv; ++a) fai[a + Nv * i] = in.fock_hp[i + No * a];
     up(p->fock_ai, fai.data(), {Nv, No});
+    // fai is freed at the end of this block: the copy must have read it
+    GBCC_CUDA(cudaStreamSynchronize(ctx.stream));
   }
   return p;
 }

@@ -127,6 +127,33 @@ def test_solve_program_matches_oracle(lib, ratio, shift, fock):
     assert _rel(_unflat(t2, (Nv, Nv, No, No)), ref["T2"]) < 1e-12
 
 
+def test_solve_and_triples_programs_match_the_committed_fixture(lib):
+    """The complex trajectory and (T) of tests/golden/oracle_cases.json."""
+    from tests.golden import cases
+    f = cases.load(cases.ORACLE_FILE)["complex"]
+    o = cases.COMPLEX_SOLVE
+    s, g = cases.complex_system(**cases.COMPLEX)
+    No, Nv, NG = s.No, s.Nv, s.NG
+    n = o["max_iterations"]
+    e, hist = np.zeros(2), np.zeros(2 * n)
+    it, conv = C.c_int(), C.c_int()
+    t1, t2 = np.zeros(2 * Nv * No), np.zeros(2 * Nv * Nv * No * No)
+    st = lib.cx_solve(No, Nv, NG, _p(s.eps_h), _p(s.eps_p), _p(_flat(g)), None, None, n,
+                      C.c_double(o["energy_convergence"]),
+                      C.c_double(o["amplitudes_convergence"]), C.c_double(0.0),
+                      C.c_double(o["mixing_ratio"]), 0, 1, o["slice_size"], _p(e),
+                      C.byref(it), C.byref(conv), _p(hist), _p(t1), _p(t2), None)
+    assert st == 0, lib.cx_last_error()
+    want = cases.complex_list(f["history"])
+    assert it.value == want.size
+    assert np.abs(hist.view(np.complex128) - want).max() < 1e-13
+    et = np.zeros(2)
+    st = lib.cx_triples(No, Nv, NG, _p(s.eps_h), _p(s.eps_p), _p(_flat(g)), _p(t1), _p(t2),
+                        _p(et))
+    assert st == 0, lib.cx_last_error()
+    assert abs(complex(et[0], et[1]) - cases.complex_list([f["triples"]])[0]) < 1e-13
+
+
 def test_program_reports_missing_inputs(lib):
     st = lib.cx_residual(0, 4, 5, None, None, None, 1, 1, 0, 1, -1, None, None, None, None)
     assert st == 1 and b"required" in lib.cx_last_error()

@@ -21,7 +21,7 @@ def ueg():
 
 def test_ueg_mp2_matches_reference_golden(ueg):
     gamma, eh, ep, ints = ueg
-    # cc4s.correct.out.yaml:148 secondOrder
+    # cc4s.correct.out.yaml:156 secondOrder
     assert abs(mp2_energy(eh, ep, ints["PPHH"]) - UEG_GOLDEN["mp2"]) < 1e-12
 
 
@@ -33,6 +33,13 @@ def test_ueg_ccsd_and_triples_match_reference_golden(ueg):
     # value carries that convergence error, the reference checks 1e-7
     # (integration-tests/testis.py:256)
     assert abs(r["energy"] - UEG_GOLDEN["ccsd"]) < 2e-9
+    # the direct and exchange parts (cc4s.correct.out.yaml:154-155), from the
+    # committed fixture of that record
+    from tests.golden import cases
+    rec = cases.load(cases.UEG_FILE)["ccsd"]
+    last = r["history"][-1]["energy"]
+    assert abs(last["direct"] - float(rec["direct"]["value"])) < 2e-9
+    assert abs(last["exchange"] - float(rec["exchange"]["value"])) < 2e-9
     et = triples_loop(eh, ep, r["T1"], r["T2"], ints["PPHH"], ints["HHHP"],
                       gamma)
     assert abs(et - UEG_GOLDEN["triples"]) < 1e-10
