@@ -10,6 +10,13 @@ if ROOT not in sys.path:
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300)")
+    # GBCC_SIM_LIB: run the tests against the host simulation of the device
+    # side (tests/harness/sim) instead of the CUDA library; set only by
+    # tests/test_sim_glue.py for its child pytest runs
+    sim = os.environ.get("GBCC_SIM_LIB")
+    if sim:
+        from sisi4s_gb300 import capi
+        capi.load(sim)
 
 
 @pytest.fixture(scope="session")

@@ -1,0 +1,81 @@
+"""Builds libgbcc_sim.so: libgbcc's host sources (the files under
+``sisi4s_gb300/csrc`` without device code) compiled by the host C++ compiler
+and linked against the host simulation of its device side (``sim.hpp``).
+Test infrastructure only.
+
+    python tests/harness/sim/build_sim.py
+"""
+import os
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(HERE)))
+CSRC = os.path.join(ROOT, "sisi4s_gb300", "csrc")
+OUT = os.path.join(os.path.dirname(HERE), "_build", "sim")
+LIB = os.path.join(OUT, "libgbcc_sim.so")
+LD_DIR = os.path.join(OUT, "ld")
+
+#: the library's translation units that hold host code only
+HOST_UNITS = ["capi.cu", "ccsd.cu", "ccsd_complex.cu", "ccsd_stored.cu", "contract.cu",
+              "serve.cu"]
+SIM_UNITS = ["sim_runtime.cpp", "sim_kernels.cpp"]
+
+
+def cuda_include():
+    for d in (os.environ.get("CUDA_HOME"), "/usr/local/cuda"):
+        if d and os.path.exists(os.path.join(d, "include", "cuda_runtime.h")):
+            return os.path.join(d, "include")
+    raise RuntimeError("cuda_runtime.h not found")
+
+
+def _deps():
+    hdrs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".hpp", ".h"))]
+    hdrs += [os.path.join(HERE, "sim.hpp"), os.path.join(ROOT, "include", "gbcc.h")]
+    return hdrs
+
+
+def _stale(target, deps):
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def build():
+    os.makedirs(OUT, exist_ok=True)
+    flags = ["g++", "-std=c++17", "-O2", "-fPIC", "-pthread", "-Wall",
+             "-I", cuda_include(), "-I", CSRC, "-I", HERE]
+    hdrs = _deps()
+    jobs, objs = [], []
+    for f in HOST_UNITS + SIM_UNITS:
+        src = os.path.join(CSRC if f in HOST_UNITS else HERE, f)
+        obj = os.path.join(OUT, f.rsplit(".", 1)[0] + ".o")
+        objs.append(obj)
+        if _stale(obj, [src] + hdrs):
+            lang = ["-x", "c++"] if f.endswith(".cu") else []
+            jobs.append(flags + lang + ["-c", src, "-o", obj])
+
+    def run(cmd):
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("sim build failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
+
+    with ThreadPoolExecutor(max_workers=min(len(jobs) or 1, os.cpu_count() or 4)) as ex:
+        list(ex.map(run, jobs))
+    if jobs or not os.path.exists(LIB):
+        run(["g++", "-shared", "-pthread", "-Wl,--no-undefined", "-o", LIB] + objs)
+    # a directory whose libgbcc.so is the simulation: with it first on
+    # LD_LIBRARY_PATH the step runner (which links libgbcc.so with a RUNPATH)
+    # runs on the simulation too
+    link = os.path.join(LD_DIR, "libgbcc.so")
+    os.makedirs(LD_DIR, exist_ok=True)
+    if not os.path.islink(link):
+        os.symlink(os.path.relpath(LIB, LD_DIR), link)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build())
+    sys.exit(0)

@@ -1,0 +1,71 @@
+"""GPU test files run on the CPU against the host simulation of the device
+side (``tests/harness/sim``).
+
+libgbcc's host code is compiled for the host and linked against host models
+of the kernel launchers and a stand-in CUDA runtime that emulates stream
+capture. That code is:
+- the C ABI;
+- the CCSD driver with its CUDA-graph capture;
+- the contraction engine;
+- the complex and stored programs on the CUDA backend;
+- serving.
+
+The step runner, which links libgbcc.so, picks up the simulation through
+LD_LIBRARY_PATH.
+
+What this checks is the host code and every call it makes into the device
+routines: argument order, shapes, buffer lifetimes, and what may run while a
+stream is captured. The kernels themselves are checked on the GPU. The
+calibration set consists of GPU tests that have already passed on a GB300.
+Running it on the simulation shows that the models follow the kernels. The
+runs below leave out tests that need torch device memory, bounded device
+waits or GPU-sized workloads.
+"""
+import os
+import subprocess
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+CALIBRATION = ["tests/test_gpu_parity.py", "-k",
+               "not dgemm_all and not matrix_vector and not c1_config"]
+RUNNER = ["tests/test_gpu_runner.py"]
+NEW_PATHS = ["tests/test_zzz_energy_terms.py", "tests/test_zzz_complex_branch.py",
+             "tests/test_zzz_stored_formulation.py", "tests/test_zzz_golden_fixtures.py"]
+
+
+@pytest.fixture(scope="module")
+def sim_env():
+    sys.path.insert(0, os.path.join(ROOT, "tests", "harness", "sim"))
+    try:
+        import build_sim
+    finally:
+        sys.path.pop(0)
+    lib = build_sim.build()
+    from sisi4s_gb300 import build
+    build.build()  # the step runner binary
+    env = dict(os.environ)
+    env["GBCC_SIM_LIB"] = lib
+    env["LD_LIBRARY_PATH"] = build_sim.LD_DIR + (
+        ":" + env["LD_LIBRARY_PATH"] if env.get("LD_LIBRARY_PATH") else "")
+    return env
+
+
+def _pytest(env, args):
+    r = subprocess.run([sys.executable, "-m", "pytest", "-m", "gpu", "-q", "-p",
+                        "no:cacheprovider"] + args, cwd=ROOT, env=env,
+                       capture_output=True, text=True, timeout=1200)
+    assert r.returncode == 0, r.stdout[-6000:] + r.stderr[-2000:]
+    return r.stdout
+
+
+def test_calibration_set_passes_on_the_simulation(sim_env):
+    out = _pytest(sim_env, CALIBRATION + RUNNER)
+    assert " passed" in out and "failed" not in out
+
+
+def test_gpu_tests_not_yet_run_on_a_gpu_pass_on_the_simulation(sim_env):
+    out = _pytest(sim_env, NEW_PATHS)
+    assert " passed" in out and "failed" not in out
