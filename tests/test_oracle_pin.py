@@ -45,6 +45,18 @@ def test_ueg_ccsd_and_triples_match_reference_golden(ueg):
     assert abs(et - UEG_GOLDEN["triples"]) < 1e-10
 
 
+@pytest.mark.parametrize("No,Nv,NG", [(1, 6, 10), (3, 1, 7)])
+def test_triples_vanish_with_one_hole_or_one_particle(No, Nv, NG):
+    """With one hole all six images of the triple coincide, with one particle
+    all (a, b, c) are equal; the spin/Fermi factors then sum to zero
+    (8 - 3*4 + 2*2) and E_(T) is round-off (CcsdPerturbativeTriples.cxx:143)."""
+    s = make_system(No, Nv, NG, seed=7)
+    ints = coulomb_integrals(s.gamma, No)
+    r = ccsd(s.eps_h, s.eps_p, ints, s.gamma, max_iterations=6)
+    et = triples_loop(s.eps_h, s.eps_p, r["T1"], r["T2"], ints["PPHH"], ints["HHHP"], s.gamma)
+    assert abs(et) < 1e-14 * abs(r["energy"])
+
+
 def test_triples_loop_equals_dense_form(ueg):
     gamma, eh, ep, ints = ueg
     s = make_system(4, 10, 24, seed=3)

@@ -78,6 +78,28 @@ def test_complex_iterations_match_oracle(ctx, ratio):
     assert _rel(got["T2"], ref["T2"]) < 1e-9
 
 
+@pytest.mark.parametrize("No,Nv,NG,slice_size", [(1, 2, 1, 1), (1, 3, 2, -1), (2, 1, 3, -1)])
+def test_complex_minimal_sizes(ctx, No, Nv, NG, slice_size):
+    """One hole or one particle, one vertex row: single-element ladder slices,
+    and (T) where all six images of a triple coincide (one hole) or all
+    particle indices are equal (one particle).  There the spin/Fermi factors
+    sum to zero (8 - 3*4 + 2*2), so E_(T) vanishes up to round-off."""
+    s, g, _, _ = _system(No, Nv, NG, seed=3)
+    ci = coulomb_integrals_complex(g, No)
+    kw = dict(max_iterations=5, energy_convergence=0.0, amplitudes_convergence=0.0,
+              slice_size=slice_size)
+    ref = ccsd_complex(s.eps_h, s.eps_p, ci, g, **kw)
+    got = gpu.ccsd_solve_complex(ctx, s.eps_h, s.eps_p, g, **kw)
+    rh = np.array([h["energy"]["value"] for h in ref["history"]])
+    assert got["iterations"] == rh.size
+    assert np.abs(got["history"] - rh).max() < 1e-12 * np.abs(rh).max()
+    et, _ = gpu.triples_complex(ctx, s.eps_h, s.eps_p, g, got["T1"], got["T2"])
+    ref_t = triples_complex_loop(s.eps_h, s.eps_p, ref["T1"], ref["T2"], ci["PPHH"],
+                                 ci["PHHH"], g)
+    scale = abs(ref["energy_complex"])
+    assert abs(ref_t) < 1e-14 * scale and abs(et) < 1e-14 * scale
+
+
 def test_real_vertex_through_the_complex_branch_equals_the_real_branch(ctx):
     s = make_system(4, 12, 30, seed=5)
     kw = dict(max_iterations=6, energy_convergence=0.0, amplitudes_convergence=0.0)
