@@ -69,3 +69,12 @@ def test_calibration_set_passes_on_the_simulation(sim_env):
 def test_gpu_tests_not_yet_run_on_a_gpu_pass_on_the_simulation(sim_env):
     out = _pytest(sim_env, NEW_PATHS)
     assert " passed" in out and "failed" not in out
+
+
+def test_smoke_entry_runs_on_the_simulation(sim_env):
+    code = ("import os; from sisi4s_gb300 import capi; capi.load(os.environ['GBCC_SIM_LIB']); "
+            "import __graft_entry__ as g; g.smoke()")
+    r = subprocess.run([sys.executable, "-c", code], cwd=ROOT, env=sim_env,
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "smoke ok" in r.stdout
