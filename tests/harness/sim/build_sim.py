@@ -76,6 +76,39 @@ def build():
     return LIB
 
 
+def build_serve_race():
+    """serve_race.cpp linked against a ThreadSanitizer build of the library's
+    host code and of the simulation; returns the binary's path."""
+    out = os.path.join(OUT, "tsan")
+    os.makedirs(out, exist_ok=True)
+    exe = os.path.join(out, "serve_race")
+    flags = ["g++", "-std=c++17", "-O1", "-g", "-fsanitize=thread", "-fPIC", "-pthread",
+             "-I", cuda_include(), "-I", CSRC, "-I", HERE,
+             "-I", os.path.join(ROOT, "include")]
+    srcs = [os.path.join(CSRC, f) for f in HOST_UNITS] + [
+        os.path.join(HERE, f) for f in SIM_UNITS + ["serve_race.cpp"]]
+    if not _stale(exe, srcs + _deps()):
+        return exe
+    objs = []
+
+    def one(src):
+        obj = os.path.join(out, os.path.basename(src).rsplit(".", 1)[0] + ".o")
+        lang = ["-x", "c++"] if src.endswith(".cu") else []
+        r = subprocess.run(flags + lang + ["-c", src, "-o", obj], capture_output=True,
+                           text=True)
+        if r.returncode != 0:
+            raise RuntimeError("tsan build failed:\n%s" % r.stderr)
+        return obj
+
+    with ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
+        objs = list(ex.map(one, srcs))
+    r = subprocess.run(["g++", "-fsanitize=thread", "-pthread", "-o", exe] + objs,
+                       capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("tsan link failed:\n%s" % r.stderr)
+    return exe
+
+
 if __name__ == "__main__":
     print(build())
     sys.exit(0)

@@ -71,6 +71,23 @@ def test_gpu_tests_not_yet_run_on_a_gpu_pass_on_the_simulation(sim_env):
     assert " passed" in out and "failed" not in out
 
 
+def test_serving_threads_have_no_data_race():
+    """gbcc_server's workers, queue and statistics under ThreadSanitizer."""
+    sys.path.insert(0, os.path.join(ROOT, "tests", "harness", "sim"))
+    try:
+        import build_sim
+    finally:
+        sys.path.pop(0)
+    exe = build_sim.build_serve_race()
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=600)
+    if "unexpected memory mapping" in r.stderr:
+        pytest.skip("ThreadSanitizer cannot run under this kernel's memory layout")
+    assert "ThreadSanitizer" not in r.stderr, r.stderr[-4000:]
+    assert r.returncode == 0, r.stdout + r.stderr[-2000:]
+    lines = [l for l in r.stdout.splitlines() if l.startswith("id ")]
+    assert len(lines) == 10 and all(" st 0 status 0 " in l for l in lines), r.stdout
+
+
 def test_smoke_entry_runs_on_the_simulation(sim_env):
     code = ("import os; from sisi4s_gb300 import capi; capi.load(os.environ['GBCC_SIM_LIB']); "
             "import __graft_entry__ as g; g.smoke()")
