@@ -299,7 +299,8 @@ gbcc_status gbcc_ccsd_result(gbcc_solver *s, gbcc_ccsd_out *out) {
     }
     if (out->energy_history) {
       const auto &h = c.history();
-      std::memcpy(out->energy_history, h.data(), sizeof(double) * h.size());
+      if (!h.empty())  // no iteration ran with maxIterations 0
+        std::memcpy(out->energy_history, h.data(), sizeof(double) * h.size());
     }
     GBCC_CUDA(cudaStreamSynchronize(ctx.stream));
     return GBCC_OK;

@@ -76,6 +76,41 @@ def build():
     return LIB
 
 
+def build_sanitized():
+    """The simulation library built with AddressSanitizer and
+    UndefinedBehaviorSanitizer; returns (library, directory whose libgbcc.so
+    is that library)."""
+    out = os.path.join(OUT, "asan")
+    ld = os.path.join(out, "ld")
+    os.makedirs(ld, exist_ok=True)
+    lib = os.path.join(out, "libgbcc_sim_asan.so")
+    flags = ["g++", "-std=c++17", "-O1", "-g", "-fsanitize=address,undefined",
+             "-fno-omit-frame-pointer", "-fPIC", "-pthread",
+             "-I", cuda_include(), "-I", CSRC, "-I", HERE]
+    srcs = [os.path.join(CSRC, f) for f in HOST_UNITS] + [
+        os.path.join(HERE, f) for f in SIM_UNITS]
+    if _stale(lib, srcs + _deps()):
+        def one(src):
+            obj = os.path.join(out, os.path.basename(src).rsplit(".", 1)[0] + ".o")
+            lang = ["-x", "c++"] if src.endswith(".cu") else []
+            r = subprocess.run(flags + lang + ["-c", src, "-o", obj], capture_output=True,
+                               text=True)
+            if r.returncode != 0:
+                raise RuntimeError("sanitized build failed:\n%s" % r.stderr)
+            return obj
+
+        with ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
+            objs = list(ex.map(one, srcs))
+        r = subprocess.run(["g++", "-shared", "-fsanitize=address,undefined", "-pthread",
+                            "-o", lib] + objs, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("sanitized link failed:\n%s" % r.stderr)
+    link = os.path.join(ld, "libgbcc.so")
+    if not os.path.islink(link):
+        os.symlink(os.path.relpath(lib, ld), link)
+    return lib, ld
+
+
 def build_serve_race():
     """serve_race.cpp linked against a ThreadSanitizer build of the library's
     host code and of the simulation; returns the binary's path."""

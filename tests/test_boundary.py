@@ -230,7 +230,12 @@ def test_tensor_lengths_are_checked_before_the_library_is_called(tmp_path, step,
     for n, shape in good.items():
         if n == bad:
             shape = shape[:-1] + (shape[-1] + 1,)
-        _write_tensor(tmp_path / ("%s.yaml" % n), rng.normal(size=shape))
+        # a well-posed system, so that on a device the step also succeeds:
+        # holes below particles, small integrals and amplitudes
+        x = {"Eh": -1.0 - rng.uniform(size=shape), "Ep": 1.0 + rng.uniform(size=shape)}.get(
+            n, 0.05 * rng.normal(size=shape))
+        _write_tensor(tmp_path / ("%s.yaml" % n), x)
+    out_keys = {"CcsdPerturbativeTriples": "{ CcsdPerturbativeTriplesEnergy: $E }"}
     r, out = _run(tmp_path, _read_steps(good) + """
 - name: %s
   in:
@@ -244,8 +249,8 @@ def test_tensor_lengths_are_checked_before_the_library_is_called(tmp_path, step,
     CcsdEnergy: 0.0
     CcsdSinglesAmplitudes: $T1
     CcsdDoublesAmplitudes: $T2
-  out: {}
-""" % step)
+  out: %s
+""" % (step, out_keys.get(step, "{}")))
     if bad is None:  # right lengths: the step reaches the library
         assert r.returncode == 0 or "GPU context: NO_DEVICE" in out["error"], out
         return
@@ -322,42 +327,47 @@ def test_complex_branch_is_chosen_by_the_integrals(tmp_path):
     # by the real path as Re.Re + Im.Im; the real (T) refuses complex amplitudes
     rng = np.random.default_rng(2)
     No, Nv, NG = 2, 3, 4
-    _write_tensor(tmp_path / "Eh.yaml", rng.normal(size=No))
-    _write_tensor(tmp_path / "Ep.yaml", rng.normal(size=Nv))
-    _write_tensor(tmp_path / "F.yaml", rng.normal(size=(No, Nv)))
-    c = lambda *shape: rng.normal(size=shape) + 1j * rng.normal(size=shape)
+    # a well-posed system, so that on a device the steps also succeed: holes
+    # below particles, small integrals and amplitudes
+    _write_tensor(tmp_path / "Eh.yaml", -1.0 - rng.uniform(size=No))
+    _write_tensor(tmp_path / "Ep.yaml", 1.0 + rng.uniform(size=Nv))
+    _write_tensor(tmp_path / "F.yaml", 0.05 * rng.normal(size=(No, Nv)))
+    c = lambda *shape: 0.05 * (rng.normal(size=shape) + 1j * rng.normal(size=shape))
     _write_complex_tensor(tmp_path / "G.yaml", c(NG, No + Nv, No + Nv))
     _write_complex_tensor(tmp_path / "V.yaml", c(Nv, Nv, No, No))
     _write_complex_tensor(tmp_path / "T1.yaml", c(Nv, No))
-    _write_tensor(tmp_path / "T2.yaml", rng.normal(size=(Nv, Nv, No, No)))
+    _write_tensor(tmp_path / "T2.yaml", 0.05 * rng.normal(size=(Nv, Nv, No, No)))
     reads = _read_steps(["Eh", "Ep", "F", "G", "V", "T1", "T2"])
     common = """    CoulombVertex: $G
     HoleEigenEnergies: $Eh
     ParticleEigenEnergies: $Ep
 """
     reaches_library = lambda r, out: r.returncode == 0 or "GPU context: NO_DEVICE" in out["error"]
-    step = lambda name, extra: (reads + "- name: %s\n  in:\n" % name + common + extra
-                                + "  out: {}\n")
+    # every output a step sets is listed, as the reference requires
+    # (Algorithm.cxx:37-45 throws on a missing argument)
+    step = lambda name, extra, outs: (reads + "- name: %s\n  in:\n" % name + common + extra
+                                      + "  out: { %s }\n" % outs)
+    e = "CcsdEnergy: $E"
     r, out = _run(tmp_path, step("CcsdEnergyFromCoulombIntegrals",
-                                 "    HPFockMatrix: $F\n    PPHHCoulombIntegrals: $V\n"))
+                                 "    HPFockMatrix: $F\n    PPHHCoulombIntegrals: $V\n", e))
     assert reaches_library(r, out), out    # the complex branch with its Fock term
     r, out = _run(tmp_path, step("CcsdEnergyFromCoulombIntegrals",
-                                 "    PPHHCoulombIntegrals: $V\n  out:\n    PairEnergy: $P\n")
-                  .replace("  out: {}\n", ""))
+                                 "    PPHHCoulombIntegrals: $V\n", e + ", PairEnergy: $P"))
     assert reaches_library(r, out), out
     r, out = _run(tmp_path, step("CcsdEnergyFromCoulombIntegralsReference",
-                                 "    PPHHCoulombIntegrals: $V\n"))
+                                 "    PPHHCoulombIntegrals: $V\n", e))
     assert r.returncode == 1 and "has a complex branch here" in out["error"], out
-    r, out = _run(tmp_path, step("CcsdEnergyFromCoulombIntegrals", "    HPFockMatrix: $F\n"))
+    r, out = _run(tmp_path, step("CcsdEnergyFromCoulombIntegrals", "    HPFockMatrix: $F\n", e))
     assert reaches_library(r, out), out
     amps = "    CcsdEnergy: 0.0\n    CcsdSinglesAmplitudes: $T1\n    CcsdDoublesAmplitudes: $T2\n"
-    r, out = _run(tmp_path, step("CcsdPerturbativeTriples", amps))
+    r, out = _run(tmp_path, step("CcsdPerturbativeTriples", amps,
+                                 "CcsdPerturbativeTriplesEnergy: $Et"))
     assert r.returncode == 1 and "CcsdPerturbativeTriplesComplex" in out["error"], out
-    r, out = _run(tmp_path, step("CcsdPerturbativeTriplesComplex", amps))
+    r, out = _run(tmp_path, step("CcsdPerturbativeTriplesComplex", amps,
+                                 "CcsdPerturbativeTriplesComplexEnergy: $Et"))
     assert reaches_library(r, out), out
-    r, out = _run(tmp_path, step("CoulombIntegralsFromVertex",
-                                 "    complex: 1\n  out:\n    PPHHCoulombIntegrals: $W\n")
-                  .replace("  out: {}\n", ""))
+    r, out = _run(tmp_path, step("CoulombIntegralsFromVertex", "    complex: 1\n",
+                                 "PPHHCoulombIntegrals: $W"))
     assert reaches_library(r, out), out
 
 
