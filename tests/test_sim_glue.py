@@ -33,7 +33,8 @@ CALIBRATION = ["tests/test_gpu_parity.py", "tests/test_gpu_failure.py", "-k",
                "not dgemm_all and not matrix_vector and not c1_config and not device_wait"]
 RUNNER = ["tests/test_gpu_runner.py"]
 NEW_PATHS = ["tests/test_zzz_energy_terms.py", "tests/test_zzz_complex_branch.py",
-             "tests/test_zzz_stored_formulation.py", "tests/test_zzz_golden_fixtures.py"]
+             "tests/test_zzz_stored_formulation.py", "tests/test_zzz_golden_fixtures.py",
+             "tests/test_zzz_solver_options.py"]
 
 
 @pytest.fixture(scope="module")
