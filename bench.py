@@ -398,6 +398,7 @@ def main():
     r = gpu.ccsd_solve(ctx, s.eps_h, s.eps_p, g_host, precision="emu",
                        initial=(t1_0, t2_host), **dict(kw, max_iterations=args.steps))
     e2e_s = time.perf_counter() - t0
+    del g_host, t2_host  # hand the page-locked staging back
     Np = W["No"] + W["Nv"]
     n2 = W["Nv"] ** 2 * W["No"] ** 2
     h2d = 8 * (W["NG"] * Np * Np + W["No"] + W["Nv"] + W["Nv"] * W["No"] + n2)
