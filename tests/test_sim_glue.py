@@ -125,18 +125,25 @@ def test_serving_threads_have_no_data_race():
     assert len(lines) == 10 and all(" st 0 status 0 " in l for l in lines), r.stdout
 
 
-def test_complex_bench_script_runs_on_the_simulation(sim_env):
-    """The complex-branch measurement script end to end (it needs no torch)."""
+@pytest.mark.parametrize("module,argv", [
+    ("complex_bench", ["3", "8", "12", "--iterations", "3"]),
+    ("solve_bench", ["3", "10", "24", "--iterations", "3", "--formulation", "stored",
+                     "--triples-fp64-on-emu"]),
+    ("solve_bench", ["3", "10", "24", "--iterations", "3"]),
+])
+def test_measurement_scripts_run_on_the_simulation(sim_env, module, argv):
+    """The measurement scripts of the complex branch and of the two real
+    formulations end to end (they need no torch)."""
     code = ("import os, sys, runpy; from sisi4s_gb300 import capi; "
             "capi.load(os.environ['GBCC_SIM_LIB']); "
-            "sys.argv = ['complex_bench', '3', '8', '12', '--iterations', '3']; "
-            "runpy.run_module('sisi4s_gb300.complex_bench', run_name='__main__')")
+            "sys.argv = [%r] + %r; "
+            "runpy.run_module('sisi4s_gb300.%s', run_name='__main__')" % (module, argv, module))
     r = subprocess.run([sys.executable, "-c", code], cwd=ROOT, env=sim_env,
                        capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout + r.stderr
     import json
     line = json.loads(r.stdout.strip().splitlines()[-1])
-    assert line["dE_ccsd_ha"] == 0.0  # FP64 GEMMs model both precisions here
+    assert line["dE_ccsd_ha"] == 0.0  # FP64 products model both precisions here
     assert set(line["emu"]) >= {"energy", "seconds_per_iteration", "e_t"}
 
 
