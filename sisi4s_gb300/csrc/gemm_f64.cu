@@ -241,14 +241,17 @@ void gemv(Context &ctx, int64_t Mo, int64_t K, double alpha, const double *A,
           int64_t ars, int64_t aks, const double *x, int64_t incx, double beta,
           double *y, int64_t incy) {
   const int64_t G = std::max(ctx.sm_count, 1);
-  if (aks == 1) {
+  // a single output (a dot product) goes to the K-split form below, whatever
+  // the layout: one warp over all of K would leave the GPU idle
+  if (aks == 1 && Mo > 1) {
     const int64_t blocks = std::min<int64_t>((Mo * 32 + 255) / 256, G * 32);
     gemv_rows_kernel<<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, ctx.stream>>>(
         Mo, K, alpha, A, ars, x, incx, beta, y, incy);
     GBCC_CHECK_LAUNCH(ctx);
     return;
   }
-  require(ars == 1, "gemv: one operand index must be contiguous");
+  // with one output the row stride is never used (row 0 only)
+  require(ars == 1 || Mo == 1, "gemv: one operand index must be contiguous");
   const int64_t bx = (Mo + 255) / 256;
   int64_t nch = std::max<int64_t>(1, std::min<int64_t>((G * 8 + bx - 1) / bx, (K + 63) / 64));
   nch = std::min<int64_t>(nch, 65535);
