@@ -186,3 +186,94 @@ def test_complex_pair_energies(ctx):
     assert np.abs(r["pair_energy"] - ref).max() < 1e-12 * np.abs(ref).max()
     # the pair energies sum to the correlation energy (:189, :227-232)
     assert abs(r["pair_energy"].sum() - r["energy"]) < 1e-12 * abs(r["energy"])
+
+
+COMPLEX_STEPS = """
+- name: DefineHolesAndParticles
+  in: { fileName: "EigenEnergies.yaml" }
+  out: { HoleEigenEnergies: $Eh, ParticleEigenEnergies: $Ep }
+- name: Read
+  in: { fileName: "CoulombVertex.yaml" }
+  out: { destination: $G }
+- name: CoulombIntegralsFromVertex
+  in: { CoulombVertex: $G, HoleEigenEnergies: $Eh, ParticleEigenEnergies: $Ep, complex: 1 }
+  out:
+    PPHHCoulombIntegrals: $PPHH
+    PHPHCoulombIntegrals: $PHPH
+    HHHHCoulombIntegrals: $HHHH
+    HHHPCoulombIntegrals: $HHHP
+    PHHHCoulombIntegrals: $PHHH
+- name: CcsdEnergyFromCoulombIntegrals
+  in:
+    maxIterations: 60
+    energyConvergence: 1e-11
+    amplitudesConvergence: 1e-9
+    HoleEigenEnergies: $Eh
+    ParticleEigenEnergies: $Ep
+    CoulombVertex: $G
+    PPHHCoulombIntegrals: $PPHH
+    PHPHCoulombIntegrals: $PHPH
+    HHHHCoulombIntegrals: $HHHH
+    HHHPCoulombIntegrals: $HHHP
+  out:
+    CcsdEnergy: $E
+    CcsdSinglesAmplitudes: $T1
+    CcsdDoublesAmplitudes: $T2
+- name: CcsdPerturbativeTriplesComplex
+  in:
+    HoleEigenEnergies: $Eh
+    ParticleEigenEnergies: $Ep
+    CoulombVertex: $G
+    PPHHCoulombIntegrals: $PPHH
+    CcsdEnergy: $E
+    CcsdSinglesAmplitudes: $T1
+    CcsdDoublesAmplitudes: $T2
+  out:
+    CcsdPerturbativeTriplesComplexEnergy: $Etot
+"""
+
+
+def test_ueg_golden_through_the_complex_pipeline_in_the_runner(tmp_path):
+    """The step runner end to end on the complex branch: the reference's UEG
+    plane-wave vertex with random orbital phases, written as a Complex64 cc4s
+    file, through CoulombIntegralsFromVertex (complex: 1), the complex CCSD
+    and CcsdPerturbativeTriplesComplex; the golden energies come out."""
+    import json
+    import os
+    import subprocess
+
+    from sisi4s_gb300 import build
+    build.build()
+    runner = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                          "sisi4s_gb300", "_lib", "sisi4s-gb300")
+    gd = UEG_GOLDEN
+    _, eps, gam, _ = ueg_planewave(gd["No"], gd["Nv"], gd["rs"])
+    ph = np.exp(1j * np.random.default_rng(11).uniform(0, 2 * np.pi, gam.shape[1]))
+    gam = np.conj(ph)[None, :, None] * gam * ph[None, None, :]
+    n = gd["No"]
+    fermi = 0.5 * (eps[:n].max() + eps[n:].min())
+    (tmp_path / "EigenEnergies.yaml").write_text(
+        "metaData:\n  fermiEnergy: %.17g\n  energies: [%s]\n"
+        % (fermi, ", ".join("%.17g" % e for e in eps)))
+    NG, Np, _ = gam.shape
+    (tmp_path / "CoulombVertex.yaml").write_text(
+        "version: 100\ntype: Tensor\ndimensions:\n"
+        "  - length: %d\n    type: AuxiliaryField\n"
+        "  - length: %d\n    type: State\n  - length: %d\n    type: State\n"
+        "scalarType: Complex64\nelements:\n  type: IeeeBinaryFile\nunit: 1.0\n" % (NG, Np, Np))
+    z = np.ascontiguousarray(gam.transpose(2, 1, 0)).ravel()
+    z.view(np.float64).tofile(tmp_path / "CoulombVertex.elements")
+    (tmp_path / "in.yaml").write_text(COMPLEX_STEPS)
+    r = subprocess.run([runner, "-i", "in.yaml", "-o", "out.yaml"], cwd=tmp_path,
+                       capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stdout + r.stderr
+    out = json.loads((tmp_path / "out.yaml").read_text())
+    steps = {s["name"]: s for s in out["steps"]}
+    cc = steps["CcsdEnergyFromCoulombIntegrals"]
+    assert cc["convergenceReached"] == 1
+    assert abs(cc["iterations"][0]["energy"]["value"] - gd["mp2"]) < 1e-12
+    assert abs(cc["energy"]["value"] - gd["ccsd"]) < 1e-8 * abs(gd["ccsd"])
+    assert abs(cc["energy"]["imaginary"]) < 1e-14
+    t = steps["CcsdPerturbativeTriplesComplex"]["energy"]
+    assert abs(t["triples"] - gd["triples"]) < 1e-10 and abs(t["triplesImaginary"]) < 1e-14
+    assert t["value"] == cc["energy"]["value"] + t["triples"]
