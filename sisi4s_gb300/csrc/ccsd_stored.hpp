@@ -137,14 +137,21 @@ void residual(RB &rb, const Ints &I, int it, const Opts &o, const View &T1, cons
     C(1.0, w.v, "alij", T1, "bl", 1.0, R2, "abij");
   }
   {
-    auto Xabcd = rb.alloc({Nv, Nv, Nv, Nv});
-    rb.axpby(1.0, Vabcd, 0.0, Xabcd.v);                             // :255
-    C(-1.0, Vabci, "cdak", T1, "bk", 1.0, Xabcd.v, "abcd");         // :256
-    C(-1.0, Vabci, "dcbk", T1, "ak", 1.0, Xabcd.v, "abcd");         // :257
-    C(1.0, Xabcd.v, "abcd", T2, "cdij", 1.0, R2, "abij");           // :260
-    auto w = rb.alloc({Nv, Nv, Nv, No});                            // :261
-    C(1.0, Xabcd.v, "abcd", T1, "ci", 0.0, w.v, "abdi");
-    C(1.0, w.v, "abdi", T1, "dj", 1.0, R2, "abij");
+    // :255-263 add X_abcd (T2_cdij + T1_ci T1_dj) with the dressed
+    //   X_abcd = V_abcd - Vabci_cdak T1_bk - Vabci_dcbk T1_ak.
+    // The same sum, without a second Nv^4 tensor:
+    //   V_abcd Xp_cdij - T1_bk Y_akij - T1_ak Y'_bkij,  Xp = T2 + T1 T1,
+    //   Y_akij = Vabci_cdak Xp_cdij,  Y'_bkij = Vabci_dcbk Xp_cdij,
+    // so the only Nv^4 operand is the resident V_abcd (one GEMM, no permute)
+    auto Xp = rb.alloc({Nv, Nv, No, No});
+    rb.axpby(1.0, T2, 0.0, Xp.v);
+    C(1.0, T1, "ci", T1, "dj", 1.0, Xp.v, "cdij");
+    C(1.0, Vabcd, "abcd", Xp.v, "cdij", 1.0, R2, "abij");
+    auto Y = rb.alloc({Nv, No, No, No});
+    C(1.0, Vabci, "cdak", Xp.v, "cdij", 0.0, Y.v, "akij");
+    C(-1.0, T1, "bk", Y.v, "akij", 1.0, R2, "abij");
+    C(1.0, Vabci, "dcbk", Xp.v, "cdij", 0.0, Y.v, "bkij");
+    C(-1.0, T1, "ak", Y.v, "bkij", 1.0, R2, "abij");
   }
   C(1.0, Kac.v, "ac", T1, "ci", 1.0, R1, "ai");                     // :271
   C(-1.0, Kki.v, "ki", T1, "ak", 1.0, R1, "ai");                    // :272

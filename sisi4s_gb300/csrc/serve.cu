@@ -59,9 +59,9 @@ size_t estimate_bytes(const gbcc_ccsd_in &in, const gbcc_ccsd_opts &o, int tripl
                  + 6.0 * n2                            // residual temporaries
                  + 2.0 * s * s * Nv * Nv;              // ladder block
   if (triples) words += Nv * Nv * Nv * No + 6.0 * Nv * Nv * Nv;
-  // stored formulation: resident Vabcd / Vabci, and the dressed Xabcd with
-  // its temporaries in every residual
-  if (o.formulation == 1) words += 2.0 * Nv * Nv * Nv * Nv + 2.0 * Nv * Nv * Nv * No;
+  // stored formulation: resident Vabcd / Vabci (the residual adds no other
+  // Nv^4 tensor) and a permuted copy of Vabci
+  if (o.formulation == 1) words += 1.0 * Nv * Nv * Nv * Nv + 2.0 * Nv * Nv * Nv * No;
   double bytes = 8.0 * words;
   if (o.precision == GBCC_PREC_EMU) bytes *= 1.6;      // digit panels
   return (size_t)(1.5 * bytes) + (64u << 20);
