@@ -62,6 +62,44 @@ def _pytest(env, args):
     return r.stdout
 
 
+def test_simulated_capture_follows_cuda_rules(sim_env):
+    """The stand-in runtime's stream capture: work is recorded, not run, and
+    runs at every graph launch; synchronising calls and copies with pageable
+    host memory are refused during the capture, as under CUDA."""
+    import ctypes as C
+
+    import numpy as np
+    lib = C.CDLL(sim_env["GBCC_SIM_LIB"])
+    vp = C.c_void_p
+    s, dev, pinned, graph, exe = vp(), vp(), vp(), vp(), vp()
+    assert lib.cudaStreamCreateWithFlags(C.byref(s), 1) == 0
+    assert lib.cudaMallocAsync(C.byref(dev), C.c_size_t(64), s) == 0
+    assert lib.cudaMallocHost(C.byref(pinned), C.c_size_t(64)) == 0
+    buf = (C.c_ubyte * 64).from_address(pinned.value)
+    C.memset(pinned, 0, 64)
+    assert lib.cudaMemsetAsync(dev, 0, C.c_size_t(64), s) == 0
+    assert lib.cudaStreamBeginCapture(s, 1) == 0
+    assert lib.cudaMemsetAsync(dev, 7, C.c_size_t(64), s) == 0
+    assert lib.cudaMemcpyAsync(pinned, dev, C.c_size_t(64), 2, s) == 0  # device to host
+    assert lib.cudaStreamSynchronize(s) != 0
+    assert lib.cudaMalloc(C.byref(vp()), C.c_size_t(8)) != 0
+    host = np.zeros(8)
+    assert lib.cudaMemcpyAsync(vp(host.ctypes.data), dev, C.c_size_t(64), 2, s) != 0
+    assert lib.cudaStreamEndCapture(s, C.byref(graph)) == 0
+    assert bytes(buf) == bytes(64)  # recorded, not run
+    assert lib.cudaGraphInstantiate(C.byref(exe), graph, C.c_ulonglong(0)) == 0
+    assert lib.cudaGraphDestroy(graph) == 0
+    assert lib.cudaGraphLaunch(exe, s) == 0
+    assert bytes(buf) == bytes([7] * 64)
+    assert lib.cudaMemsetAsync(dev, 0, C.c_size_t(64), s) == 0
+    assert lib.cudaGraphLaunch(exe, s) == 0  # runs again
+    assert bytes(buf) == bytes([7] * 64)
+    assert lib.cudaStreamSynchronize(s) == 0
+    for call in (lib.cudaGraphExecDestroy(exe), lib.cudaFreeAsync(dev, s),
+                 lib.cudaFreeHost(pinned), lib.cudaStreamDestroy(s)):
+        assert call == 0
+
+
 def test_calibration_set_passes_on_the_simulation(sim_env):
     out = _pytest(sim_env, CALIBRATION + RUNNER)
     assert " passed" in out and "failed" not in out
