@@ -34,7 +34,8 @@ CALIBRATION = ["tests/test_gpu_parity.py", "tests/test_gpu_failure.py", "-k",
 RUNNER = ["tests/test_gpu_runner.py"]
 NEW_PATHS = ["tests/test_zzz_energy_terms.py", "tests/test_zzz_complex_branch.py",
              "tests/test_zzz_stored_formulation.py", "tests/test_zzz_golden_fixtures.py",
-             "tests/test_zzz_solver_options.py", "tests/test_zzz_stepping_api.py"]
+             "tests/test_zzz_solver_options.py", "tests/test_zzz_stepping_api.py",
+             "tests/test_zzz_failure_new_paths.py"]
 
 
 @pytest.fixture(scope="module")
