@@ -64,8 +64,11 @@ def build():
 
     with ThreadPoolExecutor(max_workers=min(len(jobs) or 1, os.cpu_count() or 4)) as ex:
         list(ex.map(run, jobs))
-    if jobs or not os.path.exists(LIB):
-        run(["g++", "-shared", "-pthread", "-Wl,--no-undefined", "-o", LIB] + objs)
+    if jobs or _stale(LIB, objs + [os.path.abspath(__file__)]):
+        # -Bsymbolic: the library's calls into the stand-in runtime bind to
+        # it even in a process that has loaded the real CUDA runtime globally
+        run(["g++", "-shared", "-pthread", "-Wl,--no-undefined", "-Wl,-Bsymbolic", "-o", LIB]
+            + objs)
     # a directory whose libgbcc.so is the simulation: with it first on
     # LD_LIBRARY_PATH the step runner (which links libgbcc.so with a RUNPATH)
     # runs on the simulation too
@@ -89,7 +92,7 @@ def build_sanitized():
              "-I", cuda_include(), "-I", CSRC, "-I", HERE]
     srcs = [os.path.join(CSRC, f) for f in HOST_UNITS] + [
         os.path.join(HERE, f) for f in SIM_UNITS]
-    if _stale(lib, srcs + _deps()):
+    if _stale(lib, srcs + _deps() + [os.path.abspath(__file__)]):
         def one(src):
             obj = os.path.join(out, os.path.basename(src).rsplit(".", 1)[0] + ".o")
             lang = ["-x", "c++"] if src.endswith(".cu") else []
@@ -102,6 +105,7 @@ def build_sanitized():
         with ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
             objs = list(ex.map(one, srcs))
         r = subprocess.run(["g++", "-shared", "-fsanitize=address,undefined", "-pthread",
+                            "-Wl,-Bsymbolic",
                             "-o", lib] + objs, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("sanitized link failed:\n%s" % r.stderr)
@@ -122,7 +126,7 @@ def build_serve_race():
              "-I", os.path.join(ROOT, "include")]
     srcs = [os.path.join(CSRC, f) for f in HOST_UNITS] + [
         os.path.join(HERE, f) for f in SIM_UNITS + ["serve_race.cpp"]]
-    if not _stale(exe, srcs + _deps()):
+    if not _stale(exe, srcs + _deps() + [os.path.abspath(__file__)]):
         return exe
     objs = []
 
