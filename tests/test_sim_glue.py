@@ -29,8 +29,10 @@ import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
-CALIBRATION = ["tests/test_gpu_parity.py", "tests/test_gpu_failure.py", "-k",
-               "not dgemm_all and not matrix_vector and not c1_config and not device_wait"]
+CALIBRATION = ["tests/test_gpu_parity.py", "tests/test_gpu_failure.py",
+               "tests/test_gpu_serve.py", "-k",
+               "not dgemm_all and not matrix_vector and not c1_config and not device_wait"
+               " and not alone_equals and not requests_overlap"]
 RUNNER = ["tests/test_gpu_runner.py"]
 NEW_PATHS = ["tests/test_zzz_energy_terms.py", "tests/test_zzz_complex_branch.py",
              "tests/test_zzz_stored_formulation.py", "tests/test_zzz_golden_fixtures.py",
