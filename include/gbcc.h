@@ -25,8 +25,10 @@ extern "C" {
 typedef enum {
   GBCC_OK = 0,
   GBCC_NOT_CONVERGED = 1,    /* maxIterations reached; results are valid */
-  GBCC_DIIS_SINGULAR = 2,    /* DIIS subspace matrix singular (dsysv info != 0) */
-  GBCC_DIVERGED = 3,         /* NaN/Inf in the energy or amplitude norms */
+  GBCC_DIIS_SINGULAR = 2,    /* DIIS subspace matrix singular: an exact zero
+                                pivot, where dsysv gives info != 0 */
+  GBCC_DIVERGED = 3,         /* NaN/Inf in the energy, the amplitude norms, or
+                                the DIIS overlaps and weights (overflow) */
   GBCC_OOM = 4,              /* device allocation failed / over HBM budget */
   GBCC_BAD_ARG = 5,
   GBCC_CUDA_ERROR = 6,
@@ -194,6 +196,14 @@ gbcc_status gbcc_ccsd_result(gbcc_solver *s, gbcc_ccsd_out *out);
 gbcc_status gbcc_ccsd_device_amplitudes(gbcc_solver *s, const double **T1,
                                         const double **T2);
 void gbcc_ccsd_destroy(gbcc_solver *s);
+/* Returns the solver to its state after setup: the starting amplitudes given
+ * at setup (else zero amplitudes, so the next iteration is the MP2 start),
+ * no iterations done, an empty DIIS history.  The uploaded inputs, integrals,
+ * buffers and captured iteration graphs are kept, so a repeated solve of the
+ * same system pays none of the setup again.  No counterpart in the reference,
+ * whose algorithms run once per step (ClusterSinglesDoublesAlgorithm.cxx:38-128
+ * always starts from the data map's amplitudes). */
+gbcc_status gbcc_ccsd_restart(gbcc_solver *s);
 
 /* One residual evaluation R(T) for iteration index `it` (it == 0 without
  * initial doubles gives the MP2 start R2 = Vabij), for parity tests.
@@ -353,14 +363,18 @@ gbcc_status gbcc_dgemm(gbcc_ctx *ctx, int transA, int transB, int64_t M,
  * already holds the whole HBM budget, or a host loop that must not enter the
  * CUDA allocator.  It has no counterpart in the reference.  Its scratch (digit
  * panels of both operands, exponents, error word) lives in one fixed 32 MiB
- * device array that every GPU loading the library holds until exit; a GEMM
- * whose scratch would exceed it (S digits x 2 bytes x (M padded to 128 +
- * N padded to 64) x K padded to 32, plus 4 bytes per row and column) is
- * rejected with GBCC_BAD_ARG.  Nothing is allocated or freed.  All calls on a
- * device share the array, so calls whose work overlaps on the GPU race; order
- * them.  The first call on a device looks up the array's device address; make
- * it before any stream capture.  Device pointers, context stream, digits from
- * gbcc_ctx_set_emulation. */
+ * device array, which every GPU that runs the library's kernels holds until
+ * the process exits (with CUDA's lazy module loading, from the first use on
+ * that GPU); a GEMM whose scratch would exceed it (S digits x 2 bytes x
+ * (M padded to 128 + N padded to 64) x K padded to 32, plus 4 bytes per row
+ * and column) is rejected with GBCC_BAD_ARG.  Nothing is allocated or freed.
+ * All calls on a device share the array, so calls whose work overlaps on the
+ * GPU race; order them.  Each call waits for its GEMM to finish (it reads the
+ * kernel's error word back) before it returns.  The first call on a device
+ * looks up the array's device address and keeps it for the life of the
+ * process; make it before any stream capture, and do not call this entry point
+ * on a device after resetting it (cudaDeviceReset).  Device pointers, context
+ * stream, digits from gbcc_ctx_set_emulation. */
 gbcc_status gbcc_dgemm_emu_noalloc(gbcc_ctx *ctx, int transA, int transB,
                                    int64_t M, int64_t N, int64_t K,
                                    double alpha, const double *A, int64_t lda,

@@ -101,6 +101,7 @@ _SIGS = {
     "gbcc_ccsd_device_amplitudes": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p),
                                               C.POINTER(C.c_void_p)]),
     "gbcc_ccsd_destroy": (None, [C.c_void_p]),
+    "gbcc_ccsd_restart": (C.c_int, [C.c_void_p]),
     "gbcc_ccsd_residual": (C.c_int, [C.c_void_p, C.POINTER(CcsdIn),
                                      C.POINTER(CcsdOpts), C.c_int, _dp, _dp,
                                      _dp, _dp]),

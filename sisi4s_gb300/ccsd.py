@@ -186,15 +186,24 @@ class Solver:
                                                    C.byref(conv)))
         return e.value, bool(conv.value)
 
+    def restart(self):
+        """Back to the starting amplitudes with no iterations done; the
+        resident inputs and captured iteration graphs are kept."""
+        self.ctx.check(self.ctx.lib.gbcc_ccsd_restart(self.h))
+
     def result(self, amplitudes=True):
+        """Energy, iteration count, the energy of every iteration since the
+        start (or the last restart) and, optionally, the amplitudes."""
         No, Nv = self.inp.No, self.inp.Nv
         out = capi.CcsdOut()
         t1 = np.zeros(Nv * No) if amplitudes else None
         t2 = np.zeros(Nv * Nv * No * No) if amplitudes else None
-        out.T1, out.T2 = ptr(t1), ptr(t2)
+        hist = np.zeros(max(self.opts.max_iterations, 1))
+        out.T1, out.T2, out.energy_history = ptr(t1), ptr(t2), ptr(hist)
         self.ctx.check(self.ctx.lib.gbcc_ccsd_result(self.h, C.byref(out)))
         r = {"energy": out.energy, "iterations": out.iterations,
-             "converged": bool(out.converged)}
+             "converged": bool(out.converged),
+             "history": hist[:out.iterations].copy()}
         if amplitudes:
             r["T1"] = from_fortran_flat(t1, (Nv, No))
             r["T2"] = from_fortran_flat(t2, (Nv, Nv, No, No))

@@ -315,6 +315,14 @@ gbcc_status gbcc_ccsd_device_amplitudes(gbcc_solver *s, const double **T1,
   return GBCC_OK;
 }
 
+gbcc_status gbcc_ccsd_restart(gbcc_solver *s) {
+  if (!s) return GBCC_BAD_ARG;
+  return guard(s->ctx, [&]() {
+    s->s->restart();
+    return GBCC_OK;
+  });
+}
+
 void gbcc_ccsd_destroy(gbcc_solver *s) {
   if (!s) return;
   cudaSetDevice(s->ctx->c.device);

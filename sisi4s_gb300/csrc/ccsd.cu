@@ -10,6 +10,7 @@
 #include <cmath>
 #include <limits>
 #include <cstring>
+#include <string>
 
 #include "ccsd.hpp"
 
@@ -163,6 +164,10 @@ Ccsd::Ccsd(Context &ctx, std::unique_ptr<CcsdInputs> in,
     GBCC_CUDA(cudaMemcpyAsync(T_.as<double>() + L_.off2, init_T2_host,
                               8 * L_.n2, cudaMemcpyHostToDevice, ctx_.stream));
     init_doubles_ = true;
+  }
+  if (init_T1_host || init_T2_host) {  // kept for restart()
+    T0_.alloc(ctx_, fb);
+    copy(ctx_, T0_.as<double>(), T_.as<double>(), L_.ntot);
   }
   (void)No;
   const int nb = reduction_blocks(ctx_, L_.ntot);
@@ -409,8 +414,10 @@ void Ccsd::iteration_body() {
     const int k = next_;
     std::vector<const double *> hist;
     std::vector<int> hslot;
+    // slots filled since the start (or the last restart): 0 .. count_-1
+    // while the ring fills, all of them once it is full
     for (int i = 0; i < N; ++i)
-      if (i != k && slotD_[i].bytes()) {
+      if (i != k && i < count_) {
         hist.push_back(slotD_[i].as<double>());
         hslot.push_back(i);
       }
@@ -559,6 +566,19 @@ IterInfo Ccsd::iterate() {
   return info;
 }
 
+void Ccsd::restart() {
+  if (T0_.bytes()) copy(ctx_, T_.as<double>(), T0_.as<double>(), L_.ntot);
+  else fill(ctx_, T_.as<double>(), L_.ntot, 0.0);
+  it_ = 0;
+  count_ = 0;
+  next_ = 0;
+  have_last_ = false;  // swaps_ keeps the linear mixer's buffer parity
+  converged_ = false;
+  e_ = prev_ = dir_ = exc_ = 0.0;
+  hist_.clear();
+  ctx_.check_device_errors();
+}
+
 gbcc_status Ccsd::run(int n, double *energy, int *converged) {
   gbcc_status st = GBCC_OK;
   for (int c = 0; c < n && !converged_; ++c) {
@@ -571,11 +591,26 @@ gbcc_status Ccsd::run(int n, double *energy, int *converged) {
     ++it_;
     if (o_.mixer == 1 && ctx_.take_fault(GBCC_FAULT_DIIS_SINGULAR)) info.diis_status = 1;
     if (ctx_.take_fault(GBCC_FAULT_NAN)) info.dtdt = std::numeric_limits<double>::quiet_NaN();
-    if (info.diis_status) {
+    if (info.diis_status == 1) {
+      // an exact zero pivot: dsysv's info != 0 (DiisMixer.cxx:37-41)
+      ctx_.last_error = "DIIS subspace matrix singular at iteration " +
+                        std::to_string(it_ - 1) + " (|dT|^2 = " +
+                        std::to_string(info.dtdt) + ")";
       st = GBCC_DIIS_SINGULAR;
       break;
     }
+    if (info.diis_status == 2) {
+      // overlaps or weights overflowed: the reference's dsysv returns
+      // info == 0 there and its amplitudes become NaN
+      ctx_.last_error = "DIIS subspace matrix or weights not finite at iteration " +
+                        std::to_string(it_ - 1) + " (|dT|^2 = " +
+                        std::to_string(info.dtdt) + ", E = " + std::to_string(e_) + ")";
+      st = GBCC_DIVERGED;
+      break;
+    }
     if (!std::isfinite(e_) || !std::isfinite(info.dtdt) || !std::isfinite(info.tt)) {
+      ctx_.last_error = "energy or amplitude norms not finite at iteration " +
+                        std::to_string(it_ - 1);
       st = GBCC_DIVERGED;
       break;
     }

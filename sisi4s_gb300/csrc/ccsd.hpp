@@ -56,6 +56,10 @@ class Ccsd {
   int64_t slice_size() const { return slice_; }
   // energy of the current amplitudes without iterating (maxIterations 0)
   void evaluate_energy();
+  // back to the state after construction (the given starting amplitudes, or
+  // zero amplitudes and the MP2 start), keeping the resident integrals, the
+  // buffers and the captured iteration graphs
+  void restart();
 
  private:
   Context &ctx_;
@@ -65,6 +69,7 @@ class Ccsd {
   bool init_doubles_ = false;
   int64_t slice_ = 0;
   DBuf T_, R_;                 // current amplitudes, residual
+  DBuf T0_;                    // given starting amplitudes (restart), if any
   DBuf E_, D_, Lres_;          // linear mixer: estimate, change, last change
   std::vector<DBuf> slotA_, slotD_;  // DIIS history
   DBuf B_, w_, scal_, partials_, hist_slot_;

@@ -204,7 +204,8 @@ __global__ void diis_solve_kernel(double *B, int N, int k, int count,
     double best = fabs(M[c + dim * c]);
     for (int r = c + 1; r < dim; ++r)
       if (fabs(M[r + dim * c]) > best) { best = fabs(M[r + dim * c]); piv = r; }
-    if (!(best > 0.0) || !isfinite(best)) { st = 1; break; }
+    if (!isfinite(best)) { st = 2; break; }  // overflowed overlaps
+    if (!(best > 0.0)) { st = 1; break; }     // exact zero pivot
     if (piv != c) {
       for (int cc = 0; cc < dim; ++cc) {
         const double t = M[c + dim * cc];
@@ -226,7 +227,7 @@ __global__ void diis_solve_kernel(double *B, int N, int k, int count,
       double s = x[r];
       for (int cc = r + 1; cc < dim; ++cc) s -= M[r + dim * cc] * x[cc];
       x[r] = s / M[r + dim * r];
-      if (!isfinite(x[r])) st = 1;
+      if (!isfinite(x[r])) st = 2;
     }
   }
   *status = st;

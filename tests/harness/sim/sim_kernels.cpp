@@ -341,7 +341,11 @@ void diis_solve(Context &ctx, double *B, int N, int k, int count, const double *
           best = std::fabs(M[r + dim * c]);
           piv = r;
         }
-      if (!(best > 0.0) || !std::isfinite(best)) {
+      if (!std::isfinite(best)) {  // overflowed overlaps
+        st = 2;
+        break;
+      }
+      if (!(best > 0.0)) {  // exact zero pivot
         st = 1;
         break;
       }
@@ -362,7 +366,7 @@ void diis_solve(Context &ctx, double *B, int N, int k, int count, const double *
         double s = x[r];
         for (int cc = r + 1; cc < dim; ++cc) s -= M[r + dim * cc] * x[cc];
         x[r] = s / M[r + dim * r];
-        if (!std::isfinite(x[r])) st = 1;
+        if (!std::isfinite(x[r])) st = 2;
       }
     *status = st;
     *lambda = st ? 0.0 : x[0];
