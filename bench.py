@@ -1,27 +1,40 @@
 #!/usr/bin/env python
-"""RCCSD iteration throughput on GB300 (closed-shell CCSD of sisi4s).
+"""RCCSD(T) on one GB300: the closed-shell CCSD iteration and (T) of sisi4s.
 
-Workload: No=32, Nv=256, NG=1024 (seeded synthetic vertex, see
-sisi4s_gb300/inputs.py), MP2 start, DIIS with 5 vectors.  A step is one CCSD
-iteration (residual, Jacobi update, DIIS, energy).
+Workload (the headline system): No=32, Nv=256, NG=1024 from the seeded
+synthetic generator (sisi4s_gb300/inputs.py, seed 1), 12 iterations from the
+MP2 start with DiisMixer(5) and levelShift 16, then (T) on the amplitudes of
+the 12th iteration.  A step is one full CCSD iteration (residual, Jacobi
+update, DIIS, energy); the MP2-start iteration of each 12-iteration
+trajectory is part of its untimed set-up, so a trajectory holds 11 steps.
+K steps walk consecutive trajectories: when one ends the solver returns to
+the MP2 start (gbcc_ccsd_restart, untimed, keeping the resident integrals
+and captured graphs) and the next begins.  Each run of steps inside one
+trajectory is bracketed by a barrier and a device synchronisation, timed
+with CUDA events on the library stream, and the segment times are summed.
 
-  value      mixed-precision iterations/s (contractions emulated in FP64 on
-             the bf16 tensor cores; update, DIIS, energies in FP64), inputs
-             resident in HBM
-  fp64       the same iterations all in FP64 on the GPU, and dE between the
-             two energies after the same number of iterations
-  e2e        gbcc_ccsd_solve from host buffers (uploads, integral build,
-             iterations, amplitude download) in iterations/s
-  roofline   the dominant kernel (the tensor-core GEMM) timed live with CUDA
-             events on the library stream
+  value         precision-mode iterations/s (contractions emulated in FP64 on
+                the bf16 tensor cores; update, DIIS, energies in FP64),
+                inputs resident in HBM
+  energies      every reported energy states its error against the FP64
+                reference energies of this workload (the CPU oracle's 12
+                iterations and the FP64 (T), committed fixture)
+  fp64          the FP64 GPU path timed on the first full iteration of the
+                same trajectory, and its energy against the oracle's
+  e2e           gbcc_ccsd_solve from host buffers, as the reference's step
+                runs (upload, integrals, MP2 start + 11 iterations, amplitude
+                download), iterations/s over the same K steps
+  roofline      the dominant kernel (the tensor-core GEMM) timed live with
+                CUDA events on the library stream
   cpu_baseline  the CPU oracle (numpy restatement of the reference) on the
-             host cores, one full iteration of the same workload
+                host cores, one full iteration of the same workload
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 Under torchrun each rank runs an independent replica on its own GPU.
 """
 import argparse
 import json
+import math
 import os
 import subprocess
 import sys
@@ -31,11 +44,23 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-WORKLOAD = {"workload": "rccsd_no32_nv256_ng1024", "No": 32, "Nv": 256,
-            "NG": 1024, "seed": 1, "mixer": "DiisMixer", "maxResidua": 5}
+SYSTEM = {"No": 32, "Nv": 256, "NG": 1024, "seed": 1}
+SOLVE = {"mixer": "DiisMixer", "max_residua": 5, "level_shift": 16.0,
+         "max_iterations": 12, "energy_convergence": 0.0,
+         "amplitudes_convergence": 0.0}
+TRAJ = SOLVE["max_iterations"]          # iterations per trajectory (incl. MP2 start)
+WORKLOAD = {"workload": "rccsd_t_no32_nv256_ng1024", **SYSTEM,
+            "mixer": "DiisMixer", "maxResidua": 5, "levelShift": 16.0,
+            "maxIterations": TRAJ, "start": "MP2",
+            "steps_per_trajectory": TRAJ - 1}
 METRIC = "RCCSD iter/s mixed vs FP64 at |dE|<=1uHa; batched solves/s, p50/p99 latency"
 UNIT = "iter/s"
 REF_MAX_STEPS = 3
+FIXTURE = os.path.join(ROOT, "tests", "golden", "c2_trajectory.json")
+# DRAM bytes (read + write) per bf16 tensor flop of the emulated GEMM, from an
+# ncu capture of the same kernel (dram__bytes_read.sum + dram__bytes_write.sum
+# over 21 * 2 * 4096^3 flop at M = N = K = 4096 with 6 digits)
+EMU_GEMM_DRAM_PER_FLOP = (1.942e9 + 0.153e9) / (21 * 2.0 * 4096 ** 3)
 
 
 def _peaks():
@@ -126,6 +151,19 @@ def max_over_ranks(pg, v):
     return float(t.item())
 
 
+def load_fixture():
+    """FP64 reference energies of this workload, or None when the committed
+    fixture is missing or describes another workload."""
+    try:
+        with open(FIXTURE) as f:
+            doc = json.load(f)
+    except Exception:
+        return None
+    if doc.get("system") != SYSTEM or doc.get("solve") != SOLVE:
+        return None
+    return doc
+
+
 class CpuIterations:
     """CCSD iterations of the CPU oracle on one system (residual, update,
     DIIS, energy): the integrals and the MP2-start iteration are built once,
@@ -138,13 +176,14 @@ class CpuIterations:
         from oracle.mixers import DiisMixer
         import numpy as np
         self.sys = sys_
+        self.shift = SOLVE["level_shift"]
         self.ints = coulomb_integrals(sys_.gamma, sys_.No)
         self.d1, self.d2 = excitation_denominators(sys_.eps_h, sys_.eps_p)
         T1 = np.zeros((sys_.Nv, sys_.No))
         T2 = np.zeros((sys_.Nv, sys_.Nv, sys_.No, sys_.No))
-        self.mix = DiisMixer(5)
+        self.mix = DiisMixer(SOLVE["max_residua"])
         R1, R2 = residual(0, T1, T2, self.ints, sys_.gamma)
-        N1, N2 = update_amplitudes(R1, R2, T1, T2, self.d1, self.d2)
+        N1, N2 = update_amplitudes(R1, R2, T1, T2, self.d1, self.d2, self.shift)
         self.mix.append((N1, N2), (N1 - T1, N2 - T2))
         self.T1, self.T2 = self.mix.get()
         self.it = 1
@@ -154,12 +193,12 @@ class CpuIterations:
         t0 = time.perf_counter()
         T1, T2 = self.T1, self.T2
         R1, R2 = residual(self.it, T1, T2, self.ints, self.sys.gamma)
-        N1, N2 = update_amplitudes(R1, R2, T1, T2, self.d1, self.d2)
+        N1, N2 = update_amplitudes(R1, R2, T1, T2, self.d1, self.d2, self.shift)
         self.mix.append((N1, N2), (N1 - T1, N2 - T2))
         self.T1, self.T2 = self.mix.get()
-        energy(self.T1, self.T2, self.ints["PPHH"])
+        e = energy(self.T1, self.T2, self.ints["PPHH"])["value"]
         self.it += 1
-        return time.perf_counter() - t0
+        return time.perf_counter() - t0, e
 
 
 def pinned_copy(a):
@@ -176,9 +215,61 @@ def pinned_copy(a):
     return v, True
 
 
-def cpu_iteration_time(sys_, threads):
-    """One C2 iteration of the CPU oracle (residual, update, DIIS, energy)."""
-    return CpuIterations(sys_, threads).step()
+class Walker:
+    """Walks consecutive 12-iteration trajectories of one resident solver.
+    `done` counts iterations of the current trajectory (the MP2 start
+    included); a finished trajectory restarts from the MP2 start untimed."""
+
+    def __init__(self, sol, stream, pg):
+        self.sol, self.stream, self.pg = sol, stream, pg
+        self.done = 0
+        self.segments = 0
+        self.last_energy = None
+
+    def _begin(self):
+        self.sol.restart()
+        self.sol.step(1)          # MP2 start: set-up of the trajectory
+        self.done = 1
+
+    def walk(self, n, timed):
+        import torch
+        ms = 0.0
+        left = n
+        while left > 0:
+            if self.done in (0, TRAJ):
+                self._begin()
+            m = min(left, TRAJ - self.done)
+            if timed:
+                barrier(self.pg)
+                torch.cuda.synchronize()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(self.stream)
+                self.last_energy, _ = self.sol.step(m)
+                e1.record(self.stream)
+                torch.cuda.synchronize()
+                barrier(self.pg)
+                ms += e0.elapsed_time(e1)
+                self.segments += 1
+            else:
+                self.last_energy, _ = self.sol.step(m)
+            self.done += m
+            left -= m
+        return ms
+
+    def finish(self):
+        """Completes the current trajectory (untimed); returns its per-
+        iteration energies."""
+        if self.done == 0:
+            self._begin()
+        if self.done < TRAJ:
+            self.sol.step(TRAJ - self.done)
+            self.done = TRAJ
+        return list(self.sol.result(amplitudes=False)["history"])
+
+
+def _err(ex):
+    return "%s: %s" % (type(ex).__name__, ex)
 
 
 SERVE_OPTS = dict(mixer="DiisMixer", max_residua=5, max_iterations=100,
@@ -189,8 +280,8 @@ def serve_measure(args):
     """CCSD(T) serving on samples of the request stream (No ~ U{4..16},
     Nv log-uniform in [20, 160], NG = 4 Nv, request r seeded with r, the C1
     convergence settings): one-at-a-time FP64 and mixed on the first
-    `serve_single` requests, and batched mixed with `serve_slots` concurrent
-    solves on the first `serve_requests`, all submitted at t = 0 (saturated)."""
+    `serve_single` requests, and batched with `serve_slots` concurrent
+    solves on the first `serve_requests`."""
     from sisi4s_gb300 import serve
     reqs = serve.make_requests(max(args.serve_requests, args.serve_single))
     out = {"requests": args.serve_requests, "slots": args.serve_slots,
@@ -203,7 +294,8 @@ def serve_measure(args):
         srv.close()
         st = serve.latency_stats(recs, wall)
         out["one_at_a_time_" + prec] = {"requests": args.serve_single,
-                                        "solves_per_s": st["solves_per_s"]}
+                                        "solves_per_s": st["solves_per_s"],
+                                        "ok_solves_per_s": st["ok_solves_per_s"]}
     lam = args.serve_lambda if args.serve_lambda > 0 else None
     srv = serve.Server(slots=args.serve_slots)
     recs, wall = serve.run_stream(srv, reqs[:args.serve_requests], lam=lam,
@@ -212,8 +304,6 @@ def serve_measure(args):
     st = serve.latency_stats(recs, wall)
     st["arrivals"] = ("Poisson, rate %g /s (seed 0)" % lam) if lam else "all at t = 0"
     out["batched_" + args.serve_precision] = st
-    out["status_counts"] = {str(k): sum(1 for r in recs if r["status"] == k)
-                            for k in sorted(set(r["status"] for r in recs))}
     out["batched_over_fp64_one_at_a_time"] = (
         st["solves_per_s"] / out["one_at_a_time_fp64"]["solves_per_s"])
     out["batched_precision"] = args.serve_precision
@@ -222,20 +312,20 @@ def serve_measure(args):
 
 def run_reference(args, ws, rank, pg):
     """The reference's math on the host cores: the oracle restatement (the
-    reference's CTF build cannot be built here), one C2 iteration per step."""
+    reference's CTF build cannot be built here), one full iteration of the
+    same workload per step."""
     if rank != 0:
         return
     from sisi4s_gb300.inputs import make_system
     threads = os.cpu_count() or 1
-    s = make_system(WORKLOAD["No"], WORKLOAD["Nv"], WORKLOAD["NG"], WORKLOAD["seed"])
+    s = make_system(**SYSTEM)
     # the integrals and the MP2-start iteration are built once, untimed (this
-    # also warms the BLAS thread pool); each step times the next full CCSD
-    # iteration, so the run stays within a few minutes for small K
-    # at most REF_MAX_STEPS iterations are timed (about a minute each on 16
-    # Grace cores), so that the arm ends within a few minutes for any K
+    # also warms the BLAS thread pool); at most REF_MAX_STEPS iterations are
+    # timed (about a minute each on 16 Grace cores), so that the arm ends
+    # within a few minutes for any K
     its = CpuIterations(s, threads)
     n = max(1, min(args.steps, REF_MAX_STEPS))
-    times = [its.step() for _ in range(n)]
+    times = [its.step()[0] for _ in range(n)]
     t = sum(times)
     v = n / t
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT,
@@ -259,13 +349,14 @@ def run_reference(args, ws, rank, pg):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=2)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gbcc", choices=["gbcc", "reference"])
     ap.add_argument("--slices", type=int, default=6)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=32)
     ap.add_argument("--serve-single", type=int, default=4)
     ap.add_argument("--serve-slots", type=int, default=8)
@@ -277,16 +368,13 @@ def main():
     ap.add_argument("--serve-only", action="store_true",
                     help="run only the serving measurement (one JSON line)")
     ap.add_argument("--no-triples", action="store_true",
-                    help="skip the (T) correction on the final amplitudes")
-    ap.add_argument("--triples-fp64", action="store_true",
-                    help="also run the FP64 (T) for dE_(T) (minutes at the default size)")
+                    help="skip the (T) correction on the 12th-iteration amplitudes")
     args = ap.parse_args()
     ws, rank, local, pg = dist_init()
     if args.impl == "reference":
         run_reference(args, ws, rank, pg)
         return
 
-    import numpy as np
     import torch
     from sisi4s_gb300 import capi
     from sisi4s_gb300 import ccsd as gpu
@@ -297,156 +385,197 @@ def main():
         if rank == 0:
             print(json.dumps({"metric": METRIC, "serving": serve_measure(args)}), flush=True)
         return
-    W = WORKLOAD
-    s = make_system(W["No"], W["Nv"], W["NG"], W["seed"])
+    s = make_system(**SYSTEM)
+    fx = load_fixture()
     ctx = capi.Context(local)
     ctx.set_emulation(args.slices, 1e7)
     stream = torch.cuda.ExternalStream(ctx.stream)
-    total_it = args.warmup + args.steps
-    kw = dict(mixer=W["mixer"], max_residua=W["maxResidua"],
-              max_iterations=total_it + 1, energy_convergence=0.0,
-              amplitudes_convergence=0.0)
+    errors = {}
 
-    # ---- mixed precision, inputs resident (steady-state iterations replay
-    # captured CUDA graphs)
-    sol = gpu.Solver(ctx, s.eps_h, s.eps_p, s.gamma, precision="emu",
-                     **dict(kw, max_iterations=total_it + 2))
-    sol.step(args.warmup)
-    barrier(pg)
-    torch.cuda.synchronize()
+    # ---- precision mode, inputs resident.  One untimed trajectory captures
+    # the steady-state iteration graphs (one per DIIS ring position).
+    sol = gpu.Solver(ctx, s.eps_h, s.eps_p, s.gamma, precision="emu", **SOLVE)
+    sol.step(TRAJ)
+    walker = Walker(sol, stream, pg)
+    walker.walk(args.warmup, timed=False)
     l0 = ctx.launches
     f0 = ctx.flops
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
-        e0.record(stream)
-        e_mixed, _ = sol.step(args.steps)
-        e1.record(stream)
-        torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
-    barrier(pg)
+        ms = walker.walk(args.steps, timed=True)
     ms = max_over_ranks(pg, ms)
     launches = ctx.launches - l0
     fl = ctx.flops - f0
-    # roofline of the dominant kernel: two more (untimed) steps with CUDA
-    # events around every tensor-core GEMM launch (graphs off while profiling)
-    ctx.profile(True)
-    p0 = torch.cuda.Event(enable_timing=True)
-    p1 = torch.cuda.Event(enable_timing=True)
-    p0.record(stream)
-    sol.step(2)
-    p1.record(stream)
-    torch.cuda.synchronize()
-    ctx.profile(False)
-    prof_ms = p0.elapsed_time(p1)
-    gs = ctx.gemm_stats()
-
-    # ---- (T) on the final amplitudes: precision mode, optionally FP64
-    triples = None
-    if not args.no_triples:
-        No = W["No"]
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        e_t, _ = sol.triples("emu")
-        t_emu = time.perf_counter() - t0
-        triples = {"seconds": t_emu, "e_t": e_t,
-                   "hole_triples": No * (No + 1) * (No + 2) // 6,
-                   "precision": "emulated fp64 GEMMs (%d bf16 digits), float-float "
-                                "epilogue" % min(8, args.slices + 1),
-                   "amplitudes": "after %d iterations" % (total_it + 2)}
-        if args.triples_fp64:
-            t0 = time.perf_counter()
-            e_t64, _ = sol.triples("fp64")
-            t64 = time.perf_counter() - t0
-            triples.update(fp64_seconds=t64, e_t_fp64=e_t64, dE_t_ha=e_t - e_t64,
-                           speedup=t64 / t_emu)
-    sol.close()
     value = ws * args.steps / (ms / 1e3)
 
-    # ---- FP64 on the GPU, same iterations (for dE and the speed-up)
+    # ---- energies of one full trajectory and (T) on its 12th amplitudes,
+    # each stated against the FP64 reference energies of this workload
+    energies = {"reference": None}
+    triples = None
+    hist = walker.finish()
+    e12 = hist[-1]
+    energies["e_ccsd"] = e12
+    energies["iterations"] = len(hist)
+    if fx is not None and "oracle" in fx:
+        ref = [r["energy"] for r in fx["oracle"]["energies"]]
+        d = [a - b for a, b in zip(hist, ref)]
+        energies.update(reference="CPU oracle (numpy restatement), FP64, 12 iterations",
+                        e_ccsd_fp64=ref[-1], dE_ccsd_ha=d[-1],
+                        max_abs_dE_ccsd_ha_over_iterations=max(abs(x) for x in d))
+    if not args.no_triples:
+        try:
+            torch.cuda.synchronize()
+            t0 = torch.cuda.Event(enable_timing=True)
+            t1 = torch.cuda.Event(enable_timing=True)
+            t0.record(stream)
+            e_t, _ = sol.triples("emu")
+            t1.record(stream)
+            torch.cuda.synchronize()
+            No, Nv, NG = SYSTEM["No"], SYSTEM["Nv"], SYSTEM["NG"]
+            f_t = 2.0 * No ** 3 * Nv ** 4 + 2.0 * No ** 4 * Nv ** 3 + 2.0 * NG * No * Nv ** 3
+            sec = t0.elapsed_time(t1) / 1e3
+            triples = {"seconds": sec, "e_t": e_t, "e_ccsd_t": e12 + e_t,
+                       "hole_triples": No * (No + 1) * (No + 2) // 6,
+                       "fp64_equiv_tflops": f_t / sec / 1e12,
+                       "precision": "emulated fp64 GEMMs (%d bf16 digits), float-float "
+                                    "epilogue" % min(8, args.slices + 1),
+                       "amplitudes": "after the 12th iteration"}
+            if fx is not None and "gpu_fp64" in fx:
+                g = fx["gpu_fp64"]
+                triples.update(e_t_fp64=g["e_t"], dE_t_ha=e_t - g["e_t"],
+                               fp64_seconds=g.get("seconds_triples"))
+                if energies.get("e_ccsd_fp64") is not None:
+                    energies["dE_ccsd_t_ha"] = (e12 + e_t) - (energies["e_ccsd_fp64"] + g["e_t"])
+        except Exception as ex:  # noqa: BLE001
+            errors["triples"] = _err(ex)
+
+    # ---- roofline of the dominant kernel: two more iterations of a fresh
+    # trajectory (eager, profiling on) with CUDA events around every
+    # tensor-core GEMM launch
+    gs, prof_ms = None, None
+    try:
+        sol.restart()
+        sol.step(1)
+        ctx.profile(True)
+        p0 = torch.cuda.Event(enable_timing=True)
+        p1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        p0.record(stream)
+        sol.step(2)
+        p1.record(stream)
+        torch.cuda.synchronize()
+        ctx.profile(False)
+        prof_ms = p0.elapsed_time(p1)
+        gs = ctx.gemm_stats()
+    except Exception as ex:  # noqa: BLE001
+        errors["profile"] = _err(ex)
+        ctx.profile(False)
+    sol.close()
+
+    # ---- FP64 on the GPU: the first full iteration of the same trajectory
     fp64 = None
     if not args.no_fp64:
-        solf = gpu.Solver(ctx, s.eps_h, s.eps_p, s.gamma, precision="fp64", **kw)
-        solf.step(args.warmup + args.steps - 1)
-        torch.cuda.synchronize()
-        f0e = torch.cuda.Event(enable_timing=True)
-        f1e = torch.cuda.Event(enable_timing=True)
-        f0e.record(stream)
-        e_fp64, _ = solf.step(1)
-        f1e.record(stream)
-        torch.cuda.synchronize()
-        solf.close()
-        fms = f0e.elapsed_time(f1e)
-        fp64 = {"iter_per_s": 1e3 / fms, "energy": e_fp64,
-                "energy_mixed": e_mixed, "dE_ha": e_mixed - e_fp64,
-                "dE_rel": (e_mixed - e_fp64) / abs(e_fp64) if e_fp64 else None,
-                "mixed_over_fp64": (1e3 / (ms / args.steps)) / (1e3 / fms),
-                "iterations_compared": total_it}
+        try:
+            solf = gpu.Solver(ctx, s.eps_h, s.eps_p, s.gamma, precision="fp64", **SOLVE)
+            solf.step(1)
+            torch.cuda.synchronize()
+            f0e = torch.cuda.Event(enable_timing=True)
+            f1e = torch.cuda.Event(enable_timing=True)
+            f0e.record(stream)
+            e_fp64, _ = solf.step(1)
+            f1e.record(stream)
+            torch.cuda.synchronize()
+            solf.close()
+            fms = f0e.elapsed_time(f1e)
+            fp64 = {"iter_per_s": 1e3 / fms, "iterations_timed": 1,
+                    "energy_iteration_2": e_fp64,
+                    "mixed_over_fp64": value / ws / (1e3 / fms)}
+            if len(hist) >= 2:
+                fp64["dE_mixed_vs_fp64_iteration_2_ha"] = hist[1] - e_fp64
+            if fx is not None and "oracle" in fx:
+                fp64["dE_fp64_vs_oracle_iteration_2_ha"] = (
+                    e_fp64 - fx["oracle"]["energies"][1]["energy"])
+            if fx is not None and "gpu_fp64" in fx:
+                g = fx["gpu_fp64"]
+                fp64["trajectory_12_iterations_recorded"] = {
+                    "e_ccsd": g["energies"][-1], "e_t": g["e_t"],
+                    "seconds_ccsd": g.get("seconds_ccsd"),
+                    "seconds_triples": g.get("seconds_triples")}
+        except Exception as ex:  # noqa: BLE001
+            errors["fp64"] = _err(ex)
 
-    # ---- end to end through the C ABI from host buffers
-    # start from given amplitudes (the MP2 amplitudes) so that every timed
-    # iteration is a full CCSD iteration, as in the resident measurement
-    from sisi4s_gb300.inputs import mp2_amplitudes
-    t1_0, t2_0 = mp2_amplitudes(s)
-    # the large inputs (vertex, starting doubles) are staged in page-locked
-    # host memory before the clock starts; the column-major views pass
-    # through the Python API without a copy
-    g_host, g_pin = pinned_copy(s.gamma)
-    t2_host, t2_pin = pinned_copy(t2_0)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    r = gpu.ccsd_solve(ctx, s.eps_h, s.eps_p, g_host, precision="emu",
-                       initial=(t1_0, t2_host), **dict(kw, max_iterations=args.steps))
-    e2e_s = time.perf_counter() - t0
-    del g_host, t2_host  # hand the page-locked staging back
-    Np = W["No"] + W["Nv"]
-    n2 = W["Nv"] ** 2 * W["No"] ** 2
-    h2d = 8 * (W["NG"] * Np * Np + W["No"] + W["Nv"] + W["Nv"] * W["No"] + n2)
-    d2h = 8 * (W["Nv"] * W["No"] + n2) + 8 * 4
-    e2e = {"value": ws * r["iterations"] / e2e_s, "unit": UNIT,
-           "h2d_bytes_per_step": h2d // args.steps,
-           "d2h_bytes_per_step": d2h // args.steps,
-           "host_inputs": "pinned" if (g_pin and t2_pin) else "pageable",
-           "note": "one gbcc_ccsd_solve of %d full iterations from host "
-                   "buffers (vertex, eigenvalues and starting amplitudes "
-                   "uploaded, integrals built, amplitudes downloaded inside); "
-                   "bytes per iteration" % args.steps}
+    # ---- end to end through the C ABI from host buffers: the reference's
+    # step (MP2 start + 11 iterations per solve), as many solves as it takes
+    # to cover the K steps; the vertex is staged in page-locked memory first
+    e2e = None
+    if not args.no_e2e:
+        try:
+            g_host, g_pin = pinned_copy(s.gamma)
+            n_solves = math.ceil(args.steps / (TRAJ - 1))
+            wall = 0.0
+            done = 0
+            h2d = d2h = 0
+            No, Nv, NG = SYSTEM["No"], SYSTEM["Nv"], SYSTEM["NG"]
+            Np = No + Nv
+            for k in range(n_solves):
+                n = min(TRAJ - 1, args.steps - done)
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                r = gpu.ccsd_solve(ctx, s.eps_h, s.eps_p, g_host, precision="emu",
+                                   **dict(SOLVE, max_iterations=n + 1))
+                wall += time.perf_counter() - t0
+                done += r["iterations"] - 1
+                h2d += 8 * (NG * Np * Np + No + Nv)
+                d2h += 8 * (Nv * No + Nv * Nv * No * No) + 8 * (n + 1)
+            del g_host
+            e2e = {"value": ws * done / wall, "unit": UNIT,
+                   "h2d_bytes_per_step": h2d // max(done, 1),
+                   "d2h_bytes_per_step": d2h // max(done, 1),
+                   "host_inputs": "pinned" if g_pin else "pageable",
+                   "solves": n_solves,
+                   "note": "gbcc_ccsd_solve from host buffers per solve (vertex and "
+                           "eigenvalues uploaded, integrals built, MP2 start + "
+                           "iterations, amplitudes downloaded), %d full iterations "
+                           "in %d solves; bytes per full iteration" % (done, n_solves)}
+        except Exception as ex:  # noqa: BLE001
+            errors["e2e"] = _err(ex)
 
     peaks, pk = _peaks()
-    achieved = gs["tc_flops"] / (gs["ms"] / 1e3) / 1e12 if gs["ms"] > 0 else None
-    peak = peaks.get("bf16_tflops")
-    roof = {"kernel": "emu_gemm_kernel<%d> (tcgen05 kind::f16)" % args.slices,
-            "bound": "tensor", "achieved": achieved, "peak": peak,
-            "unit": "TFLOP/s", "frac": achieved / peak if achieved else None,
-            "peak_source": pk + " bf16 burst (MEASURED_PEAKS.json)",
-            "launches": gs["launches"],
-            "avg_launch_ms": gs["ms"] / max(gs["launches"], 1),
-            "fp64_equiv_tflops": gs["fp64_flops"] / (gs["ms"] / 1e3) / 1e12 if gs["ms"] else None,
-            "gemm_share_of_step": gs["ms"] / prof_ms if prof_ms else None}
-    # DRAM traffic per launch: the ncu capture of the same kernel at M=N=K=4096
-    # (profiles/emu_gemm_4096.md: dram read + write = 1.942 + 0.153 GB for
-    # 21 * 2 * 4096^3 bf16 flop), scaled to this run's average launch by its
-    # algorithmic work (the panel re-reads grow with M*N*K for fixed tiles)
-    if gs["launches"]:
-        per_flop = (1.942e9 + 0.153e9) / (21 * 2.0 * 4096 ** 3)
-        roof["traffic"] = per_flop * gs["tc_flops"] / gs["launches"]
-        roof["traffic_unit"] = "bytes per launch"
-        roof["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum at "
-                                  "4096^3, scaled by work per launch")
-    else:
-        roof["traffic"] = None
+    roof = None
+    if gs is not None and gs["ms"] > 0:
+        achieved = gs["tc_flops"] / (gs["ms"] / 1e3) / 1e12
+        peak = peaks.get("bf16_tflops")
+        roof = {"kernel": "emu_gemm_kernel<%d> (tcgen05 kind::f16)" % args.slices,
+                "bound": "tensor", "achieved": achieved, "peak": peak,
+                "unit": "TFLOP/s", "frac": achieved / peak,
+                "peak_source": pk + " bf16 burst (MEASURED_PEAKS.json)",
+                "launches": gs["launches"],
+                "avg_launch_ms": gs["ms"] / max(gs["launches"], 1),
+                "fp64_equiv_tflops": gs["fp64_flops"] / (gs["ms"] / 1e3) / 1e12,
+                "gemm_share_of_step": gs["ms"] / prof_ms if prof_ms else None,
+                "traffic": EMU_GEMM_DRAM_PER_FLOP * gs["tc_flops"] / gs["launches"],
+                "traffic_unit": "bytes per launch",
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum at "
+                                  "M = N = K = 4096, scaled by work per launch"}
 
     serving = None
     if not args.no_serve:
-        serving = serve_measure(args)
+        try:
+            serving = serve_measure(args)
+        except Exception as ex:  # noqa: BLE001
+            errors["serving"] = _err(ex)
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
-        threads = os.cpu_count() or 1
-        ct = cpu_iteration_time(s, threads)
-        cpu = {"value": 1.0 / ct, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": "one full CCSD iteration (residual, update, DIIS, "
-                         "energy) of the numpy restatement on this workload"}
+        try:
+            threads = os.cpu_count() or 1
+            ct, ce = CpuIterations(s, threads).step()
+            cpu = {"value": 1.0 / ct, "unit": UNIT, "cores": threads, "kind": "port",
+                   "sample": "one full CCSD iteration (residual, update, DIIS, "
+                             "energy) of the numpy restatement on this workload: the "
+                             "first after the MP2 start",
+                   "energy": ce}
+        except Exception as ex:  # noqa: BLE001
+            errors["cpu_baseline"] = _err(ex)
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
@@ -454,14 +583,17 @@ def main():
                 "ms_per_step": ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                 "data": "synthetic",
-                "config": dict(W, parallelism="replicas" if ws > 1 else "single",
+                "config": dict(WORKLOAD, parallelism="replicas" if ws > 1 else "single",
                                precision="emulated fp64, %d bf16 digits" % args.slices,
-                               l2="inputs larger than L2 (T2, V, Gamma >= 0.5 GB)"),
-                "fp64": fp64, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
-                "serving": serving, "triples": triples,
+                               l2="inputs larger than L2 (T2, V, Gamma >= 0.5 GB)",
+                               timed_segments=walker.segments),
+                "energies": energies, "fp64": fp64, "e2e": e2e, "roofline": roof,
+                "cpu_baseline": cpu, "serving": serving, "triples": triples,
                 "gpu_launches": launches,
-                "fp64_equiv_tflops_per_step": fl / args.steps / (ms / args.steps / 1e3) / 1e12,
+                "fp64_equiv_tflops_per_step": fl / (ms / 1e3) / 1e12,
                 "clocks": clk.summary()}
+        if errors:
+            line["errors"] = errors
         print(json.dumps(line), flush=True)
     ctx.close()
     if pg is not None:

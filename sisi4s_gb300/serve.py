@@ -161,8 +161,24 @@ def run_stream(server, systems, lam=None, seed=0, triples=True, **opts):
 
 
 def latency_stats(recs, wall):
+    """Throughput and arrival-to-result latency of a stream.  Requests that
+    ended with an error status (a singular DIIS matrix, divergence) or
+    without converging are served requests too, so ``solves_per_s`` counts
+    every one; ``ok_*`` count and time the converged solves (status 0)
+    alone, and ``status_counts`` gives the split."""
     lat = np.array([r["latency"] for r in recs])
-    return {"solves": len(recs), "solves_per_s": len(recs) / wall,
-            "p50_s": float(np.percentile(lat, 50)),
-            "p99_s": float(np.percentile(lat, 99)),
-            "mean_s": float(lat.mean()), "wall_s": wall}
+    ok = np.array([r["latency"] for r in recs if r["status"] == capi.OK])
+    counts = {}
+    for r in recs:
+        counts[capi.status_string(r["status"])] = counts.get(
+            capi.status_string(r["status"]), 0) + 1
+    out = {"solves": len(recs), "solves_per_s": len(recs) / wall,
+           "p50_s": float(np.percentile(lat, 50)),
+           "p99_s": float(np.percentile(lat, 99)),
+           "mean_s": float(lat.mean()), "wall_s": wall,
+           "status_counts": counts, "ok_solves": int(ok.size),
+           "ok_solves_per_s": ok.size / wall}
+    if ok.size:
+        out.update(ok_p50_s=float(np.percentile(ok, 50)),
+                   ok_p99_s=float(np.percentile(ok, 99)))
+    return out
