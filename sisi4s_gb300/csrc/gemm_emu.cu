@@ -1135,15 +1135,19 @@ void gemm_emu(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
 // panels of both operands and the error word) in one file-scope device array
 // of fixed size instead of stream-ordered allocations.
 //
-// Limits and sharing: the array holds GBCC_NOALLOC_SCRATCH_BYTES (32 MiB);
-// every GPU that loads the library holds it until the process exits.  Every
-// call on a device uses the same array and it keeps the previous call's
-// contents; the error word is cleared at the start of each call and all
-// other scratch is fully rewritten before it is read.  Calls whose work
-// overlaps on the GPU (two streams, or two host threads) race on the array
-// and must be ordered by the caller.  The device address of the array is
-// looked up once per device, on the first call made with that device
-// current; that first call should therefore come before any stream capture.
+// Limits and sharing: the array holds NOALLOC_SCRATCH_BYTES (32 MiB); every
+// GPU that runs the library's kernels holds it until the process exits (with
+// lazy module loading, from the first use on that GPU).  Every call on a
+// device uses the same array and it keeps the previous call's contents; the
+// error word is cleared at the start of each call and all other scratch is
+// fully rewritten before it is read.  Calls whose work overlaps on the GPU
+// (two streams, or two host threads) race on the array and must be ordered
+// by the caller.  Each call reads the kernel's error word back, so it returns
+// only when its GEMM has finished.  The device address of the array is looked
+// up once per device, on the first call made with that device current, and
+// kept for the life of the process: that first call should come before any
+// stream capture, and a device reset (cudaDeviceReset) makes the kept address
+// stale, so the entry point is not for use after one.
 namespace gbcc {
 namespace {
 

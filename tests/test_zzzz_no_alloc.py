@@ -2,7 +2,8 @@
 
 gbcc_dgemm_emu_noalloc serves callers that cannot let the library allocate
 device memory (their own arena already holds the HBM budget, or their hot
-loop must stay out of the CUDA allocator).  It must give the same result as
+loop must stay out of the CUDA allocator, whose latency they do not
+control).  It must give the same result as
 the allocating emulated GEMM (gbcc_dgemm with GBCC_PREC_EMU), also on a second
 call right after the first, when the shared scratch array still holds the
 first call's data.  This file is collected last on purpose, so that a failure
