@@ -1,6 +1,6 @@
 """Complex (k-point) CCSD(T) on one seeded synthetic complex system.
 
-    python -m sisi4s_gb300.complex_bench No Nv NG [--iterations N] [--no-triples]
+    python -m benchmarks.complex_bench No Nv NG [--iterations N] [--no-triples]
 
 The vertex is the seeded real synthetic one with its rows mixed by a random
 unitary and random orbital phases, so every quantity is genuinely complex.
@@ -18,7 +18,7 @@ import numpy as np
 
 
 def complex_system(No, Nv, NG, seed):
-    from .inputs import make_system
+    from sisi4s_gb300.inputs import make_system
     s = make_system(No, Nv, NG, seed)
     rng = np.random.default_rng(seed + 1000)
     W, _ = np.linalg.qr(rng.normal(size=(NG, NG)) + 1j * rng.normal(size=(NG, NG)))
@@ -28,7 +28,7 @@ def complex_system(No, Nv, NG, seed):
 
 
 def run(ctx, eh, ep, g, precision, iterations, triples):
-    from . import ccsd as gpu
+    from sisi4s_gb300 import ccsd as gpu
     kw = dict(max_iterations=iterations, energy_convergence=0.0, amplitudes_convergence=0.0,
               precision=precision)
     t0 = time.perf_counter()
@@ -55,7 +55,7 @@ def main():
     ap.add_argument("--seed", type=int, default=1)
     args = ap.parse_args()
 
-    from . import capi
+    from sisi4s_gb300 import capi
 
     eh, ep, g = complex_system(args.No, args.Nv, args.NG, args.seed)
     ctx = capi.Context(0)

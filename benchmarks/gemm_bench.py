@@ -1,6 +1,6 @@
 """Throughput of the library's GEMMs (FP64 and emulated FP64) on one GPU.
 
-  python -m sisi4s_gb300.gemm_bench M N K [--prec emu|fp64] [--slices S] [--reps R]
+  python -m benchmarks.gemm_bench M N K [--prec emu|fp64] [--slices S] [--reps R]
 
 Operands are random FP64 device buffers (column-major); timing uses CUDA
 events on the library stream after one warm-up launch.
@@ -19,7 +19,7 @@ def main():
     ap.add_argument("--reps", type=int, default=3)
     args = ap.parse_args()
     import torch
-    from . import capi
+    from sisi4s_gb300 import capi
     ctx = capi.Context(0)
     ctx.set_emulation(args.slices, 0.0)
     M, N, K = args.M, args.N, args.K

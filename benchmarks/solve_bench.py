@@ -1,6 +1,6 @@
 """Mixed vs FP64 CCSD(T) on one seeded synthetic system.
 
-    python -m sisi4s_gb300.solve_bench No Nv NG [--iterations N] [--no-triples]
+    python -m benchmarks.solve_bench No Nv NG [--iterations N] [--no-triples]
         [--formulation vertex|stored]
 
 Runs N CCSD iterations (DIIS with 5 vectors, MP2 start) in precision mode and
@@ -15,7 +15,7 @@ import time
 
 
 def run(ctx, s, precision, iterations, triples, triples_fp64=False, formulation="vertex"):
-    from . import ccsd as gpu
+    from sisi4s_gb300 import ccsd as gpu
 
     sol = gpu.Solver(ctx, s.eps_h, s.eps_p, s.gamma, mixer="DiisMixer", max_residua=5,
                      max_iterations=iterations + 1, energy_convergence=0.0,
@@ -63,8 +63,8 @@ def main():
                          "CcsdEnergyFromCoulombIntegralsReference (resident Vabcd)")
     args = ap.parse_args()
 
-    from . import capi
-    from .inputs import make_system
+    from sisi4s_gb300 import capi
+    from sisi4s_gb300.inputs import make_system
 
     s = make_system(args.No, args.Nv, args.NG, args.seed)
     ctx = capi.Context(0)

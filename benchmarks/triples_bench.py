@@ -1,6 +1,6 @@
 """Times one (T) evaluation on a seeded synthetic system.
 
-    python -m sisi4s_gb300.triples_bench No Nv NG [--prec emu|fp64] [--reps R]
+    python -m benchmarks.triples_bench No Nv NG [--prec emu|fp64] [--reps R]
 
 The amplitudes are the MP2 amplitudes of the system (T1 = 0) plus a small
 seeded T1, so that every term of the (T) energy is exercised.  Prints one JSON
@@ -25,9 +25,9 @@ def main():
 
     import torch  # device synchronisation only
 
-    from . import capi
-    from . import ccsd as gpu
-    from .inputs import make_system, mp2_amplitudes
+    from sisi4s_gb300 import capi
+    from sisi4s_gb300 import ccsd as gpu
+    from sisi4s_gb300.inputs import make_system, mp2_amplitudes
 
     s = make_system(args.No, args.Nv, args.NG, args.seed)
     T1, T2 = mp2_amplitudes(s)

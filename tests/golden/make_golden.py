@@ -10,7 +10,7 @@
 * ``oracle_cases.json``: the oracle's energies on the seeded systems of
   ``cases.py``.
 
-    python tests/golden/make_golden.py [--reference SISI4S_TREE] [--oracle-only]
+    python tests/golden/make_golden.py --reference SISI4S_TREE [--oracle-only]
 """
 import argparse
 import json
@@ -133,12 +133,15 @@ def oracle_fixture():
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference",
-                    help="sisi4s source tree holding the integration tests")
+    ap.add_argument("--reference", default=os.environ.get("SISI4S_SOURCE"),
+                    help="sisi4s source tree holding the integration tests "
+                         "(default: $SISI4S_SOURCE); not needed with --oracle-only")
     ap.add_argument("--oracle-only", action="store_true")
     args = ap.parse_args()
     from tests.golden import cases
     if not args.oracle_only:
+        if not args.reference:
+            ap.error("--reference (or SISI4S_SOURCE) is required unless --oracle-only")
         with open(cases.UEG_FILE, "w") as f:
             json.dump(ueg_fixture(args.reference), f, indent=1)
             f.write("\n")

@@ -178,7 +178,7 @@ def test_measurement_scripts_run_on_the_simulation(sim_env, module, argv):
     code = ("import os, sys, runpy; from sisi4s_gb300 import capi; "
             "capi.load(os.environ['GBCC_SIM_LIB']); "
             "sys.argv = [%r] + %r; "
-            "runpy.run_module('sisi4s_gb300.%s', run_name='__main__')" % (module, argv, module))
+            "runpy.run_module('benchmarks.%s', run_name='__main__')" % (module, argv, module))
     r = subprocess.run([sys.executable, "-c", code], cwd=ROOT, env=sim_env,
                        capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout + r.stderr
