@@ -34,6 +34,20 @@ COMPLEX = {"No": 3, "Nv": 9, "NG": 14, "seed": 6}
 COMPLEX_SOLVE = {"mixing_ratio": 1.0, "max_iterations": 10, "energy_convergence": 0.0,
                  "amplitudes_convergence": 0.0, "slice_size": 2}
 
+#: the headline workload: No=32, Nv=256, NG=1024 from seed 1, 12 iterations
+#: from the MP2 start with DIIS(5) and a level shift of 16 Ha.  On this
+#: generator the reference's default LinearMixer overflows within a few
+#: iterations, and DIIS without a shift wanders chaotically (|E| ~ 1e6 Ha by
+#: iteration 11, where two arithmetics differing at 1e-13 per step end up
+#: 1e-4 Ha apart); the shift keeps the 12 iterations well conditioned, so an
+#: energy difference between two arithmetics measures their own error.
+C2 = {"No": 32, "Nv": 256, "NG": 1024, "seed": 1}
+C2_SOLVE = {"mixer": "DiisMixer", "max_residua": 5, "level_shift": 16.0,
+            "max_iterations": 12, "energy_convergence": 0.0,
+            "amplitudes_convergence": 0.0}
+#: FP64 energies of C2 (oracle trajectory, FP64 (T)); see make_c2_fixture.py
+C2_FILE = os.path.join(HERE, "c2_trajectory.json")
+
 
 def real_system():
     return make_system(**REAL)

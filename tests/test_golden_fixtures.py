@@ -108,3 +108,28 @@ def test_oracle_reproduces_the_complex_case(fx):
     assert _close(et, cases.complex_list([f["triples"]])[0], 1e-11)
     # the vertex is a unitary rotation of a real one: the energies are real
     assert np.abs(cases.complex_list(f["history"]).imag).max() < 1e-15
+
+
+def test_c2_fixture_first_iteration_from_the_oracle():
+    """The headline workload's fixture (c2_trajectory.json): its first
+    energy is the MP2-start iteration with the level shift, T2 = -V/(D + s)
+    (update_amplitudes with T = 0; a one-vector DIIS returns the estimate),
+    recomputed here from the generator in a few seconds; and its FP64 GPU
+    trajectory follows the oracle's."""
+    from oracle.ccsd import energy, excitation_denominators
+    from sisi4s_gb300.inputs import make_system
+    doc = cases.load(cases.C2_FILE)
+    assert doc["system"] == cases.C2 and doc["solve"] == cases.C2_SOLVE
+    s = make_system(**cases.C2)
+    gai = np.ascontiguousarray(s.gamma[:, s.No:, :s.No])
+    NG, Nv, No = gai.shape
+    g2 = gai.reshape(NG, Nv * No)
+    V = (g2.T @ g2).reshape(Nv, No, Nv, No).transpose(0, 2, 1, 3)
+    _, d2 = excitation_denominators(s.eps_h, s.eps_p)
+    T2 = -V / (d2 + cases.C2_SOLVE["level_shift"])
+    e = energy(np.zeros((Nv, No)), T2, V)["value"]
+    ref = doc["oracle"]["energies"]
+    assert len(ref) == cases.C2_SOLVE["max_iterations"]
+    assert abs(e - ref[0]["energy"]) < 1e-8
+    fp = doc["gpu_fp64"]["energies"]
+    assert max(abs(a - b["energy"]) for a, b in zip(fp, ref)) <= 1e-8
