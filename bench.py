@@ -44,15 +44,29 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-SYSTEM = {"No": 32, "Nv": 256, "NG": 1024, "seed": 1}
 SOLVE = {"mixer": "DiisMixer", "max_residua": 5, "level_shift": 16.0,
          "max_iterations": 12, "energy_convergence": 0.0,
          "amplitudes_convergence": 0.0}
 TRAJ = SOLVE["max_iterations"]          # iterations per trajectory (incl. MP2 start)
-WORKLOAD = {"workload": "rccsd_t_no32_nv256_ng1024", **SYSTEM,
-            "mixer": "DiisMixer", "maxResidua": 5, "levelShift": 16.0,
-            "maxIterations": TRAJ, "start": "MP2",
-            "steps_per_trajectory": TRAJ - 1}
+# the headline system (default) and the large one (--workload c5: V_abcd
+# would be 134 GB; the ladder is streamed from the vertex)
+SYSTEMS = {"c2": {"No": 32, "Nv": 256, "NG": 1024, "seed": 1},
+           "c5": {"No": 24, "Nv": 360, "NG": 1440, "seed": 5}}
+SYSTEM = SYSTEMS["c2"]
+WORKLOAD = None
+
+
+def select_workload(name):
+    global SYSTEM, WORKLOAD
+    SYSTEM = SYSTEMS[name]
+    WORKLOAD = {"workload": "rccsd_t_no%d_nv%d_ng%d" % (SYSTEM["No"], SYSTEM["Nv"],
+                                                         SYSTEM["NG"]),
+                **SYSTEM, "mixer": "DiisMixer", "maxResidua": 5, "levelShift": 16.0,
+                "maxIterations": TRAJ, "start": "MP2",
+                "steps_per_trajectory": TRAJ - 1}
+
+
+select_workload("c2")
 METRIC = "RCCSD iter/s mixed vs FP64 at |dE|<=1uHa; batched solves/s, p50/p99 latency"
 UNIT = "iter/s"
 REF_MAX_STEPS = 3
@@ -352,6 +366,8 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gbcc", choices=["gbcc", "reference"])
+    ap.add_argument("--workload", default="c2", choices=sorted(SYSTEMS),
+                    help="c2: No=32 Nv=256 NG=1024 (default); c5: No=24 Nv=360 NG=1440")
     ap.add_argument("--slices", type=int, default=6)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -370,6 +386,7 @@ def main():
     ap.add_argument("--no-triples", action="store_true",
                     help="skip the (T) correction on the 12th-iteration amplitudes")
     args = ap.parse_args()
+    select_workload(args.workload)
     ws, rank, local, pg = dist_init()
     if args.impl == "reference":
         run_reference(args, ws, rank, pg)
@@ -394,8 +411,14 @@ def main():
 
     # ---- precision mode, inputs resident.  One untimed trajectory captures
     # the steady-state iteration graphs (one per DIIS ring position).
+    ctx.pool_high_water(reset=True)
     sol = gpu.Solver(ctx, s.eps_h, s.eps_p, s.gamma, precision="emu", **SOLVE)
     sol.step(TRAJ)
+    Nv = SYSTEM["Nv"]
+    memory = {"device_pool_peak_bytes": ctx.pool_high_water(),
+              "vabcd_bytes_if_stored": 8 * Nv ** 4,
+              "note": "peak of the library's device allocations over setup and one "
+                      "12-iteration trajectory; V_abcd is never formed"}
     walker = Walker(sol, stream, pg)
     walker.walk(args.warmup, timed=False)
     l0 = ctx.launches
@@ -587,7 +610,8 @@ def main():
                                precision="emulated fp64, %d bf16 digits" % args.slices,
                                l2="inputs larger than L2 (T2, V, Gamma >= 0.5 GB)",
                                timed_segments=walker.segments),
-                "energies": energies, "fp64": fp64, "e2e": e2e, "roofline": roof,
+                "energies": energies, "memory": memory, "fp64": fp64, "e2e": e2e,
+                "roofline": roof,
                 "cpu_baseline": cpu, "serving": serving, "triples": triples,
                 "gpu_launches": launches,
                 "fp64_equiv_tflops_per_step": fl / (ms / 1e3) / 1e12,

@@ -1,6 +1,6 @@
 """Throughput of the library's GEMMs (FP64 and emulated FP64) on one GPU.
 
-  python -m benchmarks.gemm_bench M N K [--prec emu|fp64] [--slices S] [--reps R]
+  python -m benchmarks.gemm_bench M N K [--prec emu|fp64] [--slices S] [--reps R] [--cublas]
 
 Operands are random FP64 device buffers (column-major); timing uses CUDA
 events on the library stream after one warm-up launch.
@@ -17,6 +17,8 @@ def main():
     ap.add_argument("--prec", default="emu", choices=["emu", "fp64"])
     ap.add_argument("--slices", type=int, default=6)
     ap.add_argument("--reps", type=int, default=3)
+    ap.add_argument("--cublas", action="store_true",
+                    help="with --prec fp64, also time cuBLAS DGEMM on the same shape")
     args = ap.parse_args()
     import torch
     from sisi4s_gb300 import capi
@@ -50,6 +52,22 @@ def main():
     if st["launches"]:
         out["tensor_kernel_ms"] = st["ms"] / st["launches"]
         out["tensor_kernel_bf16_tflops"] = st["tc_flops"] / st["ms"] / 1e9
+    if args.cublas and args.prec == "fp64":
+        # the library DGEMM of the same shape (cuBLAS through torch), as the
+        # FP64 reference point of this GPU
+        A = a.view(K, M).t()
+        B = b.view(N, K).t()
+        torch.matmul(A, B)
+        torch.cuda.synchronize()
+        c0 = torch.cuda.Event(enable_timing=True)
+        c1 = torch.cuda.Event(enable_timing=True)
+        c0.record()
+        for _ in range(args.reps):
+            torch.matmul(A, B)
+        c1.record()
+        torch.cuda.synchronize()
+        cms = c0.elapsed_time(c1) / args.reps
+        out.update(cublas_ms=cms, cublas_tflops=2.0 * M * N * K / cms / 1e9)
     print(json.dumps(out))
     ctx.close()
 

@@ -56,6 +56,11 @@ void gbcc_ctx_destroy(gbcc_ctx *ctx);
 const char *gbcc_last_error(const gbcc_ctx *ctx);
 const char *gbcc_status_string(int status);
 int gbcc_abi_version(void);
+/* Largest number of bytes the library's device allocations (the device's
+ * default stream-ordered memory pool) have held at once since the last reset;
+ * reset != 0 restarts the count from the current use.  No counterpart in the
+ * reference; it shows, e.g., that no Nv^4 tensor is ever allocated. */
+gbcc_status gbcc_device_pool_high_water(int device, int reset, int64_t *bytes);
 /* Number of kernels this context has launched so far (all entry points). */
 uint64_t gbcc_ctx_kernel_launches(const gbcc_ctx *ctx);
 /* Analytic FP64-equivalent flops issued to the contraction engine so far. */

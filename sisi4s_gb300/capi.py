@@ -82,6 +82,7 @@ _SIGS = {
     "gbcc_ctx_kernel_launches": (C.c_uint64, [C.c_void_p]),
     "gbcc_ctx_flops": (C.c_double, [C.c_void_p]),
     "gbcc_ctx_stream": (C.c_void_p, [C.c_void_p]),
+    "gbcc_device_pool_high_water": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_int64)]),
     "gbcc_ctx_set_emulation": (C.c_int, [C.c_void_p, C.c_int, C.c_double]),
     "gbcc_ctx_profile": (C.c_int, [C.c_void_p, C.c_int]),
     "gbcc_ctx_set_graphs": (C.c_int, [C.c_void_p, C.c_int]),
@@ -194,6 +195,7 @@ class Context:
         if st != OK:
             raise GbccError(st, self.lib.gbcc_last_error(None).decode())
         self.h = h
+        self.device = device
 
     def check(self, st, allow=(OK,)):
         if st not in allow:
@@ -231,6 +233,14 @@ class Context:
             self.h, mnk.ctypes.data_as(C.POINTER(C.c_int64)), ptr(ms), cap, C.byref(n)))
         return [(int(mnk[3 * i]), int(mnk[3 * i + 1]), int(mnk[3 * i + 2]), float(ms[i]))
                 for i in range(n.value)]
+
+    def pool_high_water(self, reset=False):
+        """Peak bytes held by the library's device allocations on this
+        context's device since the last reset (reset=True starts over)."""
+        v = C.c_int64()
+        self.check(self.lib.gbcc_device_pool_high_water(self.device, int(reset),
+                                                        C.byref(v)))
+        return v.value
 
     @property
     def launches(self):

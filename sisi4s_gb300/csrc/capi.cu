@@ -81,6 +81,23 @@ extern "C" {
 
 int gbcc_abi_version(void) { return GBCC_ABI_VERSION; }
 
+gbcc_status gbcc_device_pool_high_water(int device, int reset, int64_t *bytes) {
+  if (!bytes) return GBCC_BAD_ARG;
+  *bytes = 0;
+  return guard(nullptr, [&]() {
+    cudaMemPool_t pool = nullptr;
+    GBCC_CUDA(cudaDeviceGetDefaultMemPool(&pool, device));
+    unsigned long long v = 0;  // the attribute is a 64-bit unsigned value
+    GBCC_CUDA(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemHigh, &v));
+    *bytes = (int64_t)v;
+    if (reset) {
+      unsigned long long z = 0;
+      GBCC_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrUsedMemHigh, &z));
+    }
+    return GBCC_OK;
+  });
+}
+
 const char *gbcc_status_string(int s) {
   switch (s) {
     case GBCC_OK: return "OK";

@@ -88,6 +88,10 @@ cudaError_t cudaDeviceGetDefaultMemPool(cudaMemPool_t *pool, int) {
 cudaError_t cudaMemPoolSetAttribute(cudaMemPool_t, enum cudaMemPoolAttr, void *) {
   return cudaSuccess;
 }
+cudaError_t cudaMemPoolGetAttribute(cudaMemPool_t, enum cudaMemPoolAttr, void *v) {
+  *static_cast<unsigned long long *>(v) = 0;
+  return cudaSuccess;
+}
 cudaError_t cudaMemGetInfo(size_t *free_b, size_t *total) {
   *total = (size_t)280 << 30;
   *free_b = (size_t)270 << 30;
