@@ -72,6 +72,16 @@ void *gbcc_ctx_stream(const gbcc_ctx *ctx);
 gbcc_status gbcc_ctx_set_emulation(gbcc_ctx *ctx, int emu_slices,
                                    double emu_min_flops);
 
+/* (T) batching of this context: the hole triples run in batches whose
+ * distinct permutation images (up to 6 per triple) share one grouped
+ * tensor-core launch per W product and one epilogue launch, each image
+ * holding an Nv^3 FP64 work array.  max_images bounds the images of a batch
+ * (>= 6; 0, the default: a quarter of the free device memory, at most 8 GiB
+ * and 192 images).  Energies do not depend on it.  No counterpart in the
+ * reference, which evaluates one permutation of one triple at a time
+ * (CcsdPerturbativeTriples.cxx:156-223). */
+gbcc_status gbcc_ctx_set_triples_batch(gbcc_ctx *ctx, int max_images);
+
 /* Replay of steady-state CCSD iterations as captured CUDA graphs (default on;
  * off runs every iteration eagerly).  Results are identical either way. */
 gbcc_status gbcc_ctx_set_graphs(gbcc_ctx *ctx, int enable);

@@ -84,6 +84,7 @@ _SIGS = {
     "gbcc_ctx_stream": (C.c_void_p, [C.c_void_p]),
     "gbcc_device_pool_high_water": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_int64)]),
     "gbcc_ctx_set_emulation": (C.c_int, [C.c_void_p, C.c_int, C.c_double]),
+    "gbcc_ctx_set_triples_batch": (C.c_int, [C.c_void_p, C.c_int]),
     "gbcc_ctx_profile": (C.c_int, [C.c_void_p, C.c_int]),
     "gbcc_ctx_set_graphs": (C.c_int, [C.c_void_p, C.c_int]),
     "gbcc_ctx_gemm_stats": (C.c_int, [C.c_void_p, _dp, C.POINTER(C.c_int64),
@@ -205,6 +206,10 @@ class Context:
     def set_emulation(self, slices=6, min_flops=1e7):
         self.check(self.lib.gbcc_ctx_set_emulation(self.h, int(slices),
                                                    float(min_flops)))
+
+    def set_triples_batch(self, max_images=0):
+        """(T) batch bound in distinct triple images (0: automatic)."""
+        self.check(self.lib.gbcc_ctx_set_triples_batch(self.h, int(max_images)))
 
     def set_graphs(self, enable=True):
         self.check(self.lib.gbcc_ctx_set_graphs(self.h, 1 if enable else 0))

@@ -182,6 +182,12 @@ void *gbcc_ctx_stream(const gbcc_ctx *ctx) {
   return ctx ? static_cast<void *>(ctx->c.stream) : nullptr;
 }
 
+gbcc_status gbcc_ctx_set_triples_batch(gbcc_ctx *ctx, int max_images) {
+  if (!ctx || max_images < 0 || (max_images > 0 && max_images < 6)) return GBCC_BAD_ARG;
+  ctx->c.triples_batch_images = max_images;
+  return GBCC_OK;
+}
+
 gbcc_status gbcc_ctx_set_emulation(gbcc_ctx *ctx, int emu_slices,
                                    double emu_min_flops) {
   if (!ctx || emu_slices < 4 || emu_slices > 8 || emu_min_flops < 0)

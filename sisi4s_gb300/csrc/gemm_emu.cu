@@ -241,6 +241,16 @@ __device__ __forceinline__ double scaled_total(long long t, int e, const OutScal
   return fixed_to_double(t, e) * o.alpha;
 }
 
+// One problem of a grouped launch: many GEMMs of the same M, N, K whose
+// operands are panels of the same families (different operand indices) and
+// whose outputs are different arrays.
+struct EmuProb {
+  const __nv_bfloat16 *A, *B;
+  const int *ea, *eb;
+  double *C;
+  df32 *Cdf;
+};
+
 struct EmuArgs {
   const __nv_bfloat16 *A;  // [S][mt][kt] tiles
   const __nv_bfloat16 *B;  // [S][nt][kt] tiles
@@ -264,7 +274,20 @@ struct EmuArgs {
   int mapped;
   unsigned ml0, nl0;
   int64_t ms0, ms1, ns0, ns1;
+  // grouped launch: nprob problems of this shape, one table entry each (the
+  // pointers above are then unused); nprob = 1 with probs = nullptr is the
+  // plain GEMM.  Grouped launches have ksplit = 1.
+  int nprob = 1;
+  const EmuProb *probs = nullptr;
 };
+
+// pointers of problem q (the plain GEMM's own for a single problem)
+__device__ __forceinline__ EmuProb problem_of(const EmuArgs &a, int q) {
+  if (a.probs) return a.probs[q];
+  EmuProb p;
+  p.A = a.A; p.B = a.B; p.ea = a.ea; p.eb = a.eb; p.C = a.C; p.Cdf = a.Cdf;
+  return p;
+}
 
 // work unit u (a K-split of one output tile) -> split index and tile.
 // Grouped rasterization: consecutive units walk GROUP_M m-tiles down one
@@ -275,7 +298,7 @@ struct EmuArgs {
 __device__ __forceinline__ void unit_coords(const EmuArgs &a, int u, int &split,
                                             int &tile_m, int &tile_n) {
   const int ntiles = a.mt * a.nt;
-  split = u / ntiles;
+  split = u / ntiles;  // the problem index instead in a grouped launch
   const int t = u - split * ntiles;
   const int gsz = GROUP_M * a.nt;
   const int g = t / gsz, r = t - g * gsz;
@@ -324,7 +347,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) emu_gemm_kernel(EmuArgs a) {
   __shared__ volatile int abort_sh;
 
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-  const int nunits = a.mt * a.nt * a.ksplit;
+  const int nunits = a.mt * a.nt * a.ksplit * a.nprob;
+  const bool grouped = a.nprob > 1;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -361,6 +385,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) emu_gemm_kernel(EmuArgs a) {
       for (int u = blockIdx.x; u < nunits && ok; u += gridDim.x) {
         int split, tile_m, tile_n;
         unit_coords(a, u, split, tile_m, tile_n);
+        const EmuProb pr = problem_of(a, grouped ? split : 0);
+        if (grouped) split = 0;
         const int kb0 = split * a.kb_per_split;
         const int nkb = max(0, min(a.kt, kb0 + a.kb_per_split) - kb0);
         for (int kl = 0; kl < nkb; ++kl) {
@@ -383,12 +409,12 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) emu_gemm_kernel(EmuArgs a) {
           const uint32_t sbase = smem_base + st * STAGE_BYTES;
           for (int s = 0; s < S; ++s) {
             const __nv_bfloat16 *ga =
-                a.A + s * a_slice + ((size_t)tile_m * a.kt + kb) * (A_TILE / 2);
+                pr.A + s * a_slice + ((size_t)tile_m * a.kt + kb) * (A_TILE / 2);
             bulk_g2s(sbase + s * A_TILE, ga, A_TILE, full);
           }
           for (int s = 0; s < S; ++s) {
             const __nv_bfloat16 *gb =
-                a.B + s * b_slice + ((size_t)tile_n * a.kt + kb) * (B_TILE / 2);
+                pr.B + s * b_slice + ((size_t)tile_n * a.kt + kb) * (B_TILE / 2);
             bulk_g2s(sbase + S * A_TILE + s * B_TILE, gb, B_TILE, full);
           }
           ++g;
@@ -415,6 +441,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) emu_gemm_kernel(EmuArgs a) {
       for (int u = blockIdx.x; u < nunits && ok; u += gridDim.x) {
         int split, tile_m, tile_n;
         unit_coords(a, u, split, tile_m, tile_n);
+        if (grouped) split = 0;
         const int kb0 = split * a.kb_per_split;
         const int nkb = max(0, min(a.kt, kb0 + a.kb_per_split) - kb0);
         const int nchunks = (nkb + a.kc_blocks - 1) / a.kc_blocks;
@@ -488,6 +515,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) emu_gemm_kernel(EmuArgs a) {
     for (int u = blockIdx.x; u < nunits; u += gridDim.x) {
       int split, tile_m, tile_n;
       unit_coords(a, u, split, tile_m, tile_n);
+      const EmuProb pr = problem_of(a, grouped ? split : 0);
+      if (grouped) split = 0;
       const int kb0 = split * a.kb_per_split;
       const int nkb = max(0, min(a.kt, kb0 + a.kb_per_split) - kb0);
       const int nchunks = (nkb + a.kc_blocks - 1) / a.kc_blocks;
@@ -549,14 +578,14 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) emu_gemm_kernel(EmuArgs a) {
       const int64_t n0 = (int64_t)tile_n * TN + cgrp * EPI_COLS;
       if (a.ksplit == 1) {
         const int ebl =
-            (lane < EPI_COLS && n0 + lane < a.N) ? max(a.eb[n0 + lane], EXP_FLOOR) : 0;
+            (lane < EPI_COLS && n0 + lane < a.N) ? max(pr.eb[n0 + lane], EXP_FLOOR) : 0;
         const bool mrow = m < a.M;
-        const int ea = mrow ? max(a.ea[m], EXP_FLOOR) - 14 - a.frac : 0;
+        const int ea = mrow ? max(pr.ea[m], EXP_FLOOR) - 14 - a.frac : 0;
         const bool accumulate = a.beta != 0.0;
         if constexpr (DF) {
           // float-float output; alpha = +-2^k and beta in {0, 1} (host-checked)
-          const int ea_df = mrow ? max(a.ea[m], EXP_FLOOR) - 14 + a.os.shift : 0;
-          df32 *cp = a.Cdf + m + n0 * a.ldc;
+          const int ea_df = mrow ? max(pr.ea[m], EXP_FLOOR) - 14 + a.os.shift : 0;
+          df32 *cp = pr.Cdf + m + n0 * a.ldc;
 #pragma unroll
           for (int j0 = 0; j0 < EPI_COLS; j0 += 8) {
             df32 c[8];
@@ -581,7 +610,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) emu_gemm_kernel(EmuArgs a) {
           // runs the same loop (the shuffles stay converged)
           const unsigned mu = mrow ? (unsigned)m : 0u;
           const unsigned mq = mu / a.ml0;
-          double *rp = a.C + (int64_t)(mu - mq * a.ml0) * a.ms0 + (int64_t)mq * a.ms1;
+          double *rp = pr.C + (int64_t)(mu - mq * a.ml0) * a.ms0 + (int64_t)mq * a.ms1;
           unsigned nq = (unsigned)n0 / a.nl0, nr = (unsigned)n0 - nq * a.nl0;
 #pragma unroll
           for (int j = 0; j < EPI_COLS; ++j) {
@@ -595,7 +624,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) emu_gemm_kernel(EmuArgs a) {
           }
           continue;
         }
-        double *cp = a.C + m + n0 * a.ldc;
+        double *cp = pr.C + m + n0 * a.ldc;
 #pragma unroll
         for (int j0 = 0; j0 < EPI_COLS; j0 += 8) {
           double c[8];
@@ -1039,7 +1068,88 @@ void gemm_panels(Context &ctx, const EmuPanels &A, int ia, const EmuPanels &B, i
   }
   ctx.flops += 2.0 * (double)M * (double)N * (double)K;
 }
+// Grouped launch over panels: problem q multiplies operand ia[q] of A with
+// operand ib[q] of B into C[q] (Cdf[q] for float-float output); all problems
+// share M, N, K, alpha, beta and ldc.  One persistent launch walks the tiles
+// of every problem, so a batch of small or short-K products fills the GPU
+// and pays one launch.
+template <int S>
+void gemm_panels_grouped(Context &ctx, const EmuPanels &A, const int *ia, const EmuPanels &B,
+                         const int *ib, int nprob, double alpha, double beta,
+                         double *const *C, df32 *const *Cdf, int64_t ldc) {
+  const int64_t M = A.rows, N = B.rows, K = A.K;
+  const EmuPlan P = emu_plan(S, M, N, K, ctx.sm_count, false);
+  require((int64_t)P.mt * P.nt * nprob < (1LL << 31), "grouped GEMM: too many tiles");
+  const int64_t aplane = (int64_t)A.rt * A.kt * TM * KB;
+  const int64_t bplane = (int64_t)B.rt * B.kt * TN * KB;
+  std::vector<EmuProb> probs((size_t)nprob);
+  for (int q = 0; q < nprob; ++q) {
+    require(ia[q] >= 0 && ia[q] < A.count && ib[q] >= 0 && ib[q] < B.count,
+            "grouped GEMM: operand index");
+    EmuProb &e = probs[q];
+    e.A = A.panels.as<__nv_bfloat16>() + (int64_t)ia[q] * S * aplane;
+    e.B = B.panels.as<__nv_bfloat16>() + (int64_t)ib[q] * S * bplane;
+    e.ea = A.exps.as<int>() + (int64_t)ia[q] * M;
+    e.eb = B.exps.as<int>() + (int64_t)ib[q] * N;
+    e.C = C ? C[q] : nullptr;
+    e.Cdf = Cdf ? Cdf[q] : nullptr;
+  }
+  DBuf table(ctx, sizeof(EmuProb) * probs.size());
+  GBCC_CUDA(cudaMemcpyAsync(table.as<EmuProb>(), probs.data(), sizeof(EmuProb) * probs.size(),
+                            cudaMemcpyHostToDevice, ctx.stream));
+  constexpr int STAGE_BYTES = S * (A_TILE + B_TILE);
+  constexpr int STAGES = (SMEM_BUDGET / STAGE_BYTES) > 4 ? 4 : (SMEM_BUDGET / STAGE_BYTES);
+  const int smem = STAGES * STAGE_BYTES;
+  void (*kern)(EmuArgs) = Cdf ? emu_gemm_kernel<S, true> : emu_gemm_kernel<S, false>;
+  GBCC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  EmuArgs args{};
+  args.M = M; args.N = N; args.ldc = ldc;
+  args.mt = P.mt; args.nt = P.nt; args.kt = P.kt;
+  args.kc_blocks = P.kc_blocks;
+  args.kb_per_split = P.kb_per_split;
+  args.ksplit = 1;
+  args.frac = P.frac;
+  args.os = out_scale(alpha);
+  args.inject_wait = ctx.take_fault(GBCC_FAULT_DEVICE_WAIT) ? 1 : 0;
+  args.beta = beta;
+  args.err = ctx.device_error_word();
+  args.nprob = nprob;
+  args.probs = table.as<EmuProb>();
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  if (ctx.prof) {
+    ev0 = ctx.prof_event();
+    ev1 = ctx.prof_event();
+    GBCC_CUDA(cudaEventRecord(ev0, ctx.stream));
+  }
+  kern<<<emu_grid(ctx, (int64_t)P.mt * P.nt * nprob), NUM_THREADS, smem, ctx.stream>>>(args);
+  GBCC_CHECK_LAUNCH(ctx);
+  const double f = 2.0 * (double)M * (double)N * (double)K * nprob;
+  if (ctx.prof) {
+    GBCC_CUDA(cudaEventRecord(ev1, ctx.stream));
+    ctx.prof_recs.push_back({ev0, ev1, f * S * (S + 1) / 2.0, f, M, N, K * nprob});
+  }
+  ctx.flops += f;
+}
 }  // namespace
+
+void emu_gemm_panels_grouped(Context &ctx, const EmuPanels &A, const int *ia,
+                             const EmuPanels &B, const int *ib, int nprob, double alpha,
+                             double beta, double *const *C, df32 *const *Cdf, int64_t ldc) {
+  require(nprob >= 1, "grouped GEMM: no problems");
+  require(A.role_a && !B.role_a && A.K == B.K && A.S == B.S, "grouped GEMM: operand mismatch");
+  require((C == nullptr) != (Cdf == nullptr), "grouped GEMM: one output kind");
+  if (Cdf)
+    require(out_scale(alpha).pow2 && (beta == 0.0 || beta == 1.0),
+            "grouped GEMM: float-float output needs alpha = +-2^k and beta in {0, 1}");
+  switch (A.S) {
+    case 4: gemm_panels_grouped<4>(ctx, A, ia, B, ib, nprob, alpha, beta, C, Cdf, ldc); break;
+    case 5: gemm_panels_grouped<5>(ctx, A, ia, B, ib, nprob, alpha, beta, C, Cdf, ldc); break;
+    case 6: gemm_panels_grouped<6>(ctx, A, ia, B, ib, nprob, alpha, beta, C, Cdf, ldc); break;
+    case 7: gemm_panels_grouped<7>(ctx, A, ia, B, ib, nprob, alpha, beta, C, Cdf, ldc); break;
+    case 8: gemm_panels_grouped<8>(ctx, A, ia, B, ib, nprob, alpha, beta, C, Cdf, ldc); break;
+    default: throw Error(GBCC_BAD_ARG, "emu_slices must be in [4, 8]");
+  }
+}
 
 EmuPanels emu_split(Context &ctx, bool role_a, const double *base, int64_t R,
                     int64_t K, int64_t rs, int64_t ks, int count, int64_t pstride) {

@@ -58,6 +58,9 @@ struct Context {
   double emu_min_flops = 1e7;
   // replay steady-state CCSD iterations as captured CUDA graphs
   bool use_graphs = true;
+  // (T): distinct triple images whose W products share one batch (one W
+  // slot of Nv^3 doubles each); 0 = from the free device memory
+  int triples_batch_images = 0;
   // injected fault (GBCC_FAULT_*), consumed by the first matching event
   // (never while the stream is being captured into a graph: the fault would
   // be baked into every replay)
@@ -261,6 +264,11 @@ struct df32;
 void emu_gemm_panels(Context &ctx, const EmuPanels &A, int ia, const EmuPanels &B,
                      int ib, double alpha, double beta, double *C, int64_t ldc,
                      df32 *Cdf = nullptr);
+// Grouped form: nprob products of the same shape in one launch, problem q
+// multiplying operand ia[q] of A with operand ib[q] of B into C[q] (or Cdf[q]).
+void emu_gemm_panels_grouped(Context &ctx, const EmuPanels &A, const int *ia,
+                             const EmuPanels &B, const int *ib, int nprob, double alpha,
+                             double beta, double *const *C, df32 *const *Cdf, int64_t ldc);
 // Output index map of an emulated GEMM with two indices on each side: C(m, n)
 // lives at C + (m % ml0) ms0 + (m / ml0) ms1 + (n % nl0) ns0 + (n / nl0) ns1,
 // so a product can write a permuted layout directly (beta must be 0).

@@ -22,6 +22,8 @@
 // GEMMs.  FP64 mode runs the same kernel in double.
 
 #include <algorithm>
+#include <array>
+#include <cmath>
 #include <vector>
 
 #include "ccsd.hpp"
@@ -43,20 +45,26 @@ void perm3(int p, int img[3]) {
   for (++i; i < 3; ++i) img[i] = sub[i - 1] + 1;
 }
 
-struct EpiArgs {
+// what the epilogue needs of one hole triple (i <= j <= k)
+struct EpiTriple {
   const void *W[6];     // W_p (element type R) for each image p; aliases for repeats
   int distinct[6];
   int m[6][3];          // hole indices i o pi_p
+  int i3[3];
+  int64_t t;            // index of the triple in the i <= j <= k order
+};
+
+struct EpiArgs {
+  const EpiTriple *trip;  // one per blockIdx.y
   int img[6][3];        // Permutation<3>(s) images
   int dinv[6][3];       // D.V read: u_m = y_{dinv[p][m]}  (y_n = u_{pi_p(n)});
                         // also rho_r^-1 of the energy read, x_r(y)_m = y_{dinv[r][m]}
   int odd[6];           // parity of Permutation<3>(r)
-  int i3[3];
   const double *eps_h;
   const void *eps_p, *T1h, *Vabij;   // element type R; T1h = T1 / 2
   int64_t Nv, No;
   const int *orbits;    // [norb][3] tile coordinates A <= B <= C
-  double *partials;     // one per orbit
+  double *partials;     // [triple][orbit]
 };
 
 constexpr int OT = 8;                  // orbit tile edge
@@ -111,7 +119,8 @@ template <typename R> struct ProductSum {
   __device__ double value() const { return ar_to_double(s); }
 };
 
-// One CTA per orbit of 8^3 tiles under the six coordinate permutations.
+// One CTA per orbit of 8^3 tiles under the six coordinate permutations
+// (blockIdx.x) and per hole triple of the batch (blockIdx.y).
 // Every permuted read of the triple's epilogue stays inside the orbit:
 //   DV[u]  = (sum_p W_p[u_{pi_p(0)}, u_{pi_p(1)}, u_{pi_p(2)}]) / D_u
 //            (CcsdPerturbativeTriples.cxx:162-191; p in Permutation<3> order)
@@ -145,6 +154,7 @@ __global__ void __launch_bounds__(EPI_THREADS, 4) triples_orbit_kernel(EpiArgs a
   const R *__restrict__ eps_p = static_cast<const R *>(a.eps_p);
   const R *__restrict__ T1h = static_cast<const R *>(a.T1h);
   const R *__restrict__ Vabij = static_cast<const R *>(a.Vabij);
+  const EpiTriple &tr = a.trip[blockIdx.y];
   if (threadIdx.x == 0) {
     const int rep[3] = {a.orbits[3 * blockIdx.x], a.orbits[3 * blockIdx.x + 1],
                         a.orbits[3 * blockIdx.x + 2]};
@@ -168,14 +178,14 @@ __global__ void __launch_bounds__(EPI_THREADS, 4) triples_orbit_kernel(EpiArgs a
       for (int k = 0; k < 3; ++k) s_ps[q][k] = a.img[q][k] == 0 ? 1 : (a.img[q][k] == 1 ? OP : OP * OP);
       for (int j = 0; j < n; ++j)
         s_jt[q][j] = find_tile(tl, n, tl[j][a.dinv[q][0]], tl[j][a.dinv[q][1]], tl[j][a.dinv[q][2]]);
-      s_W[q] = static_cast<const R *>(a.W[q]);
-      s_t1[q] = Nv * a.m[q][0];
-      s_v[q] = Nv * Nv * (a.m[q][1] + No * a.m[q][2]);
-      s_dist[q] = a.distinct[q];
+      s_W[q] = static_cast<const R *>(tr.W[q]);
+      s_t1[q] = Nv * tr.m[q][0];
+      s_v[q] = Nv * Nv * (tr.m[q][1] + No * tr.m[q][2]);
+      s_dist[q] = tr.distinct[q];
       s_odd[q] = a.odd[q];
     }
     s_n = n;
-    ar_set(s_ehs, __dadd_rn(__dadd_rn(a.eps_h[a.i3[0]], a.eps_h[a.i3[1]]), a.eps_h[a.i3[2]]));
+    ar_set(s_ehs, __dadd_rn(__dadd_rn(a.eps_h[tr.i3[0]], a.eps_h[tr.i3[1]]), a.eps_h[tr.i3[2]]));
   }
   for (int i = threadIdx.x; i < 6 * OT_WORDS; i += EPI_THREADS) DV[i] = ar_zero<R>();
   __syncthreads();
@@ -264,7 +274,8 @@ __global__ void __launch_bounds__(EPI_THREADS, 4) triples_orbit_kernel(EpiArgs a
   if (threadIdx.x < 32) {
     R r = (threadIdx.x < EPI_THREADS / 32) ? red[threadIdx.x] : ar_zero<R>();
     for (int o = 16; o > 0; o >>= 1) r = ar_add(r, ar_shfl_down(r, o));
-    if (threadIdx.x == 0) a.partials[blockIdx.x] = ar_to_double(r);
+    if (threadIdx.x == 0)
+      a.partials[tr.t * (int64_t)gridDim.x + blockIdx.x] = ar_to_double(r);
   }
 }
 
@@ -325,8 +336,6 @@ double triples_energy(Context &ctx, const CcsdInputs &I, const double *T1,
   OTen Vt(ctx, {No, Nv, No, No});
   assign(ctx, 1.0, I.Vijka, "jklc", 0.0, Vt, "lcjk");
   const int64_t n3 = Nv * Nv * Nv;
-  std::vector<DBuf> Wb(6);
-  for (auto &b : Wb) b.alloc(ctx, 8 * n3);
   // epilogue operands in the epilogue type: T1 / 2 (exact scaling), and in
   // precision mode float-float copies of eps_p and Vabij
   const int64_t nv4 = Nv * Nv * No * No;
@@ -397,55 +406,104 @@ double triples_energy(Context &ctx, const CcsdInputs &I, const double *T1,
     Bh = emu_split(ctx, false, Vt.p(), Nv, No, No, 1, (int)(No * No), No * Nv);
     Wvv.buf.release();  // the FP64 copy is no longer needed
   }
+  // Triples run in batches: the distinct images of a batch's triples get
+  // their own W slots, so that all hole products of the batch are one grouped
+  // tensor-core launch, all particle products another, and the epilogue one
+  // launch over (orbit, triple).  The slot pool takes at most a quarter of
+  // the free device memory (8 GiB at most, 6 slots at least) unless the
+  // context sets the batch size.
+  size_t free_b = 0, total_b = 0;
+  GBCC_CUDA(cudaMemGetInfo(&free_b, &total_b));
+  const double slot_bytes = 8.0 * (double)n3;
+  const int max_slots =
+      ctx.triples_batch_images > 0
+          ? std::max(6, ctx.triples_batch_images)
+          : (int)std::max<double>(
+                6.0, std::min(192.0, std::floor(std::min(free_b / 4.0, 8.0 * (1ull << 30)) /
+                                                slot_bytes)));
+  DBuf pool(ctx, (size_t)max_slots * 8 * (size_t)n3);
+  auto slot_ptr = [&](int q) { return pool.as<double>() + (int64_t)q * n3; };
+  std::vector<EpiTriple> trips;
+  std::vector<int> h_ia, h_ib, p_ia, p_ib;     // hole / particle operand indices
+  std::vector<df32 *> cdf;                     // output slot per problem
+  std::vector<std::array<int, 3>> img_m;       // m per problem (FP64 mode)
+  auto flush = [&]() {
+    if (trips.empty()) return;
+    const int np = (int)cdf.size();
+    if (emu) {
+      // the short-K hole products first (beta = 0: no read of W), then the
+      // particle products accumulate, their C reads hidden behind K = Nv
+      emu_gemm_panels_grouped(ctx, Ah, h_ia.data(), Bh, h_ib.data(), np, -1.0, 0.0,
+                              nullptr, cdf.data(), Nv * Nv);
+      emu_gemm_panels_grouped(ctx, At, p_ia.data(), Bw, p_ib.data(), np, 1.0, 1.0,
+                              nullptr, cdf.data(), Nv);
+    } else {
+      for (int q = 0; q < np; ++q) {
+        const int *m = img_m[q].data();
+        double *Wp = slot_ptr(q);
+        // W[a,(b,c)] = sum_d T2[a,d,m0,m1] Wvv[d,(b,c),m2]
+        gemm(ctx, false, false, Nv, Nv * Nv, Nv, 1.0,
+             T2 + Nv * Nv * (m[0] + No * m[1]), Nv, Wvv.p() + n3 * m[2], Nv,
+             0.0, Wp, Nv, 1, 0, 0, 0, precision);
+        // W[(a,b),c] -= sum_l T2[a,b,m0,l] Vt[l,c,m1,m2]
+        gemm(ctx, false, false, Nv * Nv, Nv, No, -1.0,
+             T2 + Nv * Nv * m[0], Nv * Nv * No,
+             Vt.p() + No * Nv * (m[1] + No * m[2]), No, 1.0, Wp, Nv * Nv, 1,
+             0, 0, 0, precision);
+      }
+    }
+    DBuf tbuf(ctx, sizeof(EpiTriple) * trips.size());
+    GBCC_CUDA(cudaMemcpyAsync(tbuf.as<EpiTriple>(), trips.data(),
+                              sizeof(EpiTriple) * trips.size(), cudaMemcpyHostToDevice,
+                              ctx.stream));
+    EpiArgs a = base;
+    a.trip = tbuf.as<EpiTriple>();
+    a.partials = partials.as<double>();
+    const dim3 grid((unsigned)nb, (unsigned)trips.size());
+    if (emu)
+      triples_orbit_kernel<df32><<<grid, EPI_THREADS, 0, ctx.stream>>>(a);
+    else
+      triples_orbit_kernel<double><<<grid, EPI_THREADS, 0, ctx.stream>>>(a);
+    GBCC_CHECK_LAUNCH(ctx);
+    trips.clear();
+    h_ia.clear(); h_ib.clear(); p_ia.clear(); p_ib.clear();
+    cdf.clear(); img_m.clear();
+  };
   int64_t t = 0;
   for (int i0 = 0; i0 < No; ++i0)
     for (int i1 = i0; i1 < No; ++i1)
       for (int i2 = i1; i2 < No; ++i2, ++t) {
         const int iv[3] = {i0, i1, i2};
-        EpiArgs a = base;
-        a.i3[0] = i0; a.i3[1] = i1; a.i3[2] = i2;
+        const int ndist = (i0 == i1 && i1 == i2) ? 1 : ((i0 == i1 || i1 == i2) ? 3 : 6);
+        if ((int)cdf.size() + ndist > max_slots || trips.size() >= 65535) flush();
+        EpiTriple tr{};
+        tr.i3[0] = i0; tr.i3[1] = i1; tr.i3[2] = i2;
+        tr.t = t;
         for (int p = 0; p < 6; ++p) {
           int m[3];
           for (int n = 0; n < 3; ++n) m[n] = iv[img[p][n]];
           int q = 0;
           for (; q < p; ++q)
-            if (a.m[q][0] == m[0] && a.m[q][1] == m[1] && a.m[q][2] == m[2]) break;
-          for (int n = 0; n < 3; ++n) a.m[p][n] = m[n];
+            if (tr.m[q][0] == m[0] && tr.m[q][1] == m[1] && tr.m[q][2] == m[2]) break;
+          for (int n = 0; n < 3; ++n) tr.m[p][n] = m[n];
           if (q < p) {                                            // :166-172
-            a.distinct[p] = 0;
-            a.W[p] = a.W[q];
+            tr.distinct[p] = 0;
+            tr.W[p] = tr.W[q];
             continue;
           }
-          a.distinct[p] = 1;
-          a.W[p] = Wb[p].as<void>();
-          if (emu) {
-            // the short-K hole product first (beta = 0: no read of W), then the
-            // particle product accumulates, its C reads hidden behind K = Nv
-            df32 *Wp = Wb[p].as<df32>();
-            emu_gemm_panels(ctx, Ah, m[0], Bh, (int)(m[1] + No * m[2]), -1.0, 0.0, nullptr,
-                            Nv * Nv, Wp);
-            emu_gemm_panels(ctx, At, (int)(m[0] + No * m[1]), Bw, m[2], 1.0, 1.0, nullptr, Nv,
-                            Wp);
-            continue;
-          }
-          double *Wp = Wb[p].as<double>();
-          // W[a,(b,c)] = sum_d T2[a,d,m0,m1] Wvv[d,(b,c),m2]
-          gemm(ctx, false, false, Nv, Nv * Nv, Nv, 1.0,
-               T2 + Nv * Nv * (m[0] + No * m[1]), Nv, Wvv.p() + n3 * m[2], Nv,
-               0.0, Wp, Nv, 1, 0, 0, 0, precision);
-          // W[(a,b),c] -= sum_l T2[a,b,m0,l] Vt[l,c,m1,m2]
-          gemm(ctx, false, false, Nv * Nv, Nv, No, -1.0,
-               T2 + Nv * Nv * m[0], Nv * Nv * No,
-               Vt.p() + No * Nv * (m[1] + No * m[2]), No, 1.0, Wp, Nv * Nv, 1,
-               0, 0, 0, precision);
+          tr.distinct[p] = 1;
+          const int slot = (int)cdf.size();
+          tr.W[p] = slot_ptr(slot);
+          cdf.push_back(reinterpret_cast<df32 *>(slot_ptr(slot)));
+          img_m.push_back({m[0], m[1], m[2]});
+          h_ia.push_back(m[0]);
+          h_ib.push_back((int)(m[1] + No * m[2]));
+          p_ia.push_back((int)(m[0] + No * m[1]));
+          p_ib.push_back(m[2]);
         }
-        a.partials = partials.as<double>() + (int64_t)nb * t;
-        if (emu)
-          triples_orbit_kernel<df32><<<nb, EPI_THREADS, 0, ctx.stream>>>(a);
-        else
-          triples_orbit_kernel<double><<<nb, EPI_THREADS, 0, ctx.stream>>>(a);
-        GBCC_CHECK_LAUNCH(ctx);
+        trips.push_back(tr);
       }
+  flush();
   sum_rows_kernel<<<(unsigned)ntrip, 256, 0, ctx.stream>>>(partials.as<double>(), nb,
                                                            per_trip.as<double>());
   GBCC_CHECK_LAUNCH(ctx);

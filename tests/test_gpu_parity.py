@@ -269,3 +269,30 @@ def test_triples_emulated_matches_oracle(ctx, No, Nv, NG):
     # six bf16 digits: ~2^-40 relative per contraction
     assert abs(et - ref) < 1e-10 * max(1.0, abs(ref))
 
+
+
+@pytest.mark.parametrize("precision", ["fp64", "emu"])
+def test_triples_batching_does_not_change_the_bits(ctx, precision):
+    """(T) runs its hole triples in batches (grouped W products, one epilogue
+    launch per batch); every batch size gives the same energy, bit for bit:
+    one triple per batch, batches that end inside the i <= j <= k order at
+    varying points, and the automatic size (all triples of this system in one
+    batch).  Checked against the oracle as well."""
+    No, Nv, NG = 5, 24, 60
+    s = make_system(No, Nv, NG, seed=41)
+    ints = oracle_ints(s.gamma, No)
+    T1, T2 = _rand_amplitudes(Nv, No, seed=4, scale=0.05)
+    ref = triples_dense(s.eps_h, s.eps_p, T1, T2, ints["PPHH"], ints["HHHP"], s.gamma)
+    ctx.set_emulation(6, 0.0)
+    got = []
+    try:
+        for images in (6, 7, 13, 0):
+            ctx.set_triples_batch(images)
+            got.append(gpu.triples(ctx, s.eps_h, s.eps_p, s.gamma, T1, T2,
+                                   precision=precision)[0])
+    finally:
+        ctx.set_triples_batch(0)
+        ctx.set_emulation(6, 1e7)
+    assert got.count(got[0]) == len(got), got
+    tol = 1e-12 if precision == "fp64" else 1e-10
+    assert abs(got[0] - ref) < tol * max(1.0, abs(ref))
