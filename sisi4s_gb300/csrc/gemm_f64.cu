@@ -88,13 +88,22 @@ __device__ __forceinline__ void store_tiles(double (*As)[BM + 1],
   }
 }
 
+// Split-K: with fewer output tiles than the GPU has SMs, blockIdx.x also
+// selects one of `ksplit` consecutive K ranges of `kchunk` (a multiple of
+// BK); each writes its unscaled partial product to W[split][z][m + n M], and
+// splitk_reduce_kernel sums the partials in split order (deterministic).
+struct SplitK {
+  int64_t ksplit = 1, kchunk = 0;
+  double *W = nullptr;
+};
+
 template <bool TA, bool TB, bool PTR>
 __global__ void __launch_bounds__(NT)
     dgemm_kernel(int64_t M, int64_t N, int64_t K, double alpha,
                  const double *__restrict__ A0, int64_t lda,
                  const double *__restrict__ B0, int64_t ldb, double beta,
                  double *__restrict__ C0, int64_t ldc, int64_t sA, int64_t sB,
-                 int64_t sC, PtrBatch pb, int64_t tiles_m) {
+                 int64_t sC, PtrBatch pb, int64_t tiles_m, SplitK sk) {
   __shared__ double As[BK][BM + 1];
   __shared__ double Bs[BK][BN + 1];
   const int64_t z = blockIdx.z + (int64_t)gridDim.z * blockIdx.y;
@@ -110,9 +119,15 @@ __global__ void __launch_bounds__(NT)
     B = B0 + z * sB;
     C = C0 + z * sC;
   }
-  const int64_t tm = blockIdx.x % tiles_m;
-  const int64_t tn = blockIdx.x / tiles_m;
+  const int64_t ntiles = (int64_t)gridDim.x / sk.ksplit;
+  const int64_t split = blockIdx.x / ntiles;
+  const int64_t tile = blockIdx.x - split * ntiles;
+  const int64_t tm = tile % tiles_m;
+  const int64_t tn = tile / tiles_m;
   const int64_t m0 = tm * BM, n0 = tn * BN;
+  // this block's K range [kb, kend)
+  const int64_t kb = sk.ksplit > 1 ? split * sk.kchunk : 0;
+  const int64_t kend = sk.ksplit > 1 ? min(K, kb + sk.kchunk) : K;
   const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
   double acc[4][4];
 #pragma unroll
@@ -121,12 +136,12 @@ __global__ void __launch_bounds__(NT)
     for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
 
   double ra[4], rb[4];
-  load_tiles<TA, TB>(A, lda, B, ldb, M, N, K, m0, n0, 0, ra, rb);
-  for (int64_t k0 = 0; k0 < K; k0 += BK) {
+  load_tiles<TA, TB>(A, lda, B, ldb, M, N, kend, m0, n0, kb, ra, rb);
+  for (int64_t k0 = kb; k0 < kend; k0 += BK) {
     store_tiles<TA, TB>(As, Bs, ra, rb);
     __syncthreads();
-    if (k0 + BK < K)
-      load_tiles<TA, TB>(A, lda, B, ldb, M, N, K, m0, n0, k0 + BK, ra, rb);
+    if (k0 + BK < kend)
+      load_tiles<TA, TB>(A, lda, B, ldb, M, N, kend, m0, n0, k0 + BK, ra, rb);
 #pragma unroll
     for (int kk = 0; kk < BK; ++kk) {
       double a[4], b[4];
@@ -140,6 +155,20 @@ __global__ void __launch_bounds__(NT)
         for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
     }
     __syncthreads();
+  }
+  if (sk.ksplit > 1) {
+    double *w = sk.W + ((int64_t)split * gridDim.y * gridDim.z + z) * M * N;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int64_t n = n0 + ty + 16 * j;
+      if (n >= N) continue;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int64_t m = m0 + tx + 16 * i;
+        if (m < M) w[m + n * M] = acc[i][j];
+      }
+    }
+    return;
   }
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
@@ -157,6 +186,27 @@ __global__ void __launch_bounds__(NT)
   }
 }
 
+// C[z](m, n) = alpha sum_s W[s][z](m, n) + beta C[z](m, n), splits summed in
+// order; one thread per output
+template <bool PTR>
+__global__ void splitk_reduce_kernel(int64_t M, int64_t N, int64_t nbatch, int64_t ks,
+                                     const double *__restrict__ W, double alpha, double beta,
+                                     double *__restrict__ C0, int64_t ldc, int64_t sC,
+                                     PtrBatch pb) {
+  const int64_t per = M * N;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < per * nbatch;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t z = e / per, r = e - z * per;
+    const int64_t n = r / M, m = r - n * M;
+    double s = 0.0;
+    for (int64_t q = 0; q < ks; ++q) s += W[(q * nbatch + z) * per + r];
+    double *c = (PTR ? pb.C[z] : C0 + z * sC) + m + n * ldc;
+    double v = alpha * s;
+    if (beta != 0.0) v = fma(beta, *c, v);
+    *c = v;
+  }
+}
+
 template <bool PTR>
 void launch(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
             double alpha, const double *A, int64_t lda, const double *B,
@@ -171,15 +221,43 @@ void launch(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
   while (batch % gz) --gz;
   const int64_t gy = batch / gz;
   require(gy <= 65535, "gemm: batch too large");
-  dim3 grid((unsigned)(tiles_m * tiles_n), (unsigned)gy, (unsigned)gz);
+  // split K when the tiles of all batch entries fill less than the GPU: aim
+  // for about three blocks per SM, every split at least 4 k-tiles long
+  SplitK sk;
+  const int64_t G = std::max(ctx.sm_count, 1);
+  const int64_t blocks = tiles_m * tiles_n * batch;
+  DBuf wsp;
+  if (blocks < G && K >= 8 * BK) {
+    int64_t ks = std::min<int64_t>((3 * G + blocks - 1) / blocks, 64);
+    ks = std::min<int64_t>(ks, K / (4 * BK));
+    if (ks > 1) {
+      int64_t kchunk = (K + ks - 1) / ks;
+      kchunk = (kchunk + BK - 1) / BK * BK;
+      ks = (K + kchunk - 1) / kchunk;
+      if (ks > 1) {
+        sk.ksplit = ks;
+        sk.kchunk = kchunk;
+        wsp.alloc(ctx, sizeof(double) * ks * batch * M * N);
+        sk.W = wsp.as<double>();
+      }
+    }
+  }
+  dim3 grid((unsigned)(tiles_m * tiles_n * sk.ksplit), (unsigned)gy, (unsigned)gz);
   auto k00 = dgemm_kernel<false, false, PTR>;
   auto k01 = dgemm_kernel<false, true, PTR>;
   auto k10 = dgemm_kernel<true, false, PTR>;
   auto k11 = dgemm_kernel<true, true, PTR>;
   auto kern = ta ? (tb ? k11 : k10) : (tb ? k01 : k00);
   kern<<<grid, NT, 0, ctx.stream>>>(M, N, K, alpha, A, lda, B, ldb, beta, C,
-                                    ldc, sA, sB, sC, pb, tiles_m);
+                                    ldc, sA, sB, sC, pb, tiles_m, sk);
   GBCC_CHECK_LAUNCH(ctx);
+  if (sk.ksplit > 1) {
+    const int64_t n = M * N * batch;
+    const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, G * 8));
+    splitk_reduce_kernel<PTR><<<g, 256, 0, ctx.stream>>>(M, N, batch, sk.ksplit, sk.W, alpha,
+                                                          beta, C, ldc, sC, pb);
+    GBCC_CHECK_LAUNCH(ctx);
+  }
   ctx.flops += 2.0 * (double)M * (double)N * (double)K * (double)batch;
 }
 
