@@ -296,15 +296,17 @@ def serve_measure(args):
     convergence settings): one-at-a-time FP64 and mixed on the first
     `serve_single` requests, and batched with `serve_slots` concurrent
     solves on the first `serve_requests`."""
-    from sisi4s_gb300 import serve
+    from sisi4s_gb300 import autotune, serve
+    table = autotune.load()
     reqs = serve.make_requests(max(args.serve_requests, args.serve_single))
     out = {"requests": args.serve_requests, "slots": args.serve_slots,
+           "tuning": "none" if table is None else "autotuner table (per shape bucket)",
            "solve": "RCCSD + (T), DIIS(5), energyConvergence 3e-11, "
                     "amplitudesConvergence 1e-7, maxIterations 100"}
     for prec in ("fp64", "emu"):
         srv = serve.Server(slots=1)
         recs, wall = serve.run_stream(srv, reqs[:args.serve_single], lam=None,
-                                      precision=prec, **SERVE_OPTS)
+                                      precision=prec, tuning=table, **SERVE_OPTS)
         srv.close()
         st = serve.latency_stats(recs, wall)
         out["one_at_a_time_" + prec] = {"requests": args.serve_single,
@@ -313,7 +315,8 @@ def serve_measure(args):
     lam = args.serve_lambda if args.serve_lambda > 0 else None
     srv = serve.Server(slots=args.serve_slots)
     recs, wall = serve.run_stream(srv, reqs[:args.serve_requests], lam=lam,
-                                  precision=args.serve_precision, **SERVE_OPTS)
+                                  precision=args.serve_precision, tuning=table,
+                                  **SERVE_OPTS)
     srv.close()
     st = serve.latency_stats(recs, wall)
     st["arrivals"] = ("Poisson, rate %g /s (seed 0)" % lam) if lam else "all at t = 0"

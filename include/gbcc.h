@@ -81,6 +81,10 @@ gbcc_status gbcc_ctx_set_emulation(gbcc_ctx *ctx, int emu_slices,
  * reference, which evaluates one permutation of one triple at a time
  * (CcsdPerturbativeTriples.cxx:156-223). */
 gbcc_status gbcc_ctx_set_triples_batch(gbcc_ctx *ctx, int max_images);
+/* K-split policies of this context's GEMMs (see gbcc_ccsd_opts):
+ * f64_blocks_per_sm >= 0, emu_max_ksplit in [1, 64].  No counterpart in the
+ * reference. */
+gbcc_status gbcc_ctx_set_splits(gbcc_ctx *ctx, int f64_blocks_per_sm, int emu_max_ksplit);
 
 /* Replay of steady-state CCSD iterations as captured CUDA graphs (default on;
  * off runs every iteration eagerly).  Results are identical either way. */
@@ -153,6 +157,17 @@ typedef struct {
                                     (stored Vabcd / Vabci,
                                     CcsdEnergyFromCoulombIntegralsReference.cxx:29-292) */
   int only_ppl;                  /* onlyPPL of formulation 1, default 0 */
+  /* Execution tuning (no counterpart in the reference; results do not
+   * depend on them beyond rounding).  gbcc_ccsd_opts_default sets them to
+   * "keep the context's setting"; a set value is applied to the context by
+   * the call that takes these options. */
+  double emu_min_flops;          /* > 0: smallest GEMM (flops) emulated on the
+                                    tensor cores in precision mode; smaller
+                                    ones run in FP64 (context default 1e7) */
+  int f64_split_blocks;          /* FP64 GEMM K-split target in blocks per SM
+                                    (0: no split; context default 3) */
+  int emu_max_ksplit;            /* most K-splits of an emulated GEMM
+                                    (1: none; context default 64) */
 } gbcc_ccsd_opts;
 
 void gbcc_ccsd_opts_default(gbcc_ccsd_opts *opts);

@@ -28,7 +28,9 @@ class CcsdOpts(C.Structure):
                 ("ppl", C.c_int), ("integrals_slice_size", C.c_int),
                 ("integrals_slice_factor", C.c_double),
                 ("precision", C.c_int), ("emu_slices", C.c_int),
-                ("formulation", C.c_int), ("only_ppl", C.c_int)]
+                ("formulation", C.c_int), ("only_ppl", C.c_int),
+                ("emu_min_flops", C.c_double), ("f64_split_blocks", C.c_int),
+                ("emu_max_ksplit", C.c_int)]
 
 
 class CcsdIn(C.Structure):
@@ -85,6 +87,7 @@ _SIGS = {
     "gbcc_device_pool_high_water": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_int64)]),
     "gbcc_ctx_set_emulation": (C.c_int, [C.c_void_p, C.c_int, C.c_double]),
     "gbcc_ctx_set_triples_batch": (C.c_int, [C.c_void_p, C.c_int]),
+    "gbcc_ctx_set_splits": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "gbcc_ctx_profile": (C.c_int, [C.c_void_p, C.c_int]),
     "gbcc_ctx_set_graphs": (C.c_int, [C.c_void_p, C.c_int]),
     "gbcc_ctx_gemm_stats": (C.c_int, [C.c_void_p, _dp, C.POINTER(C.c_int64),
@@ -210,6 +213,11 @@ class Context:
     def set_triples_batch(self, max_images=0):
         """(T) batch bound in distinct triple images (0: automatic)."""
         self.check(self.lib.gbcc_ctx_set_triples_batch(self.h, int(max_images)))
+
+    def set_splits(self, f64_blocks_per_sm=3, emu_max_ksplit=64):
+        """K-split policies of the FP64 and emulated GEMMs (defaults shown)."""
+        self.check(self.lib.gbcc_ctx_set_splits(self.h, int(f64_blocks_per_sm),
+                                                int(emu_max_ksplit)))
 
     def set_graphs(self, enable=True):
         self.check(self.lib.gbcc_ctx_set_graphs(self.h, 1 if enable else 0))

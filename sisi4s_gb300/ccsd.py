@@ -21,7 +21,8 @@ def make_opts(mixer="LinearMixer", max_residua=4, mixing_ratio=1.0,
               max_iterations=16, energy_convergence=1e-6,
               amplitudes_convergence=1e-5, level_shift=0.0, distinguishable=0,
               ppl=1, slice_size=-1, slice_factor=None, precision="fp64",
-              emu_slices=0, formulation="vertex", only_ppl=0):
+              emu_slices=0, formulation="vertex", only_ppl=0, emu_min_flops=None,
+              f64_split_blocks=None, emu_max_ksplit=None):
     o = capi.CcsdOpts()
     capi.load().gbcc_ccsd_opts_default(C.byref(o))
     o.mixer = {"LinearMixer": 0, "DiisMixer": 1}[mixer]
@@ -41,6 +42,13 @@ def make_opts(mixer="LinearMixer", max_residua=4, mixing_ratio=1.0,
     # CcsdEnergyFromCoulombIntegralsReference (resident Vabcd / Vabci)
     o.formulation = {"vertex": 0, "stored": 1}[formulation]
     o.only_ppl = int(only_ppl)
+    # execution tuning (None: keep the context's setting)
+    if emu_min_flops is not None:
+        o.emu_min_flops = float(emu_min_flops)
+    if f64_split_blocks is not None:
+        o.f64_split_blocks = int(f64_split_blocks)
+    if emu_max_ksplit is not None:
+        o.emu_max_ksplit = int(emu_max_ksplit)
     return o
 
 

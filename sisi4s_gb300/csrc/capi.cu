@@ -73,6 +73,9 @@ void check_opts(const gbcc_ccsd_opts &o) {
 
 void apply_precision_opts(gbcc::Context &c, const gbcc_ccsd_opts &o) {
   if (o.emu_slices > 0) c.emu_slices = o.emu_slices;
+  if (o.emu_min_flops > 0) c.emu_min_flops = o.emu_min_flops;
+  if (o.f64_split_blocks >= 0) c.f64_split_blocks = o.f64_split_blocks;
+  if (o.emu_max_ksplit >= 1) c.emu_max_ksplit = std::min(o.emu_max_ksplit, 64);
 }
 
 }  // namespace
@@ -182,6 +185,14 @@ void *gbcc_ctx_stream(const gbcc_ctx *ctx) {
   return ctx ? static_cast<void *>(ctx->c.stream) : nullptr;
 }
 
+gbcc_status gbcc_ctx_set_splits(gbcc_ctx *ctx, int f64_blocks_per_sm, int emu_max_ksplit) {
+  if (!ctx || f64_blocks_per_sm < 0 || emu_max_ksplit < 1 || emu_max_ksplit > 64)
+    return GBCC_BAD_ARG;
+  ctx->c.f64_split_blocks = f64_blocks_per_sm;
+  ctx->c.emu_max_ksplit = emu_max_ksplit;
+  return GBCC_OK;
+}
+
 gbcc_status gbcc_ctx_set_triples_batch(gbcc_ctx *ctx, int max_images) {
   if (!ctx || max_images < 0 || (max_images > 0 && max_images < 6)) return GBCC_BAD_ARG;
   ctx->c.triples_batch_images = max_images;
@@ -266,6 +277,9 @@ void gbcc_ccsd_opts_default(gbcc_ccsd_opts *o) {
   o->emu_slices = 0;
   o->formulation = 0;
   o->only_ppl = 0;
+  o->emu_min_flops = -1.0;
+  o->f64_split_blocks = -1;
+  o->emu_max_ksplit = -1;
 }
 
 gbcc_status gbcc_ccsd_setup(gbcc_ctx *ctx, const gbcc_ccsd_in *in,

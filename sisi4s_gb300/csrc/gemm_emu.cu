@@ -820,7 +820,7 @@ struct EmuPlan {
 // have work; the split totals are exact, so the split does not change the
 // result.
 EmuPlan emu_plan(int S, int64_t M, int64_t N, int64_t K, int sm_count,
-                 bool allow_split) {
+                 bool allow_split, int max_split = 64) {
   EmuPlan p{};
   p.mt = (int)((M + TM - 1) / TM);
   p.nt = (int)((N + TN - 1) / TN);
@@ -841,7 +841,7 @@ EmuPlan emu_plan(int S, int64_t M, int64_t N, int64_t K, int sm_count,
                          (1.6e15 / (double)G);
   int best_cps = nchunks;
   double best_t = 1e300;
-  const int max_ks = allow_split ? std::min(nchunks, 64) : 1;
+  const int max_ks = allow_split ? std::max(1, std::min(nchunks, std::min(max_split, 64))) : 1;
   for (int ks = 1; ks <= max_ks; ++ks) {
     const int cps = (nchunks + ks - 1) / ks;
     const int kse = (nchunks + cps - 1) / cps;
@@ -864,7 +864,7 @@ void run_emu(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
              double alpha, const double *A, int64_t lda, const double *B,
              int64_t ldb, double beta, double *C, int64_t ldc,
              const OutMap &map = OutMap{}) {
-  const EmuPlan P = emu_plan(S, M, N, K, ctx.sm_count, true);
+  const EmuPlan P = emu_plan(S, M, N, K, ctx.sm_count, true, ctx.emu_max_ksplit);
   const int mt = P.mt, nt = P.nt, kt = P.kt;
   require((int64_t)mt * nt * P.ksplit < (1LL << 31), "emu gemm: grid too large");
   // strides of op(A)(m,k) and op(B)^T(n,k)
@@ -1016,7 +1016,7 @@ void gemm_panels(Context &ctx, const EmuPanels &A, int ia, const EmuPanels &B, i
                  double alpha, double beta, double *C, df32 *Cdf, int64_t ldc) {
   const int64_t M = A.rows, N = B.rows, K = A.K;
   // float-float output is written directly (no K-split workspace)
-  const EmuPlan P = emu_plan(S, M, N, K, ctx.sm_count, Cdf == nullptr);
+  const EmuPlan P = emu_plan(S, M, N, K, ctx.sm_count, Cdf == nullptr, ctx.emu_max_ksplit);
   const int64_t aplane = (int64_t)A.rt * A.kt * TM * KB;
   const int64_t bplane = (int64_t)B.rt * B.kt * TN * KB;
   DBuf wsp;

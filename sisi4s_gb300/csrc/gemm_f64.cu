@@ -222,13 +222,14 @@ void launch(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
   const int64_t gy = batch / gz;
   require(gy <= 65535, "gemm: batch too large");
   // split K when the tiles of all batch entries fill less than the GPU: aim
-  // for about three blocks per SM, every split at least 4 k-tiles long
+  // for ctx.f64_split_blocks blocks per SM (3 by default), every split at
+  // least 4 k-tiles long
   SplitK sk;
   const int64_t G = std::max(ctx.sm_count, 1);
   const int64_t blocks = tiles_m * tiles_n * batch;
   DBuf wsp;
-  if (blocks < G && K >= 8 * BK) {
-    int64_t ks = std::min<int64_t>((3 * G + blocks - 1) / blocks, 64);
+  if (ctx.f64_split_blocks > 0 && blocks < G && K >= 8 * BK) {
+    int64_t ks = std::min<int64_t>((ctx.f64_split_blocks * G + blocks - 1) / blocks, 64);
     ks = std::min<int64_t>(ks, K / (4 * BK));
     if (ks > 1) {
       int64_t kchunk = (K + ks - 1) / ks;

@@ -56,6 +56,11 @@ struct Context {
   int emu_slices = 6;
   // GEMMs smaller than this many flops stay in FP64 in precision mode
   double emu_min_flops = 1e7;
+  // K-split policies: an FP64 GEMM whose output tiles fill less than the GPU
+  // splits K to reach about this many blocks per SM (0: never splits); an
+  // emulated GEMM splits K into at most this many parts (1: never)
+  int f64_split_blocks = 3;
+  int emu_max_ksplit = 64;
   // replay steady-state CCSD iterations as captured CUDA graphs
   bool use_graphs = true;
   // (T): distinct triple images whose W products share one batch (one W

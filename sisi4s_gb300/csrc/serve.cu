@@ -47,6 +47,14 @@ struct Request {
 
 // Device footprint of one solve (bytes), from the tensors the solver keeps
 // resident plus the peak of its temporaries, with a 1.5x margin.
+// (T) of a served solve runs its hole triples in batches of at most this many
+// W work arrays (Nv^3 doubles each, about 512 MiB in all), so that its memory
+// is known at admission
+int served_triples_images(int64_t Nv) {
+  const double per = 8.0 * (double)Nv * (double)Nv * (double)Nv;
+  return (int)std::max(6.0, std::min(192.0, std::floor(512.0 * (1 << 20) / per)));
+}
+
 size_t estimate_bytes(const gbcc_ccsd_in &in, const gbcc_ccsd_opts &o, int triples) {
   const double No = in.No, Nv = in.Nv, NG = in.NG;
   const double n2 = Nv * Nv * No * No, n1 = Nv * No;
@@ -58,7 +66,7 @@ size_t estimate_bytes(const gbcc_ccsd_in &in, const gbcc_ccsd_opts &o, int tripl
                  + 2.0 * (n1 + n2) * (2.0 + 2.0 * m)   // T, R, history / mixer
                  + 6.0 * n2                            // residual temporaries
                  + 2.0 * s * s * Nv * Nv;              // ladder block
-  if (triples) words += Nv * Nv * Nv * No + 6.0 * Nv * Nv * Nv;
+  if (triples) words += Nv * Nv * Nv * No + served_triples_images(in.Nv) * Nv * Nv * Nv;
   // stored formulation: resident Vabcd / Vabci (the residual adds no other
   // Nv^4 tensor) and a permuted copy of Vabci
   if (o.formulation == 1) words += 1.0 * Nv * Nv * Nv * Nv + 2.0 * Nv * Nv * Nv * No;
@@ -88,7 +96,12 @@ struct gbcc_server {
 void gbcc_server::run_one(gbcc_ctx *ctx, Request &r) {
   gbcc_solver *s = nullptr;
   r.res.t_start = now_s();
-  gbcc_status st = gbcc_ccsd_setup(ctx, &r.in, &r.opts, &s);
+  // every request starts from the library's execution defaults; its own
+  // options (e.g. a tuned configuration of its shape) are applied at setup
+  gbcc_status st = gbcc_ctx_set_emulation(ctx, 6, 1e7);
+  if (st == GBCC_OK) st = gbcc_ctx_set_splits(ctx, 3, 64);
+  if (st == GBCC_OK) st = gbcc_ctx_set_triples_batch(ctx, served_triples_images(r.in.Nv));
+  if (st == GBCC_OK) st = gbcc_ccsd_setup(ctx, &r.in, &r.opts, &s);
   if (st == GBCC_OK) {
     double e = 0;
     int conv = 0;

@@ -72,7 +72,15 @@ class Server:
             raise capi.GbccError(st, "server creation failed")
         self.h = h
 
-    def submit(self, system, triples=True, **opts):
+    def submit(self, system, triples=True, tuning=None, **opts):
+        """Queues a CCSD(T) solve.  With an autotuner table (``tuning``, see
+        ``autotune.load``), the execution settings of the request's shape
+        bucket are applied unless ``opts`` sets them."""
+        if tuning:
+            from .autotune import lookup
+            prec = opts.get("precision", "fp64")
+            for k, v in lookup(tuning, prec, system.No, system.Nv).items():
+                opts.setdefault(k, v)
         inp = CcsdInput(system.eps_h, system.eps_p, system.gamma)
         o = make_opts(**opts)
         rid = C.c_int64()
@@ -127,9 +135,10 @@ def make_requests(n, first=0):
     return out
 
 
-def run_stream(server, systems, lam=None, seed=0, triples=True, **opts):
+def run_stream(server, systems, lam=None, seed=0, triples=True, tuning=None, **opts):
     """Submit ``systems`` with Poisson arrivals of rate ``lam`` (all at once if
-    lam is None), wait for every result, return per-request records."""
+    lam is None), wait for every result, return per-request records.
+    ``tuning``: an autotuner table applied to every request."""
     n = len(systems)
     if lam is None:
         gaps = np.zeros(n)
@@ -146,7 +155,7 @@ def run_stream(server, systems, lam=None, seed=0, triples=True, **opts):
             if delay > 0:
                 time.sleep(delay)
             t_arrive[k] = time.perf_counter()
-            ids[k] = server.submit(systems[k], triples=triples, **opts)
+            ids[k] = server.submit(systems[k], triples=triples, tuning=tuning, **dict(opts))
 
     th = threading.Thread(target=submitter)
     th.start()
