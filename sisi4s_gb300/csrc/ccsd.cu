@@ -348,10 +348,50 @@ void Ccsd::residual(int it, const double *Tp, double *Rp) {
     auto emulated = [&](int64_t M, int64_t N, int64_t K) {
       return emu && 2.0 * (double)M * (double)N * (double)K >= ctx.emu_min_flops;
     };
+    // Fused form (every pair emulated, Nv a multiple of 16): each V block
+    // goes from the tensor cores straight into the digit panels of R = V.X,
+    // its row exponents bounded in advance from the column norms of the
+    // dressed vertex (Cauchy-Schwarz), so V never exists in FP64 and is
+    // neither re-read for its exponents nor re-split.  The V product then
+    // takes its B operand as [G, d, y] and R sums over k = d + Nv c, so X
+    // enters as X'[d,c,i,j] = X[c,d,i,j].
+    const int64_t s_last = Nv - (ns - 1) * s;
+    const bool fused = Nv % 16 == 0 && emulated(s_last * Nv, s_last * Nv, NG) &&
+                       emulated(s_last * s_last, No * No, Nv * Nv);
+    if (fused) {
+      DBuf amax(ctx, sizeof(unsigned long long) * Nv);
+      ladder_amax(ctx, dG.p(), NG, Nv, amax.as<void>());
+      std::vector<OTen> slT;
+      for (int64_t v = 0; v < ns; ++v) {
+        const int64_t nx = sl[v].t.lens[1];
+        slT.emplace_back(ctx, std::initializer_list<int64_t>{NG, Nv, nx});
+        assign(ctx, 1.0, sl[v], "Gyd", 0.0, slT.back(), "Gdy");
+      }
+      EmuPanels Xq;
+      {
+        OTen Xt(ctx, {Nv, Nv, No, No});
+        assign(ctx, 1.0, X, "cdij", 0.0, Xt, "dcij");
+        Xq = emu_split(ctx, false, Xt.p(), No * No, Nv * Nv, Nv * Nv, 1, 1, 0);
+      }
+      for (int64_t m = 0; m < ns; ++m) {                           // :418
+        for (int64_t n = m; n < ns; ++n) {                         // :419
+          const int64_t nx = sl[n].t.lens[1], ny = sl[m].t.lens[1];
+          const int64_t a0 = n * s, b0 = m * s;
+          EmuPanels Vp = emu_panels_alloc(ctx, true, nx * ny, Nv * Nv);
+          ladder_row_exponents(ctx, amax.as<void>(), a0, nx, b0, ny, Vp.exps.as<int>());
+          // V[(x,c),(d,y)] = sum_G sl_n[G,(x,c)] slT_m[G,(d,y)]   :425-434
+          gemm_emu_to_panels(ctx, nx * Nv, ny * Nv, NG, sl[n].p(), NG, slT[m].p(), NG, nx,
+                             Nv, Vp);
+          OTen Rxy(ctx, {nx, ny, No, No});                         // :443
+          emu_gemm_panels(ctx, Vp, 0, Xq, 0, 1.0, 0.0, Rxy.p(), nx * ny);
+          slice_add(ctx, R2.p, Rxy.p(), Nv, No, a0, b0, nx, ny, a0 > b0);  // :444-447
+        }
+      }
+    }
     EmuPanels Xp;
-    if (emulated(s * s, No * No, Nv * Nv))
+    if (!fused && emulated(s * s, No * No, Nv * Nv))
       Xp = emu_split(ctx, false, X.p(), No * No, Nv * Nv, Nv * Nv, 1, 1, 0);
-    for (int64_t m = 0; m < ns; ++m) {                             // :418
+    for (int64_t m = 0; m < ns && !fused; ++m) {                   // :418
       for (int64_t n = m; n < ns; ++n) {                           // :419
         const int64_t nx = sl[n].t.lens[1], ny = sl[m].t.lens[1];
         OTen Vs(ctx, {nx, ny, Nv, Nv});                            // :425-434

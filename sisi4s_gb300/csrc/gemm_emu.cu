@@ -241,6 +241,14 @@ __device__ __forceinline__ double scaled_total(long long t, int e, const OutScal
   return fixed_to_double(t, e) * o.alpha;
 }
 
+// bf16 bits of a small integer v (|v| <= 2^8: exact in bf16), FP32-pipe
+// and integer instructions only: the magic-number add makes the float v
+// exactly, and its upper 16 bits are the bf16 encoding.
+__device__ __forceinline__ uint32_t small_int_bf16_bits(int v) {
+  const float f = __int_as_float(0x4B400000 + v) - 12582912.0f;  // 1.5 * 2^23
+  return __float_as_uint(f) >> 16;
+}
+
 // One problem of a grouped launch: many GEMMs of the same M, N, K whose
 // operands are panels of the same families (different operand indices) and
 // whose outputs are different arrays.
@@ -279,6 +287,17 @@ struct EmuArgs {
   // plain GEMM.  Grouped launches have ksplit = 1.
   int nprob = 1;
   const EmuProb *probs = nullptr;
+  // digit-panel output (the particle ladder): instead of C, the product
+  // V[(x,c),(d,y)] is written as the S bf16 digits of the A operand of the
+  // next product, rows r = x + px*y, K index k = d + pd*c (m = x + px*c,
+  // n = d + pd*y), with the row exponents pexp[r] given (max|V| < 2^pexp[r]);
+  // tiles [S][prt][pkt] of TM rows x KB k as split_kernel writes them.
+  // Needs beta = 0, ksplit = 1, pd a multiple of 16.
+  __nv_bfloat16 *pout = nullptr;
+  const int *pexp = nullptr;
+  int prt = 0, pkt = 0;
+  unsigned px = 0, pd = 0;
+  int64_t pplane = 0;
 };
 
 // pointers of problem q (the plain GEMM's own for a single problem)
@@ -604,6 +623,65 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) emu_gemm_kernel(EmuArgs a) {
             }
           }
         } else {
+        if (a.pout) {
+          // digit-panel output: this thread's 16 columns are 16 consecutive d
+          // of one y, so each digit of each 8-column half is one 16-byte
+          // row segment of a panel tile
+          // n0 is the same for the whole warp; rows past M only skip their
+          // stores, so that every lane takes part in the shuffles below
+          if (n0 >= a.N) continue;
+          const unsigned mu = mrow ? (unsigned)m : 0u, nu = (unsigned)n0;
+          const unsigned x = mu % a.px, c = mu / a.px;
+          const unsigned d0 = nu % a.pd, y = nu / a.pd;
+          const unsigned r = x + a.px * y;
+          const unsigned k0 = d0 + a.pd * c;
+          const int er = mrow ? a.pexp[r] : EXP_FLOOR - 1;
+          const int F = 7 * S;
+          long long bias = 0;
+#pragma unroll
+          for (int q = 1; q < S; ++q) bias += 64LL << (7 * (S - 1 - q));
+          const unsigned rr = r % TM, tr = r / TM;
+          const unsigned tk = k0 / KB, kk0 = k0 % KB;  // kk0 is 0 or 16
+          const int64_t off0 = ((int64_t)tr * a.pkt + tk) * (TM * KB) +
+                               (int64_t)(((rr / 8) * (KB / 8) + kk0 / 8) * 64 + (rr % 8) * 8);
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            uint32_t packed[S][4];
+#pragma unroll
+            for (int jj = 0; jj < 8; ++jj) {
+              const int j = 8 * h + jj;
+              const int eb = __shfl_sync(0xffffffffu, ebl, j);
+              const long long t = tot[j];
+              long long X = 0;
+              if (t != 0 && er >= EXP_FLOOR) {
+                const int sh = ea + eb + F - er;
+                const unsigned long long mag =
+                    t < 0 ? 0ull - (unsigned long long)t : (unsigned long long)t;
+                unsigned long long xm;
+                if (sh >= 0) xm = sh > 62 ? 0ull : (mag << sh);
+                else if (sh <= -63) xm = 0ull;
+                else xm = (mag + (1ull << (-sh - 1))) >> (-sh);
+                X = t < 0 ? -(long long)xm : (long long)xm;
+              }
+              const long long Y = X + bias;
+#pragma unroll
+              for (int q = 0; q < S; ++q) {
+                const int dg = q == 0 ? (int)(Y >> (7 * (S - 1)))
+                                      : (int)((Y >> (7 * (S - 1 - q))) & 127) - 64;
+                const uint32_t bits = small_int_bf16_bits(dg);
+                if (jj % 2 == 0) packed[q][jj / 2] = bits;
+                else packed[q][jj / 2] |= bits << 16;
+              }
+            }
+            if (mrow) {
+#pragma unroll
+              for (int q = 0; q < S; ++q)
+                *reinterpret_cast<uint4 *>(a.pout + q * a.pplane + off0 + 64 * h) =
+                    make_uint4(packed[q][0], packed[q][1], packed[q][2], packed[q][3]);
+            }
+          }
+          continue;
+        }
         if (a.mapped) {
           // permuted output layout, beta = 0 (host-checked): row offset once,
           // column offsets stepped through the mixed radix of n; every lane
@@ -720,13 +798,6 @@ __device__ __forceinline__ long long to_fixed(double x, int e, int F) {
   return (bits >> 63) ? -X : X;
 }
 
-// bf16 bits of a small integer v (|v| <= 2^8: exact in bf16), FP32-pipe
-// and integer instructions only: the magic-number add makes the float v
-// exactly, and its upper 16 bits are the bf16 encoding.
-__device__ __forceinline__ uint32_t small_int_bf16_bits(int v) {
-  const float f = __int_as_float(0x4B400000 + v) - 12582912.0f;  // 1.5 * 2^23
-  return __float_as_uint(f) >> 16;
-}
 
 // digits of one operand into tiles [S][rt][kt] of TR rows x 32 k.
 // One thread writes one 16-byte core-matrix row (8 consecutive k) per digit.
@@ -778,6 +849,40 @@ __global__ void split_kernel(const double *__restrict__ base, int64_t R,
       *reinterpret_cast<uint4 *>(out + s * plane + off) =
           make_uint4(packed[s][0], packed[s][1], packed[s][2], packed[s][3]);
   }
+}
+
+// Row-exponent bound of the ladder's V blocks.  amax[a] = max_c ||dG[., a, c]||
+// over the columns of the dressed vertex dG [G, Nv, Nv] (G fastest), one warp
+// per (a, c); the maximum is taken on the IEEE bits of the non-negative
+// norms (their integer order), so it does not depend on the order.
+__global__ void column_norm_max_kernel(const double *__restrict__ dG, int64_t G,
+                                       int64_t ncol, int64_t Nv,
+                                       unsigned long long *__restrict__ amax) {
+  const int64_t col = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
+  const int lane = threadIdx.x % 32;
+  if (col >= ncol) return;
+  const double *p = dG + col * G;
+  double s = 0.0;
+  for (int64_t g = lane; g < G; g += 32) s = fma(p[g], p[g], s);
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0)
+    atomicMax(&amax[col % Nv], (unsigned long long)__double_as_longlong(sqrt(s)));
+}
+
+// er[x + nx y] = exponent e with amax[x0 + x] amax[y0 + y] (1 + 2^-20) < 2^e:
+// by Cauchy-Schwarz |V[x,y,c,d]| = |sum_G dG[G,x,c] dG[G,y,d]| is below it (the
+// factor covers the rounding of the norms and of the operands' digits).  A
+// zero bound keeps the "zero row" sentinel.
+__global__ void ladder_row_exponent_kernel(const unsigned long long *__restrict__ amax,
+                                           int64_t x0, int64_t nx, int64_t y0, int64_t ny,
+                                           int *__restrict__ er) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nx * ny) return;
+  const int64_t x = r % nx, y = r / nx;
+  const double b = __longlong_as_double((long long)amax[x0 + x]) *
+                   __longlong_as_double((long long)amax[y0 + y]) * (1.0 + 0x1p-20);
+  const int e = frexp_exponent(b);
+  er[r] = e == INT_MIN ? (int)0x80808080 : e;
 }
 
 // out = alpha * 2^(ea+eb-14-frac) * sum_s W[s] + beta * C, summing the exact
@@ -1149,6 +1254,135 @@ void emu_gemm_panels_grouped(Context &ctx, const EmuPanels &A, const int *ia,
     case 8: gemm_panels_grouped<8>(ctx, A, ia, B, ib, nprob, alpha, beta, C, Cdf, ldc); break;
     default: throw Error(GBCC_BAD_ARG, "emu_slices must be in [4, 8]");
   }
+}
+
+EmuPanels emu_panels_alloc(Context &ctx, bool role_a, int64_t R, int64_t K) {
+  require(R > 0 && K > 0, "emu_panels_alloc: empty operand");
+  EmuPanels P;
+  P.role_a = role_a;
+  P.S = ctx.emu_slices;
+  P.rows = R;
+  P.K = K;
+  P.count = 1;
+  P.rt = (int)((R + (role_a ? TM : TN) - 1) / (role_a ? TM : TN));
+  P.kt = (int)((K + KB - 1) / KB);
+  P.panels.alloc(ctx, (size_t)P.S * P.rt * P.kt * (role_a ? A_TILE : B_TILE));
+  P.exps.alloc(ctx, sizeof(int) * (size_t)R);
+  return P;
+}
+
+void ladder_amax(Context &ctx, const double *dG, int64_t G, int64_t Nv, void *amax) {
+  GBCC_CUDA(cudaMemsetAsync(amax, 0, sizeof(unsigned long long) * Nv, ctx.stream));
+  const int64_t ncol = Nv * Nv;
+  column_norm_max_kernel<<<(unsigned)((ncol * 32 + 255) / 256), 256, 0, ctx.stream>>>(
+      dG, G, ncol, Nv, static_cast<unsigned long long *>(amax));
+  GBCC_CHECK_LAUNCH(ctx);
+}
+
+void ladder_row_exponents(Context &ctx, const void *amax, int64_t x0, int64_t nx, int64_t y0,
+                          int64_t ny, int *er) {
+  const int64_t R = nx * ny;
+  ladder_row_exponent_kernel<<<(unsigned)((R + 255) / 256), 256, 0, ctx.stream>>>(
+      static_cast<const unsigned long long *>(amax), x0, nx, y0, ny, er);
+  GBCC_CHECK_LAUNCH(ctx);
+}
+
+namespace {
+template <int S>
+void run_emu_to_panels(Context &ctx, int64_t M, int64_t N, int64_t K, const double *A,
+                       int64_t lda, const double *B, int64_t ldb, unsigned px, unsigned pd,
+                       EmuPanels &P) {
+  const EmuPlan pl = emu_plan(S, M, N, K, ctx.sm_count, false);
+  const int mt = pl.mt, nt = pl.nt, kt = pl.kt;
+  require((int64_t)mt * nt < (1LL << 31), "emu gemm: grid too large");
+  // op(A)(m, k) = A[k + m lda], op(B)^T(n, k) = B[k + n ldb]
+  DBuf ea(ctx, sizeof(int) * M), eb(ctx, sizeof(int) * N);
+  DBuf asl(ctx, (size_t)S * mt * kt * A_TILE), bsl(ctx, (size_t)S * nt * kt * B_TILE);
+  auto exponents = [&](const double *p, int64_t R, int64_t rs, int *e) {
+    GBCC_CUDA(cudaMemsetAsync(e, 0x80, sizeof(int) * R, ctx.stream));
+    const int64_t kchunk = std::max<int64_t>(1024, (K + 4095) / 4096);
+    const dim3 grid((unsigned)((R + 7) / 8), (unsigned)((K + kchunk - 1) / kchunk));
+    exponent_rows_warp_kernel<<<grid, 256, 0, ctx.stream>>>(p, R, K, rs, 1, kchunk, e);
+    GBCC_CHECK_LAUNCH(ctx);
+  };
+  exponents(A, M, lda, ea.as<int>());
+  exponents(B, N, ldb, eb.as<int>());
+  auto grid_for = [&](int64_t segs) {
+    require(segs < (1LL << 31), "emulated GEMM: operand too large to split");
+    int64_t g = (segs + 255) / 256;
+    const int64_t cap = (int64_t)std::max(ctx.sm_count, 1) * 16;
+    return (unsigned)std::max<int64_t>(1, std::min(g, cap));
+  };
+  split_kernel<S, TM><<<grid_for((int64_t)mt * TM * kt * 4), 256, 0, ctx.stream>>>(
+      A, M, K, lda, 1, ea.as<int>(), mt, kt, asl.as<__nv_bfloat16>());
+  GBCC_CHECK_LAUNCH(ctx);
+  split_kernel<S, TN><<<grid_for((int64_t)nt * TN * kt * 4), 256, 0, ctx.stream>>>(
+      B, N, K, ldb, 1, eb.as<int>(), nt, kt, bsl.as<__nv_bfloat16>());
+  GBCC_CHECK_LAUNCH(ctx);
+  // rows past R are never written: give them the digits of zero
+  if (P.rows % TM != 0)
+    GBCC_CUDA(cudaMemsetAsync(P.panels.as<void>(), 0, P.panels.bytes(), ctx.stream));
+  constexpr int STAGE_BYTES = S * (A_TILE + B_TILE);
+  constexpr int STAGES = (SMEM_BUDGET / STAGE_BYTES) > 4 ? 4 : (SMEM_BUDGET / STAGE_BYTES);
+  const int smem = STAGES * STAGE_BYTES;
+  GBCC_CUDA(cudaFuncSetAttribute(emu_gemm_kernel<S, false>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  EmuArgs args{};
+  args.A = asl.as<__nv_bfloat16>();
+  args.B = bsl.as<__nv_bfloat16>();
+  args.ea = ea.as<int>();
+  args.eb = eb.as<int>();
+  args.M = M; args.N = N; args.ldc = 0;
+  args.mt = mt; args.nt = nt; args.kt = kt;
+  args.kc_blocks = pl.kc_blocks;
+  args.kb_per_split = pl.kb_per_split;
+  args.ksplit = 1;
+  args.frac = pl.frac;
+  args.os = out_scale(1.0);
+  args.inject_wait = ctx.take_fault(GBCC_FAULT_DEVICE_WAIT) ? 1 : 0;
+  args.beta = 0.0;
+  args.err = ctx.device_error_word();
+  args.pout = P.panels.as<__nv_bfloat16>();
+  args.pexp = P.exps.as<int>();
+  args.prt = P.rt;
+  args.pkt = P.kt;
+  args.px = px;
+  args.pd = pd;
+  args.pplane = (int64_t)P.rt * P.kt * TM * KB;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  if (ctx.prof) {
+    ev0 = ctx.prof_event();
+    ev1 = ctx.prof_event();
+    GBCC_CUDA(cudaEventRecord(ev0, ctx.stream));
+  }
+  emu_gemm_kernel<S, false><<<emu_grid(ctx, (int64_t)mt * nt), NUM_THREADS, smem,
+                              ctx.stream>>>(args);
+  GBCC_CHECK_LAUNCH(ctx);
+  if (ctx.prof) {
+    GBCC_CUDA(cudaEventRecord(ev1, ctx.stream));
+    const double f = 2.0 * (double)M * (double)N * (double)K;
+    ctx.prof_recs.push_back({ev0, ev1, f * S * (S + 1) / 2.0, f, M, N, K});
+  }
+}
+}  // namespace
+
+void gemm_emu_to_panels(Context &ctx, int64_t M, int64_t N, int64_t K, const double *A,
+                        int64_t lda, const double *B, int64_t ldb, int64_t px, int64_t pd,
+                        EmuPanels &P) {
+  require(P.role_a && P.count == 1 && P.S == ctx.emu_slices, "gemm_emu_to_panels: panels");
+  require(px > 0 && pd > 0 && pd % 16 == 0 && M % px == 0 && N % pd == 0,
+          "gemm_emu_to_panels: shape");
+  require(P.rows == px * (N / pd) && P.K == pd * (M / px), "gemm_emu_to_panels: panel shape");
+  require(M < (1LL << 31) && N < (1LL << 31), "gemm_emu_to_panels: size");
+  switch (ctx.emu_slices) {
+    case 4: run_emu_to_panels<4>(ctx, M, N, K, A, lda, B, ldb, (unsigned)px, (unsigned)pd, P); break;
+    case 5: run_emu_to_panels<5>(ctx, M, N, K, A, lda, B, ldb, (unsigned)px, (unsigned)pd, P); break;
+    case 6: run_emu_to_panels<6>(ctx, M, N, K, A, lda, B, ldb, (unsigned)px, (unsigned)pd, P); break;
+    case 7: run_emu_to_panels<7>(ctx, M, N, K, A, lda, B, ldb, (unsigned)px, (unsigned)pd, P); break;
+    case 8: run_emu_to_panels<8>(ctx, M, N, K, A, lda, B, ldb, (unsigned)px, (unsigned)pd, P); break;
+    default: throw Error(GBCC_BAD_ARG, "emu_slices must be in [4, 8]");
+  }
+  ctx.flops += 2.0 * (double)M * (double)N * (double)K;
 }
 
 EmuPanels emu_split(Context &ctx, bool role_a, const double *base, int64_t R,

@@ -202,6 +202,59 @@ void gemm_emu_mapped(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64
   });
 }
 
+EmuPanels emu_panels_alloc(Context &ctx, bool role_a, int64_t R, int64_t K) {
+  require(R > 0 && K > 0, "emu_panels_alloc: empty operand");
+  EmuPanels P;
+  P.role_a = role_a;
+  P.S = ctx.emu_slices;
+  P.rows = R;
+  P.K = K;
+  P.count = 1;
+  P.panels.alloc(ctx, sizeof(double) * (size_t)R * K);
+  P.exps.alloc(ctx, sizeof(int) * (size_t)R);
+  return P;
+}
+
+// the V product stored as the next product's operand, panels[k][r] with
+// r = x + px y, k = d + pd c (m = x + px c, n = d + pd y)
+void gemm_emu_to_panels(Context &ctx, int64_t M, int64_t N, int64_t K, const double *A,
+                        int64_t lda, const double *B, int64_t ldb, int64_t px, int64_t pd,
+                        EmuPanels &P) {
+  require(P.role_a && P.count == 1 && P.S == ctx.emu_slices, "gemm_emu_to_panels: panels");
+  require(px > 0 && pd > 0 && pd % 16 == 0 && M % px == 0 && N % pd == 0,
+          "gemm_emu_to_panels: shape");
+  require(P.rows == px * (N / pd) && P.K == pd * (M / px), "gemm_emu_to_panels: panel shape");
+  ctx.flops += 2.0 * (double)M * (double)N * (double)K;
+  double *out = P.panels.as<double>();
+  const int64_t R = P.rows;
+  launch(ctx, [=]() {
+    for (int64_t n = 0; n < N; ++n)
+      for (int64_t m = 0; m < M; ++m) {
+        double acc = 0.0;
+        for (int64_t k = 0; k < K; ++k) acc += A[k + m * lda] * B[k + n * ldb];
+        const int64_t x = m % px, c = m / px, d = n % pd, y = n / pd;
+        out[(x + px * y) + R * (d + pd * c)] = acc;
+      }
+  });
+}
+
+// the bound kernels only set digit exponents, which the FP64 model ignores
+void ladder_amax(Context &ctx, const double *dG, int64_t G, int64_t Nv, void *amax) {
+  (void)dG; (void)G;
+  double *a = static_cast<double *>(amax);
+  launch(ctx, [=]() {
+    for (int64_t i = 0; i < Nv; ++i) a[i] = 0.0;
+  });
+}
+
+void ladder_row_exponents(Context &ctx, const void *amax, int64_t x0, int64_t nx, int64_t y0,
+                          int64_t ny, int *er) {
+  (void)amax; (void)x0; (void)y0;
+  launch(ctx, [=]() {
+    for (int64_t r = 0; r < nx * ny; ++r) er[r] = 0;
+  });
+}
+
 void gemm_emu_noalloc(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
                       double alpha, const double *A, int64_t lda, const double *B,
                       int64_t ldb, double beta, double *C, int64_t ldc) {
