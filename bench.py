@@ -71,10 +71,12 @@ METRIC = "RCCSD iter/s mixed vs FP64 at |dE|<=1uHa; batched solves/s, p50/p99 la
 UNIT = "iter/s"
 REF_MAX_STEPS = 3
 FIXTURE = os.path.join(ROOT, "tests", "golden", "c2_trajectory.json")
-# DRAM bytes (read + write) per bf16 tensor flop of the emulated GEMM, from an
-# ncu capture of the same kernel (dram__bytes_read.sum + dram__bytes_write.sum
-# over 21 * 2 * 4096^3 flop at M = N = K = 4096 with 6 digits)
-EMU_GEMM_DRAM_PER_FLOP = (1.942e9 + 0.153e9) / (21 * 2.0 * 4096 ** 3)
+# DRAM bytes (read + write) per bf16 tensor flop of the emulated GEMM, from a
+# one-pass ncu capture of the same kernel on this workload
+# (dram__bytes_read.sum + dram__bytes_write.sum of 12 consecutive ladder
+# launches, V = G.G at 8192 x 8192 x 1024 and R = V.X at 1024 x 1024 x 65536,
+# 21 * 2 * 8192^2 * 1024 bf16 flop each: 17.458e9 + 5.292e9 bytes)
+EMU_GEMM_DRAM_PER_FLOP = (17.458e9 + 5.292e9) / (12 * 21 * 2.0 * 8192 ** 2 * 1024)
 
 
 def _peaks():
@@ -580,8 +582,9 @@ def main():
                 "gemm_share_of_step": gs["ms"] / prof_ms if prof_ms else None,
                 "traffic": EMU_GEMM_DRAM_PER_FLOP * gs["tc_flops"] / gs["launches"],
                 "traffic_unit": "bytes per launch",
-                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum at "
-                                  "M = N = K = 4096, scaled by work per launch"}
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of "
+                                  "the ladder's launches on this workload, per bf16 flop, "
+                                  "scaled to the average launch's work"}
 
     serving = None
     if not args.no_serve:
