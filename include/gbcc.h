@@ -85,6 +85,13 @@ gbcc_status gbcc_ctx_set_triples_batch(gbcc_ctx *ctx, int max_images);
  * f64_blocks_per_sm >= 0, emu_max_ksplit in [1, 64].  No counterpart in the
  * reference. */
 gbcc_status gbcc_ctx_set_splits(gbcc_ctx *ctx, int f64_blocks_per_sm, int emu_max_ksplit);
+/* Precision mode: a solver's integrals and vertex blocks do not change
+ * during the solve, so the digit panels split from them (one set per layout
+ * the contractions use, at most 12 GiB per context) are kept and reused
+ * (enable = 1, the default) instead of being permuted and split again in
+ * every iteration.  Results are the same bits either way.  No counterpart in
+ * the reference. */
+gbcc_status gbcc_ctx_set_operand_cache(gbcc_ctx *ctx, int enable);
 
 /* Replay of steady-state CCSD iterations as captured CUDA graphs (default on;
  * off runs every iteration eagerly).  Results are identical either way. */

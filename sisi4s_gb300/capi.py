@@ -88,6 +88,7 @@ _SIGS = {
     "gbcc_ctx_set_emulation": (C.c_int, [C.c_void_p, C.c_int, C.c_double]),
     "gbcc_ctx_set_triples_batch": (C.c_int, [C.c_void_p, C.c_int]),
     "gbcc_ctx_set_splits": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "gbcc_ctx_set_operand_cache": (C.c_int, [C.c_void_p, C.c_int]),
     "gbcc_ctx_profile": (C.c_int, [C.c_void_p, C.c_int]),
     "gbcc_ctx_set_graphs": (C.c_int, [C.c_void_p, C.c_int]),
     "gbcc_ctx_gemm_stats": (C.c_int, [C.c_void_p, _dp, C.POINTER(C.c_int64),
@@ -218,6 +219,10 @@ class Context:
         """K-split policies of the FP64 and emulated GEMMs (defaults shown)."""
         self.check(self.lib.gbcc_ctx_set_splits(self.h, int(f64_blocks_per_sm),
                                                 int(emu_max_ksplit)))
+
+    def set_operand_cache(self, enable=True):
+        """Reuse of the digit panels of a solver's constant operands."""
+        self.check(self.lib.gbcc_ctx_set_operand_cache(self.h, int(bool(enable))))
 
     def set_graphs(self, enable=True):
         self.check(self.lib.gbcc_ctx_set_graphs(self.h, 1 if enable else 0))

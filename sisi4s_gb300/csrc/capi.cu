@@ -185,6 +185,12 @@ void *gbcc_ctx_stream(const gbcc_ctx *ctx) {
   return ctx ? static_cast<void *>(ctx->c.stream) : nullptr;
 }
 
+gbcc_status gbcc_ctx_set_operand_cache(gbcc_ctx *ctx, int enable) {
+  if (!ctx) return GBCC_BAD_ARG;
+  ctx->c.use_panel_cache = enable != 0;
+  return GBCC_OK;
+}
+
 gbcc_status gbcc_ctx_set_splits(gbcc_ctx *ctx, int f64_blocks_per_sm, int emu_max_ksplit) {
   if (!ctx || f64_blocks_per_sm < 0 || emu_max_ksplit < 1 || emu_max_ksplit > 64)
     return GBCC_BAD_ARG;

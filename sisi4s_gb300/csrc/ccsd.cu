@@ -118,6 +118,11 @@ std::unique_ptr<CcsdInputs> upload_inputs(Context &ctx, const gbcc_ccsd_in &in,
       contract(ctx, 1.0, p->Gab, "Gac", p->Gai, "Gbi", 0.0, p->Vabci, "abci", precision);
     }
   }
+  // unchanged for the solver's life: their digit panels are split once
+  p->ctx = &ctx;
+  for (const OTen *t : {&p->Vabij, &p->Vx, &p->Vaibj, &p->Vijkl, &p->Vijka, &p->Gai,
+                        &p->Gab, &p->Gij})
+    if (t->p()) ctx.register_constant(t->p(), sizeof(double) * (size_t)t->t.size());
   if (in.fock_hp) {
     // f[i,a] is kept as f[a,i], so the noncanonical energy term is a plain
     // dot with T1[a,i]
@@ -129,6 +134,12 @@ std::unique_ptr<CcsdInputs> upload_inputs(Context &ctx, const gbcc_ccsd_in &in,
     GBCC_CUDA(cudaStreamSynchronize(ctx.stream));
   }
   return p;
+}
+
+CcsdInputs::~CcsdInputs() {
+  if (!ctx) return;
+  for (const OTen *t : {&Vabij, &Vx, &Vaibj, &Vijkl, &Vijka, &Gai, &Gab, &Gij})
+    if (t->p()) ctx->forget_constant(t->p());
 }
 
 Ccsd::Ccsd(Context &ctx, std::unique_ptr<CcsdInputs> in,

@@ -9,6 +9,9 @@
 namespace gbcc {
 
 struct CcsdInputs {
+  Context *ctx = nullptr;     // the integrals and vertex blocks are registered
+                              // as constants of this context while alive
+  ~CcsdInputs();
   int64_t No = 0, Nv = 0, NG = 0;
   OTen eps_h, eps_p;          // [No], [Nv]
   OTen Gai, Gab, Gij;         // [NG,Nv,No], [NG,Nv,Nv], [NG,No,No]

@@ -8,7 +8,9 @@
 // indices already form [M|K] / [K|M] blocks are used in place (op N / op T)
 // and C is written directly when its indices form [M|N] (or [N|M], by
 // computing the transposed product).
+#include <cstdio>
 #include <cstring>
+#include <memory>
 #include <string>
 
 #include "internal.hpp"
@@ -37,6 +39,91 @@ int64_t prod(const std::string &s, const int64_t *len) {
 }
 
 }  // namespace
+
+// The plan of contract() with emulated panels, for a contraction with a
+// registered constant operand: the constant operand's panels (after its
+// permutation, if the plan has one) are split once per layout and role and
+// kept in the context; the other operand is permuted and split as usual.
+// The digits are those the plain route would produce, so the result is the
+// same bit for bit.
+void contract_cached(Context &ctx, double alpha, const Ten &A, const std::string &sa,
+                     const Ten &B, const std::string &sb, double beta, const Ten &C,
+                     const std::string &sc, const std::string &m, const std::string &n,
+                     const std::string &k, bool permA, bool ta, bool permB, bool tb,
+                     bool permC, bool swap, const int64_t *len) {
+  const int64_t sM = prod(m, len), sN = prod(n, len), sK = prod(k, len);
+  // panels of one operand: tensor T (index string st), GEMM order `order`
+  // (permuted into it when perm), matrix with `rows` rows, element (r, q) at
+  // r*rs + q*ks of the GEMM-ready buffer
+  auto panels = [&](const Ten &T, const std::string &st, bool perm, const std::string &order,
+                    bool role_a, int64_t rows, int64_t rs, int64_t ks)
+      -> std::shared_ptr<EmuPanels> {
+    const bool constant = ctx.is_constant(T.p, sizeof(double) * T.size());
+    std::string key;
+    if (constant) {
+      char buf[64];
+      std::snprintf(buf, sizeof buf, "%p", (const void *)T.p);
+      key = std::string(buf) + "|" + st + ">" + order + "|" + (role_a ? "A" : "B") + "|" +
+            std::to_string(rows) + "|" + std::to_string(rs) + "|" + std::to_string(ks) +
+            "|" + std::to_string(ctx.emu_slices);
+      auto it = ctx.panel_cache.find(key);
+      if (it != ctx.panel_cache.end()) return it->second.panels;
+    }
+    const double *base = T.p;
+    OTen tmp;
+    if (perm) {
+      tmp = OTen(ctx, {T.size()});
+      Ten t = T;
+      t.p = tmp.p();
+      for (size_t d = 0; d < order.size(); ++d) t.lens[d] = len[(unsigned char)order[d]];
+      assign(ctx, 1.0, T, st.c_str(), 0.0, t, order.c_str());
+      base = t.p;
+    }
+    auto P = std::make_shared<EmuPanels>(
+        emu_split(ctx, role_a, base, rows, sK, rs, ks, 1, 0));
+    if (constant) {
+      cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+      const size_t bytes = P->panels.bytes() + P->exps.bytes();
+      // never keep buffers allocated inside a stream capture
+      if (cudaStreamIsCapturing(ctx.stream, &cs) == cudaSuccess &&
+          cs == cudaStreamCaptureStatusNone &&
+          ctx.panel_cache_bytes + bytes <= Context::PANEL_CACHE_LIMIT) {
+        ctx.panel_cache[key] = {T.p, P, bytes};
+        ctx.panel_cache_bytes += bytes;
+      }
+    }
+    return P;
+  };
+  // op(A)(m, k): from A's buffer in order m+k (ta = 0) or k+m (ta = 1)
+  const std::string oa = permA ? m + k : sa;
+  const bool tA = permA ? false : ta;
+  const int64_t lda = tA ? sK : sM;
+  // op(B)(k, n): order k+n (tb = 0) or n+k (tb = 1)
+  const std::string ob = permB ? k + n : sb;
+  const bool tB = permB ? false : tb;
+  const int64_t ldb = tB ? sN : sK;
+  // kernel roles: C = A_role (rows M) x B_role (rows N)^T, or the transposed
+  // product when the plan computes C^T
+  auto PA = panels(A, sa, permA, oa, !swap, sM, tA ? lda : 1, tA ? 1 : lda);
+  auto PB = panels(B, sb, permB, ob, swap, sN, tB ? 1 : ldb, tB ? ldb : 1);
+  double *pc = C.p;
+  double gbeta = beta;
+  OTen tc;
+  if (permC) {
+    tc = OTen(ctx, {C.size()});
+    pc = tc.p();
+    gbeta = 0.0;
+  }
+  if (!swap) emu_gemm_panels(ctx, *PA, 0, *PB, 0, alpha, gbeta, pc, sM);
+  else emu_gemm_panels(ctx, *PB, 0, *PA, 0, alpha, gbeta, pc, sN);
+  if (permC) {
+    Ten t = C;
+    t.p = pc;
+    const std::string o = m + n;
+    for (size_t d = 0; d < o.size(); ++d) t.lens[d] = len[(unsigned char)o[d]];
+    assign(ctx, 1.0, t, o.c_str(), beta, C, sc.c_str());
+  }
+}
 
 void assign(Context &ctx, double alpha, const Ten &A, const char *ia,
             double beta, const Ten &C, const char *ic) {
@@ -122,6 +209,14 @@ void contract(Context &ctx, double alpha, const Ten &A, const char *ia,
         if (p.cost < best.cost) best = p;
       }
   const Plan &p = best;
+  if (ctx.use_panel_cache && precision == GBCC_PREC_EMU && sK > 0 && sM > 1 && sN > 1 &&
+      2.0 * (double)sM * (double)sN * (double)sK >= ctx.emu_min_flops &&
+      (ctx.is_constant(A.p, sizeof(double) * A.size()) ||
+       ctx.is_constant(B.p, sizeof(double) * B.size()))) {
+    contract_cached(ctx, alpha, A, sa, B, sb, beta, C, sc, p.m, p.n, p.k, p.permA, p.ta,
+                    p.permB, p.tb, p.permC, p.swap, len);
+    return;
+  }
   // operand A as a [M,K] (ta=0) or [K,M] (ta=1) matrix
   const double *pa = A.p;
   int64_t lda = p.ta ? sK : sM;

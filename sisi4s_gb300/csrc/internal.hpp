@@ -6,6 +6,8 @@
 
 #include <array>
 #include <atomic>
+#include <map>
+#include <memory>
 #include <cstdint>
 #include <stdexcept>
 #include <string>
@@ -44,6 +46,8 @@ inline void require(bool ok, const std::string &msg) {
   if (!ok) throw Error(GBCC_BAD_ARG, msg);
 }
 
+struct EmuPanels;
+
 struct Context {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -66,6 +70,49 @@ struct Context {
   // (T): distinct triple images whose W products share one batch (one W
   // slot of Nv^3 doubles each); 0 = from the free device memory
   int triples_batch_images = 0;
+  // Tensors that stay unchanged while registered (a solver's integrals and
+  // vertex blocks): the contraction engine keeps the digit panels it splits
+  // from them, one set per layout, and reuses them instead of permuting and
+  // splitting again.  Entries are dropped when their tensor is forgotten.
+  struct ConstRange {
+    const double *p;
+    size_t bytes;
+  };
+  std::vector<ConstRange> const_tensors;
+  struct CachedPanels {
+    const double *owner;
+    std::shared_ptr<EmuPanels> panels;
+    size_t bytes;
+  };
+  std::map<std::string, CachedPanels> panel_cache;
+  size_t panel_cache_bytes = 0;
+  bool use_panel_cache = true;
+  static constexpr size_t PANEL_CACHE_LIMIT = (size_t)12 << 30;
+  void register_constant(const double *p, size_t bytes) {
+    if (p && bytes) const_tensors.push_back({p, bytes});
+  }
+  bool is_constant(const double *p, size_t bytes) const {
+    for (const auto &r : const_tensors)
+      if (p >= r.p && (const char *)(p) + bytes <= (const char *)(r.p) + r.bytes) return true;
+    return false;
+  }
+  void forget_constant(const double *p) {
+    for (size_t i = 0; i < const_tensors.size(); ++i) {
+      if (const_tensors[i].p != p) continue;
+      const char *lo = (const char *)p, *hi = lo + const_tensors[i].bytes;
+      for (auto it = panel_cache.begin(); it != panel_cache.end();) {
+        const char *o = (const char *)it->second.owner;
+        if (o >= lo && o < hi) {
+          panel_cache_bytes -= it->second.bytes;
+          it = panel_cache.erase(it);
+        } else {
+          ++it;
+        }
+      }
+      const_tensors.erase(const_tensors.begin() + i);
+      return;
+    }
+  }
   // injected fault (GBCC_FAULT_*), consumed by the first matching event
   // (never while the stream is being captured into a graph: the fault would
   // be baked into every replay)

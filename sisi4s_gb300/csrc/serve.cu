@@ -71,7 +71,9 @@ size_t estimate_bytes(const gbcc_ccsd_in &in, const gbcc_ccsd_opts &o, int tripl
   // Nv^4 tensor) and a permuted copy of Vabci
   if (o.formulation == 1) words += 1.0 * Nv * Nv * Nv * Nv + 2.0 * Nv * Nv * Nv * No;
   double bytes = 8.0 * words;
-  if (o.precision == GBCC_PREC_EMU) bytes *= 1.6;      // digit panels
+  // digit panels, including those kept for the constant integrals and
+  // vertex blocks (one set per layout the contractions use)
+  if (o.precision == GBCC_PREC_EMU) bytes *= 2.4;
   return (size_t)(1.5 * bytes) + (64u << 20);
 }
 

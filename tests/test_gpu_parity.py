@@ -301,3 +301,33 @@ def test_triples_batching_does_not_change_the_bits(ctx, precision):
     assert got.count(got[0]) == len(got), got
     tol = 1e-12 if precision == "fp64" else 1e-10
     assert abs(got[0] - ref) < tol * max(1.0, abs(ref))
+
+
+@pytest.mark.parametrize("mixer", ["DiisMixer", "LinearMixer"])
+def test_operand_cache_gives_the_same_bits(ctx, mixer):
+    """Precision mode keeps the digit panels of the integrals and vertex blocks
+    (constant for a solve) instead of splitting them in every iteration; the
+    iterations, captured graphs included, give the same bits with and without
+    the cache, and so does (T)."""
+    s = make_system(4, 32, 90, seed=61)
+    kw = dict(mixer=mixer, max_residua=3, mixing_ratio=0.8, max_iterations=8,
+              energy_convergence=0.0, amplitudes_convergence=0.0, precision="emu")
+    ctx.set_emulation(6, 1e4)
+    out = []
+    try:
+        for enable in (False, True):
+            ctx.set_operand_cache(enable)
+            sol = gpu.Solver(ctx, s.eps_h, s.eps_p, s.gamma, **kw)
+            try:
+                sol.step(8)
+                r = sol.result()
+                r["et"] = sol.triples("emu")[0]
+            finally:
+                sol.close()
+            out.append(r)
+    finally:
+        ctx.set_operand_cache(True)
+        ctx.set_emulation(6, 1e7)
+    assert np.array_equal(out[0]["history"], out[1]["history"])
+    assert np.array_equal(out[0]["T2"], out[1]["T2"])
+    assert out[0]["et"] == out[1]["et"]
