@@ -359,7 +359,7 @@ void Ccsd::residual(int it, const double *Tp, double *Rp) {
     auto emulated = [&](int64_t M, int64_t N, int64_t K) {
       return emu && 2.0 * (double)M * (double)N * (double)K >= ctx.emu_min_flops;
     };
-    // Fused form (every pair emulated, Nv a multiple of 16): each V block
+    // Fused form (every pair emulated, Nv a multiple of 8): each V block
     // goes from the tensor cores straight into the digit panels of R = V.X,
     // its row exponents bounded in advance from the column norms of the
     // dressed vertex (Cauchy-Schwarz), so V never exists in FP64 and is
@@ -367,7 +367,7 @@ void Ccsd::residual(int it, const double *Tp, double *Rp) {
     // takes its B operand as [G, d, y] and R sums over k = d + Nv c, so X
     // enters as X'[d,c,i,j] = X[c,d,i,j].
     const int64_t s_last = Nv - (ns - 1) * s;
-    const bool fused = Nv % 16 == 0 && emulated(s_last * Nv, s_last * Nv, NG) &&
+    const bool fused = Nv % 8 == 0 && emulated(s_last * Nv, s_last * Nv, NG) &&
                        emulated(s_last * s_last, No * No, Nv * Nv);
     if (fused) {
       DBuf amax(ctx, sizeof(unsigned long long) * Nv);

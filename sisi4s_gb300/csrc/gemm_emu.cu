@@ -292,7 +292,7 @@ struct EmuArgs {
   // next product, rows r = x + px*y, K index k = d + pd*c (m = x + px*c,
   // n = d + pd*y), with the row exponents pexp[r] given (max|V| < 2^pexp[r]);
   // tiles [S][prt][pkt] of TM rows x KB k as split_kernel writes them.
-  // Needs beta = 0, ksplit = 1, pd a multiple of 16.
+  // Needs beta = 0, ksplit = 1, pd a multiple of 8.
   __nv_bfloat16 *pout = nullptr;
   const int *pexp = nullptr;
   int prt = 0, pkt = 0;
@@ -624,28 +624,30 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) emu_gemm_kernel(EmuArgs a) {
           }
         } else {
         if (a.pout) {
-          // digit-panel output: this thread's 16 columns are 16 consecutive d
-          // of one y, so each digit of each 8-column half is one 16-byte
-          // row segment of a panel tile
-          // n0 is the same for the whole warp; rows past M only skip their
-          // stores, so that every lane takes part in the shuffles below
+          // digit-panel output: each 8-column half of this thread's 16
+          // columns holds 8 consecutive d of one y (pd is a multiple of 8),
+          // so each digit of a half is one 16-byte row segment of a panel tile
+          // (n0 is the same for the whole warp; rows past M only skip their
+          // stores, so that every lane takes part in the shuffles below)
           if (n0 >= a.N) continue;
-          const unsigned mu = mrow ? (unsigned)m : 0u, nu = (unsigned)n0;
+          const unsigned mu = mrow ? (unsigned)m : 0u;
           const unsigned x = mu % a.px, c = mu / a.px;
-          const unsigned d0 = nu % a.pd, y = nu / a.pd;
-          const unsigned r = x + a.px * y;
-          const unsigned k0 = d0 + a.pd * c;
-          const int er = mrow ? a.pexp[r] : EXP_FLOOR - 1;
           const int F = 7 * S;
           long long bias = 0;
 #pragma unroll
           for (int q = 1; q < S; ++q) bias += 64LL << (7 * (S - 1 - q));
-          const unsigned rr = r % TM, tr = r / TM;
-          const unsigned tk = k0 / KB, kk0 = k0 % KB;  // kk0 is 0 or 16
-          const int64_t off0 = ((int64_t)tr * a.pkt + tk) * (TM * KB) +
-                               (int64_t)(((rr / 8) * (KB / 8) + kk0 / 8) * 64 + (rr % 8) * 8);
 #pragma unroll
           for (int h = 0; h < 2; ++h) {
+            const unsigned nu = (unsigned)n0 + 8u * h;
+            if (nu >= (unsigned)a.N) break;  // warp-uniform
+            const unsigned d0 = nu % a.pd, y = nu / a.pd;
+            const unsigned r = x + a.px * y;
+            const unsigned k0 = d0 + a.pd * c;
+            const int er = mrow ? a.pexp[r] : EXP_FLOOR - 1;
+            const unsigned rr = r % TM, tr = r / TM;
+            const unsigned tk = k0 / KB, kk = k0 % KB;  // kk is a multiple of 8
+            const int64_t off = ((int64_t)tr * a.pkt + tk) * (TM * KB) +
+                                (int64_t)(((rr / 8) * (KB / 8) + kk / 8) * 64 + (rr % 8) * 8);
             uint32_t packed[S][4];
 #pragma unroll
             for (int jj = 0; jj < 8; ++jj) {
@@ -676,7 +678,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) emu_gemm_kernel(EmuArgs a) {
             if (mrow) {
 #pragma unroll
               for (int q = 0; q < S; ++q)
-                *reinterpret_cast<uint4 *>(a.pout + q * a.pplane + off0 + 64 * h) =
+                *reinterpret_cast<uint4 *>(a.pout + q * a.pplane + off) =
                     make_uint4(packed[q][0], packed[q][1], packed[q][2], packed[q][3]);
             }
           }
@@ -883,6 +885,29 @@ __global__ void ladder_row_exponent_kernel(const unsigned long long *__restrict_
                    __longlong_as_double((long long)amax[y0 + y]) * (1.0 + 0x1p-20);
   const int e = frexp_exponent(b);
   er[r] = e == INT_MIN ? (int)0x80808080 : e;
+}
+
+// Rows R .. rt*TM of A-role panels (the padding of the last tile row) set to
+// the digits of zero, which the panel-output GEMM never writes: one 16-byte
+// row segment per thread.
+__global__ void zero_panel_rows_kernel(__nv_bfloat16 *__restrict__ P, int64_t R, int rt,
+                                       int kt, int S, int64_t plane) {
+  const int64_t pad = (int64_t)rt * TM - R;
+  const int64_t n = pad * kt * (KB / 8) * S;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    int64_t t = i;
+    const int64_t row = R + t % pad;
+    t /= pad;
+    const int seg = (int)(t % (KB / 8));
+    t /= (KB / 8);
+    const int64_t tk = t % kt;
+    const int64_t q = t / kt;
+    const int64_t tr = row / TM, rr = row % TM;
+    const int64_t off = q * plane + (tr * kt + tk) * (TM * KB) +
+                        ((rr / 8) * (KB / 8) + seg) * 64 + (rr % 8) * 8;
+    *reinterpret_cast<uint4 *>(P + off) = make_uint4(0u, 0u, 0u, 0u);
+  }
 }
 
 // out = alpha * 2^(ea+eb-14-frac) * sum_s W[s] + beta * C, summing the exact
@@ -1320,8 +1345,16 @@ void run_emu_to_panels(Context &ctx, int64_t M, int64_t N, int64_t K, const doub
       B, N, K, ldb, 1, eb.as<int>(), nt, kt, bsl.as<__nv_bfloat16>());
   GBCC_CHECK_LAUNCH(ctx);
   // rows past R are never written: give them the digits of zero
-  if (P.rows % TM != 0)
-    GBCC_CUDA(cudaMemsetAsync(P.panels.as<void>(), 0, P.panels.bytes(), ctx.stream));
+  if (P.rows % TM != 0) {
+    const int64_t pad = (int64_t)P.rt * TM - P.rows;
+    const int64_t n = pad * P.kt * (KB / 8) * S;
+    const unsigned g = (unsigned)std::max<int64_t>(
+        1, std::min<int64_t>((n + 255) / 256, (int64_t)std::max(ctx.sm_count, 1) * 16));
+    zero_panel_rows_kernel<<<g, 256, 0, ctx.stream>>>(P.panels.as<__nv_bfloat16>(), P.rows,
+                                                      P.rt, P.kt, S,
+                                                      (int64_t)P.rt * P.kt * TM * KB);
+    GBCC_CHECK_LAUNCH(ctx);
+  }
   constexpr int STAGE_BYTES = S * (A_TILE + B_TILE);
   constexpr int STAGES = (SMEM_BUDGET / STAGE_BYTES) > 4 ? 4 : (SMEM_BUDGET / STAGE_BYTES);
   const int smem = STAGES * STAGE_BYTES;
@@ -1370,7 +1403,7 @@ void gemm_emu_to_panels(Context &ctx, int64_t M, int64_t N, int64_t K, const dou
                         int64_t lda, const double *B, int64_t ldb, int64_t px, int64_t pd,
                         EmuPanels &P) {
   require(P.role_a && P.count == 1 && P.S == ctx.emu_slices, "gemm_emu_to_panels: panels");
-  require(px > 0 && pd > 0 && pd % 16 == 0 && M % px == 0 && N % pd == 0,
+  require(px > 0 && pd > 0 && pd % 8 == 0 && M % px == 0 && N % pd == 0,
           "gemm_emu_to_panels: shape");
   require(P.rows == px * (N / pd) && P.K == pd * (M / px), "gemm_emu_to_panels: panel shape");
   require(M < (1LL << 31) && N < (1LL << 31), "gemm_emu_to_panels: size");

@@ -328,7 +328,7 @@ EmuPanels emu_panels_alloc(Context &ctx, bool role_a, int64_t R, int64_t K);
 // (operand rows K-major: A[k + m lda], B[k + n ldb]; m = x + px c,
 // n = d + pd y) written straight into the digit panels P of the next
 // product's A operand: rows x + px y, K index d + pd c, with P's row
-// exponents set beforehand (ladder_row_exponents).  pd % 16 == 0.
+// exponents set beforehand (ladder_row_exponents).  pd % 8 == 0.
 void gemm_emu_to_panels(Context &ctx, int64_t M, int64_t N, int64_t K, const double *A,
                         int64_t lda, const double *B, int64_t ldb, int64_t px, int64_t pd,
                         EmuPanels &P);

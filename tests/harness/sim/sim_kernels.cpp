@@ -221,7 +221,7 @@ void gemm_emu_to_panels(Context &ctx, int64_t M, int64_t N, int64_t K, const dou
                         int64_t lda, const double *B, int64_t ldb, int64_t px, int64_t pd,
                         EmuPanels &P) {
   require(P.role_a && P.count == 1 && P.S == ctx.emu_slices, "gemm_emu_to_panels: panels");
-  require(px > 0 && pd > 0 && pd % 16 == 0 && M % px == 0 && N % pd == 0,
+  require(px > 0 && pd > 0 && pd % 8 == 0 && M % px == 0 && N % pd == 0,
           "gemm_emu_to_panels: shape");
   require(P.rows == px * (N / pd) && P.K == pd * (M / px), "gemm_emu_to_panels: panel shape");
   ctx.flops += 2.0 * (double)M * (double)N * (double)K;

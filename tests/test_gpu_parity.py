@@ -121,16 +121,18 @@ def test_residual_matches_oracle(ctx, No, Nv, NG, dist, ppl, slice_size):
 @pytest.mark.parametrize("No,Nv,NG,slice_size,dist", [(4, 23, 50, 5, 0), (3, 40, 64, 16, 0),
                                                       (5, 30, 70, 30, 1), (2, 9, 20, 4, 0),
                                                       (2, 40, 600, 10, 0), (3, 32, 64, 5, 0),
-                                                      (4, 48, 96, 16, 0), (2, 64, 600, 24, 1)])
+                                                      (4, 48, 96, 16, 0), (2, 64, 600, 24, 1),
+                                                      (3, 40, 64, 5, 0), (2, 24, 50, 7, 1)])
 def test_residual_emulated_matches_oracle(ctx, No, Nv, NG, slice_size, dist):
     # every GEMM emulated (threshold 0), ragged ladder slices: the ladder's
     # V_xycd is written by the emulated GEMM straight into its permuted layout
     # (with NG = 600 over two K-chunks and few tiles, through the K-split
-    # reduction).  With Nv a multiple of 16 the ladder takes its fused form:
+    # reduction).  With Nv a multiple of 8 the ladder takes its fused form:
     # V_xycd goes straight into the digit panels of R = V.X, with row
     # exponents bounded from the vertex column norms (Nv = 32 with slices of
     # 5: blocks of 25 rows, panel rows padded; Nv = 48: whole 128-row tiles;
-    # Nv = 64: two K-chunks over NG, distinguishable)
+    # Nv = 64: two K-chunks over NG, distinguishable; Nv = 40 and 24 with
+    # odd slices: product widths that end half-way through a 16-column group)
     s = make_system(No, Nv, NG, seed=No * 7 + Nv)
     ints = oracle_ints(s.gamma, No)
     T1, T2 = _rand_amplitudes(Nv, No, seed=Nv + 1)
