@@ -1,6 +1,7 @@
 """Times one (T) evaluation on a seeded synthetic system.
 
     python -m benchmarks.triples_bench No Nv NG [--prec emu|fp64] [--reps R]
+        [--batch-images B]
 
 The amplitudes are the MP2 amplitudes of the system (T1 = 0) plus a small
 seeded T1, so that every term of the (T) energy is exercised.  Prints one JSON
@@ -21,6 +22,8 @@ def main():
     ap.add_argument("--prec", default="emu", choices=["emu", "fp64"])
     ap.add_argument("--reps", type=int, default=2)
     ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--batch-images", type=int, default=0,
+                    help="bound on the triple images per (T) batch (0: automatic)")
     args = ap.parse_args()
 
     import torch  # device synchronisation only
@@ -33,6 +36,7 @@ def main():
     T1, T2 = mp2_amplitudes(s)
     T1 = T1 + 1e-3 * np.random.default_rng(args.seed + 1).normal(size=T1.shape)
     ctx = capi.Context(0)
+    ctx.set_triples_batch(args.batch_images)
     times, e_t = [], None
     for _ in range(args.reps):
         torch.cuda.synchronize()
