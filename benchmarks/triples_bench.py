@@ -22,6 +22,10 @@ def main():
     ap.add_argument("--prec", default="emu", choices=["emu", "fp64"])
     ap.add_argument("--reps", type=int, default=2)
     ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--profile", action="store_true",
+                    help="CUDA events around every tensor-core launch of the last "
+                         "repetition: time of the W products by kind, the rest is "
+                         "the epilogue and set-up")
     ap.add_argument("--batch-images", type=int, default=0,
                     help="bound on the triple images per (T) batch (0: automatic)")
     args = ap.parse_args()
@@ -38,15 +42,33 @@ def main():
     ctx = capi.Context(0)
     ctx.set_triples_batch(args.batch_images)
     times, e_t = [], None
-    for _ in range(args.reps):
+    for rep in range(args.reps):
+        if args.profile and rep == args.reps - 1:
+            ctx.profile(True)
+            ctx.gemm_records()  # drop older records
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         e_t, _ = gpu.triples(ctx, s.eps_h, s.eps_p, s.gamma, T1, T2,
                              precision=args.prec)
         times.append(time.perf_counter() - t0)
-    print(json.dumps({"No": args.No, "Nv": args.Nv, "NG": args.NG,
-                      "precision": args.prec, "seconds": times, "e_t": e_t,
-                      "hole_triples": args.No * (args.No + 1) * (args.No + 2) // 6}))
+    out = {"No": args.No, "Nv": args.Nv, "NG": args.NG,
+           "precision": args.prec, "seconds": times, "e_t": e_t,
+           "hole_triples": args.No * (args.No + 1) * (args.No + 2) // 6}
+    if args.profile:
+        ctx.profile(False)
+        recs = ctx.gemm_records()
+        Nv = args.Nv
+        hole = lambda r: r[0] == Nv * Nv and r[1] == Nv
+        part = lambda r: r[0] == Nv and r[1] == Nv * Nv
+        kinds = {"hole (M = Nv^2, N = Nv, K = No)": hole,
+                 "particle (M = Nv, N = Nv^2, K = Nv)": part,
+                 "other (Wvv and integral builds)": lambda r: not hole(r) and not part(r)}
+        for name, sel in kinds.items():
+            rr = [r for r in recs if sel(r)]
+            out["gemm_" + name] = {"launches": len(rr), "ms": sum(r[3] for r in rr)}
+        out["gemm_ms_total"] = sum(r[3] for r in recs)
+        out["rest_ms"] = 1e3 * times[-1] - out["gemm_ms_total"]
+    print(json.dumps(out))
     ctx.close()
 
 
