@@ -221,6 +221,23 @@ typedef struct {
 gbcc_status gbcc_ccsd_solve(gbcc_ctx *ctx, const gbcc_ccsd_in *in,
                             const gbcc_ccsd_opts *opts, gbcc_ccsd_out *out);
 
+/* Lockstep solve of nsys closed-shell systems of one shape: the same No, Nv
+ * and NG, each with its own vertex, eigenenergies and optional starting
+ * amplitudes (all or none of them starting from given doubles), one set of
+ * options (DiisMixer, CcsdEnergyFromCoulombIntegrals, maxIterations >= 1).
+ * Every contraction of the residual runs once for all systems, as one
+ * batched product; each system keeps its own update, DIIS history and
+ * convergence test, and stops where it would stop alone (its energies agree
+ * with gbcc_ccsd_solve's up to the rounding of the batched products).
+ * status[z] receives what gbcc_ccsd_solve would return for system z, and
+ * outs[z] (if outs is not NULL) its results.  Returns GBCC_OK when the batch
+ * ran, whatever the systems' statuses, else the error that stopped it.  No
+ * counterpart in the reference, which solves one system per algorithm run
+ * (ClusterSinglesDoublesAlgorithm.cxx:38-128). */
+gbcc_status gbcc_ccsd_solve_batch(gbcc_ctx *ctx, int nsys, const gbcc_ccsd_in *ins,
+                                  const gbcc_ccsd_opts *opts, gbcc_ccsd_out *outs,
+                                  gbcc_status *status);
+
 /* Device-resident solver: setup uploads inputs and builds integrals once;
  * step runs n more iterations (stopping early on convergence);
  * amplitudes can then be read back or handed to the (T) step. */

@@ -99,6 +99,9 @@ _SIGS = {
     "gbcc_ccsd_opts_default": (None, [C.POINTER(CcsdOpts)]),
     "gbcc_ccsd_solve": (C.c_int, [C.c_void_p, C.POINTER(CcsdIn),
                                   C.POINTER(CcsdOpts), C.POINTER(CcsdOut)]),
+    "gbcc_ccsd_solve_batch": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(CcsdIn),
+                                        C.POINTER(CcsdOpts), C.POINTER(CcsdOut),
+                                        C.POINTER(C.c_int)]),
     "gbcc_ccsd_setup": (C.c_int, [C.c_void_p, C.POINTER(CcsdIn),
                                   C.POINTER(CcsdOpts), C.POINTER(C.c_void_p)]),
     "gbcc_ccsd_step": (C.c_int, [C.c_void_p, C.c_int, _dp,

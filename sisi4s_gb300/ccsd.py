@@ -159,6 +159,43 @@ def ccsd_solve(ctx, eps_h, eps_p, gamma, ints=None, initial=None,
     return r
 
 
+def ccsd_solve_batch(ctx, systems, want_amplitudes=False, **opts):
+    """Solves several systems of one shape in lockstep
+    (``gbcc_ccsd_solve_batch``): each contraction runs once for all of them.
+    ``systems`` is a list of ``(eps_h, eps_p, gamma)`` or
+    ``(eps_h, eps_p, gamma, initial)`` tuples.  Returns one result dict per
+    system, as ``ccsd_solve`` gives it; a system that fails carries its error
+    status in ``status`` instead of raising."""
+    inps = [CcsdInput(*((sy[0], sy[1], sy[2]) + ((None, sy[3]) if len(sy) > 3 else ())))
+            for sy in systems]
+    n = len(inps)
+    o = make_opts(**opts)
+    outs = (capi.CcsdOut * n)()
+    ins = (capi.CcsdIn * n)(*[i.s for i in inps])
+    st = (C.c_int * n)()
+    keep = []
+    for z, inp in enumerate(inps):
+        No, Nv = inp.No, inp.Nv
+        hist = np.zeros(max(o.max_iterations, 1))
+        t1 = np.zeros(Nv * No) if want_amplitudes else None
+        t2 = np.zeros(Nv * Nv * No * No) if want_amplitudes else None
+        outs[z].T1, outs[z].T2, outs[z].energy_history = ptr(t1), ptr(t2), ptr(hist)
+        keep.append((hist, t1, t2))
+    ctx.check(ctx.lib.gbcc_ccsd_solve_batch(ctx.h, n, ins, C.byref(o), outs, st))
+    res = []
+    for z, inp in enumerate(inps):
+        out = outs[z]
+        hist, t1, t2 = keep[z]
+        r = {"energy": out.energy, "direct": out.direct, "exchange": out.exchange,
+             "iterations": out.iterations, "converged": bool(out.converged),
+             "status": st[z], "history": hist[:out.iterations].copy()}
+        if want_amplitudes:
+            r["T1"] = from_fortran_flat(t1, (inp.Nv, inp.No))
+            r["T2"] = from_fortran_flat(t2, (inp.Nv, inp.Nv, inp.No, inp.No))
+        res.append(r)
+    return res
+
+
 def ccsd_residual(ctx, it, T1, T2, eps_h, eps_p, gamma, ints=None,
                   initial=None, **opts):
     inp = CcsdInput(eps_h, eps_p, gamma, ints, initial)

@@ -5,6 +5,7 @@
 #include <string>
 
 #include "ccsd.hpp"
+#include "ccsd_batch.hpp"
 
 namespace gbcc {
 double triples_energy(Context &ctx, const CcsdInputs &I, const double *T1,
@@ -315,37 +316,82 @@ gbcc_status gbcc_ccsd_step(gbcc_solver *s, int n, double *energy,
   return guard(s->ctx, [&]() { return s->s->run(n, energy, converged); });
 }
 
+namespace {
+// gbcc_ccsd_out of one solver (the caller synchronises the stream)
+void fill_result(gbcc::Ccsd &c, gbcc::Context &ctx, gbcc_ccsd_out *out) {
+  const auto &L = c.layout();
+  out->energy = c.energy();
+  out->direct = c.direct();
+  out->exchange = c.exchange();
+  out->iterations = c.iterations_done();
+  out->converged = c.converged() ? 1 : 0;
+  if (out->T1)
+    GBCC_CUDA(cudaMemcpyAsync(out->T1, c.amplitudes(), 8 * L.n1,
+                              cudaMemcpyDeviceToHost, ctx.stream));
+  if (out->T2)
+    GBCC_CUDA(cudaMemcpyAsync(out->T2, c.amplitudes() + L.off2, 8 * L.n2,
+                              cudaMemcpyDeviceToHost, ctx.stream));
+  if (out->pair_energy) {
+    gbcc::DBuf pe(ctx, 8 * L.No * L.No);
+    c.pair_energies(pe.as<double>());
+    GBCC_CUDA(cudaMemcpyAsync(out->pair_energy, pe.as<double>(), 8 * L.No * L.No,
+                              cudaMemcpyDeviceToHost, ctx.stream));
+    GBCC_CUDA(cudaStreamSynchronize(ctx.stream));
+  }
+  if (out->energy_history) {
+    const auto &h = c.history();
+    if (!h.empty())
+      std::memcpy(out->energy_history, h.data(), sizeof(double) * h.size());
+  }
+}
+}  // namespace
+
+gbcc_status gbcc_ccsd_solve_batch(gbcc_ctx *ctx, int nsys, const gbcc_ccsd_in *ins,
+                                  const gbcc_ccsd_opts *opts, gbcc_ccsd_out *outs,
+                                  gbcc_status *status) {
+  if (!ctx || !ins || nsys < 1 || !status) return GBCC_BAD_ARG;
+  return guard(ctx, [&]() {
+    gbcc_ccsd_opts o;
+    if (opts) o = *opts; else gbcc_ccsd_opts_default(&o);
+    check_opts(o);
+    gbcc::require(o.max_iterations >= 1, "a batch of systems needs maxIterations >= 1");
+    apply_precision_opts(ctx->c, o);
+    std::vector<std::unique_ptr<gbcc::Ccsd>> sys;
+    for (int z = 0; z < nsys; ++z) {
+      auto inputs = gbcc::upload_inputs(ctx->c, ins[z], o.precision, true, false);
+      sys.push_back(std::make_unique<gbcc::Ccsd>(ctx->c, std::move(inputs), o, ins[z].init_T1,
+                                                 ins[z].init_T2));
+    }
+    std::vector<gbcc_status> st((size_t)nsys, GBCC_OK);
+    std::vector<gbcc::Ccsd *> done;
+    std::unique_ptr<gbcc::BatchCcsd> batch;
+    if (nsys == 1) {
+      st[0] = sys[0]->run(o.max_iterations, nullptr, nullptr);
+      done.push_back(sys[0].get());
+    } else {
+      batch = std::make_unique<gbcc::BatchCcsd>(ctx->c, std::move(sys));
+      batch->run(o.max_iterations);
+      for (int z = 0; z < nsys; ++z) {
+        st[z] = batch->status(z);
+        done.push_back(&batch->system(z));
+      }
+    }
+    for (int z = 0; z < nsys; ++z) {
+      gbcc::Ccsd &c = *done[z];
+      status[z] = st[z] != GBCC_OK ? st[z] : (c.converged() ? GBCC_OK : GBCC_NOT_CONVERGED);
+      if (outs) fill_result(c, ctx->c, &outs[z]);
+    }
+    GBCC_CUDA(cudaStreamSynchronize(ctx->c.stream));
+    ctx->c.check_device_errors();
+    return GBCC_OK;
+  });
+}
+
 gbcc_status gbcc_ccsd_result(gbcc_solver *s, gbcc_ccsd_out *out) {
   if (!s || !out) return GBCC_BAD_ARG;
   return guard(s->ctx, [&]() {
-    gbcc::Ccsd &c = *s->s;
-    gbcc::Context &ctx = s->ctx->c;
-    const auto &L = c.layout();
-    out->energy = c.energy();
-    out->direct = c.direct();
-    out->exchange = c.exchange();
-    out->iterations = c.iterations_done();
-    out->converged = c.converged() ? 1 : 0;
-    if (out->T1)
-      GBCC_CUDA(cudaMemcpyAsync(out->T1, c.amplitudes(), 8 * L.n1,
-                                cudaMemcpyDeviceToHost, ctx.stream));
-    if (out->T2)
-      GBCC_CUDA(cudaMemcpyAsync(out->T2, c.amplitudes() + L.off2, 8 * L.n2,
-                                cudaMemcpyDeviceToHost, ctx.stream));
-    if (out->pair_energy) {
-      gbcc::DBuf pe(ctx, 8 * L.No * L.No);
-      c.pair_energies(pe.as<double>());
-      GBCC_CUDA(cudaMemcpyAsync(out->pair_energy, pe.as<double>(),
-                                8 * L.No * L.No, cudaMemcpyDeviceToHost,
-                                ctx.stream));
-      GBCC_CUDA(cudaStreamSynchronize(ctx.stream));
-    }
-    if (out->energy_history) {
-      const auto &h = c.history();
-      if (!h.empty())  // no iteration ran with maxIterations 0
-        std::memcpy(out->energy_history, h.data(), sizeof(double) * h.size());
-    }
-    GBCC_CUDA(cudaStreamSynchronize(ctx.stream));
+    fill_result(*s->s, s->ctx->c, out);
+    GBCC_CUDA(cudaStreamSynchronize(s->ctx->c.stream));
     return GBCC_OK;
   });
 }

@@ -222,54 +222,81 @@ void Ccsd::residual(int it, const double *Tp, double *Rp) {
     residual_stored(it, Tp, Rp);
     return;
   }
-  Context &ctx = ctx_;
-  CcsdInputs &I = *in_;
-  const int prec = o_.precision;
-  const int64_t No = L_.No, Nv = L_.Nv, NG = I.NG;
-  const bool dist = o_.distinguishable != 0;
+  fill(ctx_, Rp, L_.ntot, 0.0);                                    // :37-38
+  ResidualArgs a;
+  a.I = in_.get();
+  a.o = &o_;
+  a.nz = 1;
+  a.slice = slice_;
+  a.init_doubles = init_doubles_;
+  a.T1 = T1v(L_, const_cast<double *>(Tp));
+  a.T2 = T2v(L_, const_cast<double *>(Tp));
+  a.R1 = T1v(L_, Rp);
+  a.R2 = T2v(L_, Rp);
+  residual_program(ctx_, a, it);
+}
+
+// The statements of getResiduum over nz systems of one shape at once.  With
+// nz > 1 every tensor (amplitudes, residuals, inputs and intermediates)
+// carries a trailing system index Z, its slowest, so each system's data is
+// one contiguous block and every contraction below is one batched product
+// (a grouped tensor-core launch in precision mode).  R arrives zeroed.
+void residual_program(Context &ctx, const ResidualArgs &ra, int it) {
+  const CcsdInputs &I = *ra.I;
+  const gbcc_ccsd_opts &o = *ra.o;
+  const int prec = o.precision;
+  const int64_t nz = ra.nz;
+  const int64_t No = I.No, Nv = I.Nv, NG = I.NG;
+  const int64_t n2 = Nv * Nv * No * No;
+  const bool dist = o.distinguishable != 0;
+  // index strings and shapes gain the system index when nz > 1
+  auto ix = [&](const char *s) { return nz > 1 ? std::string(s) + "Z" : std::string(s); };
   auto C = [&](double al, const Ten &A, const char *ia, const Ten &B,
                const char *ib, double be, const Ten &Cc, const char *ic) {
-    contract(ctx, al, A, ia, B, ib, be, Cc, ic, prec);
+    contract(ctx, al, A, ix(ia).c_str(), B, ix(ib).c_str(), be, Cc, ix(ic).c_str(), prec);
   };
-  Ten T1 = T1v(L_, const_cast<double *>(Tp)), T2 = T2v(L_, const_cast<double *>(Tp));
-  Ten R1 = T1v(L_, Rp), R2 = T2v(L_, Rp);
-  fill(ctx, Rp, L_.ntot, 0.0);                                     // :37-38
+  auto shp = [&](std::initializer_list<int64_t> l) {
+    std::vector<int64_t> v(l);
+    if (nz > 1) v.push_back(nz);
+    return v;
+  };
+  const Ten &T1 = ra.T1, &T2 = ra.T2, &R1 = ra.R1, &R2 = ra.R2;
   const Ten &V = I.Vabij, &Vx = I.Vx;
-  if (it == 0 && !init_doubles_) {                                 // :47-51
-    copy(ctx, R2.p, V.p, L_.n2);
+  if (it == 0 && !ra.init_doubles) {                               // :47-51
+    copy(ctx, R2.p, V.p, n2 * nz);
     return;
   }
   const Ten &Vaibj = I.Vaibj, &Vijkl = I.Vijkl, &Vijka = I.Vijka;
   const Ten &Gai = I.Gai, &Gab = I.Gab, &Gij = I.Gij;
 
-  OTen X(ctx, {Nv, Nv, No, No});                                   // :136-138
-  outer_add(ctx, X.p(), T2.p, T1.p, 1.0, Nv, No);
-  OTen Kac(ctx, {Nv, Nv}), Kki(ctx, {No, No});
+  OTen X(ctx, shp({Nv, Nv, No, No}));                                   // :136-138
+  outer_add(ctx, X.p(), T2.p, T1.p, 1.0, Nv, No, nz);
+  OTen Kac(ctx, shp({Nv, Nv})), Kki(ctx, shp({No, No}));
   {
-    OTen Lac(ctx, {Nv, Nv}), Lki(ctx, {No, No});
+    OTen Lac(ctx, shp({Nv, Nv})), Lki(ctx, shp({No, No}));
     C(-2.0, V, "cdkl", X, "adkl", 0.0, Kac, "ac");                 // :146
     C(1.0, Vx, "cdkl", X, "adkl", 1.0, Kac, "ac");                 // :147 V["dckl"]
-    if (!dist) copy(ctx, Lac.p(), Kac.p(), Nv * Nv);               // :151
+    if (!dist) copy(ctx, Lac.p(), Kac.p(), Nv * Nv * nz);               // :151
     else {
-      OTen Y(ctx, {Nv, Nv, No, No});                               // :154-156
-      outer_add(ctx, Y.p(), T2.p, T1.p, 2.0, Nv, No);
+      OTen Y(ctx, shp({Nv, Nv, No, No}));                               // :154-156
+      outer_add(ctx, Y.p(), T2.p, T1.p, 2.0, Nv, No, nz);
       C(-1.0, V, "cdkl", Y, "adkl", 0.0, Lac, "ac");               // :157-158
       C(0.5, Vx, "cdkl", Y, "adkl", 1.0, Lac, "ac");               // :159-160
     }
     {
-      OTen t(ctx, {NG});                                           // :162-163
+      OTen t(ctx, shp({NG}));                                           // :162-163
       C(1.0, Gai, "Gdk", T1, "dk", 0.0, t, "G");
       C(2.0, Gab, "Gca", t, "G", 1.0, Lac, "ac");
-      OTen Q(ctx, {NG, Nv, No});                                   // :166-167
+      OTen Q(ctx, shp({NG, Nv, No}));                                   // :166-167
       C(1.0, Gab, "Gda", T1, "dk", 0.0, Q, "Gak");
       C(-1.0, Gai, "Gck", Q, "Gak", 1.0, Lac, "ac");
     }
     C(2.0, V, "cdkl", X, "cdil", 0.0, Kki, "ki");                  // :172
     C(-1.0, Vx, "cdkl", X, "cdil", 1.0, Kki, "ki");                // :173 V["dckl"]
-    if (!dist) copy(ctx, Lki.p(), Kki.p(), No * No);               // :177
+    if (!dist) copy(ctx, Lki.p(), Kki.p(), No * No * nz);               // :177
     else {
-      OTen Y(ctx, {Nv, Nv, No, No});                               // :180-182
-      outer_add(ctx, Y.p(), T2.p, T1.p, 2.0, Nv, No);
+      OTen Y(ctx, shp({Nv, Nv, No, No}));                               // :180-182
+      outer_add(ctx, Y.p(), T2.p, T1.p, 2.0, Nv, No, nz);
       C(1.0, V, "cdkl", Y, "cdil", 0.0, Lki, "ki");                // :183-184
       C(-0.5, Vx, "cdkl", Y, "cdil", 1.0, Lki, "ki");              // :185-186
     }
@@ -279,39 +306,39 @@ void Ccsd::residual(int it, const double *Tp, double *Rp) {
     C(-1.0, Lki, "ki", T2, "abkj", 1.0, R2, "abij");               // :195
   }
   {
-    OTen dGai(ctx, {NG, Nv, No});                                  // :200-206
+    OTen dGai(ctx, shp({NG, Nv, No}));                                  // :200-206
     copy(ctx, dGai.p(), Gai.p, Gai.size());
     C(-1.0, Gij, "Gki", T1, "ak", 1.0, dGai, "Gai");
-    OTen Z(ctx, {NG, Nv, No});                                     // :208-209
+    OTen Z(ctx, shp({NG, Nv, No}));                                     // :208-209
     C(1.0, Gab, "Gbc", T1, "cj", 0.0, Z, "Gbj");
     C(1.0, dGai, "Gai", Z, "Gbj", 1.0, R2, "abij");
     C(-1.0, Vijka, "jika", T1, "bk", 1.0, R2, "abij");             // :213
-    OTen W(ctx, {Nv, No, No, No});                                 // :214-215
+    OTen W(ctx, shp({Nv, No, No, No}));                                 // :214-215
     C(1.0, V, "acik", T1, "cj", 0.0, W, "aikj");
     C(-1.0, T1, "bk", W, "aikj", 1.0, R2, "abij");
   }
   {
-    OTen Xakic(ctx, {Nv, No, No, Nv});                             // :218-252
+    OTen Xakic(ctx, shp({Nv, No, No, Nv}));                             // :218-252
     {
-      OTen dGai(ctx, {NG, Nv, No});                                // :222-231
+      OTen dGai(ctx, shp({NG, Nv, No}));                                // :222-231
       copy(ctx, dGai.p(), Gai.p, Gai.size());
       C(-1.0, Gij, "Gil", T1, "al", 1.0, dGai, "Gai");
       C(1.0, Gab, "Gad", T1, "di", 1.0, dGai, "Gai");
       C(1.0, dGai, "Gai", Gai, "Gck", 0.0, Xakic, "akic");         // :234-235
     }
-    OTen Y(ctx, {Nv, Nv, No, No});                                 // :238-240
-    outer_add(ctx, Y.p(), T2.p, T1.p, 2.0, Nv, No);
+    OTen Y(ctx, shp({Nv, Nv, No, No}));                                 // :238-240
+    outer_add(ctx, Y.p(), T2.p, T1.p, 2.0, Nv, No, nz);
     C(-0.5, V, "dclk", Y, "dail", 1.0, Xakic, "akic");             // :242
     C(1.0, V, "dclk", T2, "adil", 1.0, Xakic, "akic");             // :243
     if (!dist) C(-0.5, V, "cdlk", T2, "adil", 1.0, Xakic, "akic"); // :245
-    axpby(ctx, L_.n2, 2.0, T2.p, 0.0, Y.p());                      // :248
-    assign(ctx, -1.0, T2, "bckj", 1.0, Y, "cbkj");                 // :249
+    axpby(ctx, n2 * nz, 2.0, T2.p, 0.0, Y.p());                      // :248
+    assign(ctx, -1.0, T2, ix("bckj").c_str(), 1.0, Y, ix("cbkj").c_str());                 // :249
     C(1.0, Xakic, "akic", Y, "cbkj", 1.0, R2, "abij");             // :251
   }
   {
-    OTen Xakci(ctx, {Nv, No, Nv, No});                             // :254-293
+    OTen Xakci(ctx, shp({Nv, No, Nv, No}));                             // :254-293
     {
-      OTen dGab(ctx, {NG, Nv, Nv}), dGij(ctx, {NG, No, No});
+      OTen dGab(ctx, shp({NG, Nv, Nv})), dGij(ctx, shp({NG, No, No}));
       copy(ctx, dGab.p(), Gab.p, Gab.size());
       copy(ctx, dGij.p(), Gij.p, Gij.size());
       C(-1.0, Gai, "Gcl", T1, "al", 1.0, dGab, "Gac");             // :270
@@ -321,37 +348,37 @@ void Ccsd::residual(int it, const double *Tp, double *Rp) {
     if (!dist) C(-0.5, V, "cdlk", T2, "dail", 1.0, Xakci, "akci"); // :284
     C(-1.0, Xakci, "akci", T2, "cbkj", 1.0, R2, "abij");           // :288
     C(-1.0, Xakci, "bkci", T2, "ackj", 1.0, R2, "abij");           // :289
-    OTen Rc(ctx, {Nv, Nv, No, No});                                // :292
-    copy(ctx, Rc.p(), R2.p, L_.n2);
-    assign(ctx, 1.0, Rc, "baji", 1.0, R2, "abij");
+    OTen Rc(ctx, shp({Nv, Nv, No, No}));                                // :292
+    copy(ctx, Rc.p(), R2.p, n2 * nz);
+    assign(ctx, 1.0, Rc, ix("baji").c_str(), 1.0, R2, ix("abij").c_str());
   }
-  axpby(ctx, L_.n2, 1.0, V.p, 1.0, R2.p);                          // :301
+  axpby(ctx, n2 * nz, 1.0, V.p, 1.0, R2.p);                          // :301
   {
-    OTen Xklij(ctx, {No, No, No, No});                             // :305-333
-    copy(ctx, Xklij.p(), Vijkl.p, No * No * No * No);              // :308
+    OTen Xklij(ctx, shp({No, No, No, No}));                             // :305-333
+    copy(ctx, Xklij.p(), Vijkl.p, No * No * No * No * nz);              // :308
     C(1.0, Vijka, "klic", T1, "cj", 1.0, Xklij, "klij");           // :309
     C(1.0, Vijka, "lkjc", T1, "ci", 1.0, Xklij, "klij");           // :310
     C(1.0, Xklij, "klij", X, "abkl", 1.0, R2, "abij");             // :313
     if (!dist) C(1.0, V, "cdkl", X, "cdij", 0.0, Xklij, "klij");   // :317
     else {
-      OTen Wq(ctx, {Nv, No, No, No});                              // :319
+      OTen Wq(ctx, shp({Nv, No, No, No}));                              // :319
       C(1.0, V, "cdkl", T1, "dj", 0.0, Wq, "cklj");
       C(1.0, T1, "ci", Wq, "cklj", 0.0, Xklij, "klij");
     }
-    if (o_.ppl) C(1.0, Xklij, "klij", T2, "abkl", 1.0, R2, "abij");  // :330
+    if (o.ppl) C(1.0, Xklij, "klij", T2, "abkl", 1.0, R2, "abij");  // :330
     else C(1.0, Xklij, "klij", X, "abkl", 1.0, R2, "abij");          // :332
   }
-  if (o_.ppl) {                                                    // :374-452
-    OTen dG(ctx, {NG, Nv, Nv});                                    // :392-400
+  if (o.ppl) {                                                    // :374-452
+    OTen dG(ctx, shp({NG, Nv, Nv}));                               // :392-400
     copy(ctx, dG.p(), Gab.p, Gab.size());
     C(-1.0, Gai, "Gbk", T1, "ak", 1.0, dG, "Gab");
-    const int64_t s = slice_;
+    const int64_t s = ra.slice;
     const int64_t ns = (Nv + s - 1) / s;                           // :387
     std::vector<OTen> sl;                                          // :402-416
     for (int64_t v = 0; v < ns; ++v) {
       const int64_t x0 = v * s, nx = std::min(s, Nv - x0);
-      sl.emplace_back(ctx, std::initializer_list<int64_t>{NG, nx, Nv});
-      gather_slice(ctx, sl.back().p(), dG.p(), NG, Nv, x0, nx);
+      sl.emplace_back(ctx, shp({NG, nx, Nv}));
+      gather_slice(ctx, sl.back().p(), dG.p(), NG, Nv, x0, nx, nz);
     }
     // precision mode: X[c,d,i,j] (rows ij, K = cd) is the B operand of every
     // slice pair's R = V.X, so its digit panels are split once
@@ -367,7 +394,7 @@ void Ccsd::residual(int it, const double *Tp, double *Rp) {
     // takes its B operand as [G, d, y] and R sums over k = d + Nv c, so X
     // enters as X'[d,c,i,j] = X[c,d,i,j].
     const int64_t s_last = Nv - (ns - 1) * s;
-    const bool fused = Nv % 8 == 0 && emulated(s_last * Nv, s_last * Nv, NG) &&
+    const bool fused = nz == 1 && Nv % 8 == 0 && emulated(s_last * Nv, s_last * Nv, NG) &&
                        emulated(s_last * s_last, No * No, Nv * Nv);
     if (fused) {
       DBuf amax(ctx, sizeof(unsigned long long) * Nv);
@@ -400,13 +427,13 @@ void Ccsd::residual(int it, const double *Tp, double *Rp) {
       }
     }
     EmuPanels Xp;
-    if (!fused && emulated(s * s, No * No, Nv * Nv))
+    if (!fused && nz == 1 && emulated(s * s, No * No, Nv * Nv))
       Xp = emu_split(ctx, false, X.p(), No * No, Nv * Nv, Nv * Nv, 1, 1, 0);
     for (int64_t m = 0; m < ns && !fused; ++m) {                   // :418
       for (int64_t n = m; n < ns; ++n) {                           // :419
         const int64_t nx = sl[n].t.lens[1], ny = sl[m].t.lens[1];
-        OTen Vs(ctx, {nx, ny, Nv, Nv});                            // :425-434
-        if (emulated(nx * Nv, ny * Nv, NG)) {
+        OTen Vs(ctx, shp({nx, ny, Nv, Nv}));                       // :425-434
+        if (nz == 1 && emulated(nx * Nv, ny * Nv, NG)) {
           // V[(x,c),(y,d)] = sum_G sl_n[G,(x,c)] sl_m[G,(y,d)], written
           // straight into the V[x,y,c,d] layout of the next product
           const OutMap vmap{nx, 1, nx * ny, ny, nx, nx * ny * Nv};
@@ -415,7 +442,7 @@ void Ccsd::residual(int it, const double *Tp, double *Rp) {
         } else {
           C(1.0, sl[n], "Gxc", sl[m], "Gyd", 0.0, Vs, "xycd");
         }
-        OTen Rxy(ctx, {nx, ny, No, No});                           // :443
+        OTen Rxy(ctx, shp({nx, ny, No, No}));                      // :443
         if (Xp.count > 0 && emulated(nx * ny, No * No, Nv * Nv)) {
           const EmuPanels Vp = emu_split(ctx, true, Vs.p(), nx * ny, Nv * Nv, 1, nx * ny, 1, 0);
           emu_gemm_panels(ctx, Vp, 0, Xp, 0, 1.0, 0.0, Rxy.p(), nx * ny);
@@ -423,24 +450,24 @@ void Ccsd::residual(int it, const double *Tp, double *Rp) {
           C(1.0, Vs, "xycd", X, "cdij", 0.0, Rxy, "xyij");
         }
         const int64_t a0 = n * s, b0 = m * s;                      // :444-447
-        slice_add(ctx, R2.p, Rxy.p(), Nv, No, a0, b0, nx, ny, a0 > b0);
+        slice_add(ctx, R2.p, Rxy.p(), Nv, No, a0, b0, nx, ny, a0 > b0, nz);
       }
     }
   }
   {
     C(1.0, Kac, "ac", T1, "ci", 1.0, R1, "ai");                    // :466
     C(-1.0, Kki, "ki", T1, "ak", 1.0, R1, "ai");                   // :467
-    OTen Kck(ctx, {Nv, No});
+    OTen Kck(ctx, shp({Nv, No}));
     C(2.0, V, "cdkl", T1, "dl", 0.0, Kck, "ck");                   // :470
     C(-1.0, Vx, "cdkl", T1, "dl", 1.0, Kck, "ck");                 // :471 V["dckl"]
     C(2.0, Kck, "ck", T2, "caki", 1.0, R1, "ai");                  // :474
     C(-1.0, Kck, "ck", T2, "caik", 1.0, R1, "ai");                 // :475
-    OTen u(ctx, {No, No});                                         // :476
+    OTen u(ctx, shp({No, No}));                                         // :476
     C(1.0, Kck, "ck", T1, "ci", 0.0, u, "ki");
     C(1.0, T1, "ak", u, "ki", 1.0, R1, "ai");
     C(2.0, V, "acik", T1, "ck", 1.0, R1, "ai");                    // :477
     C(-1.0, Vaibj, "ciak", T1, "ck", 1.0, R1, "ai");               // :478
-    OTen H(ctx, {NG, Nv, No});                                     // :480-483
+    OTen H(ctx, shp({NG, Nv, No}));                                     // :480-483
     C(1.0, Gai, "Gdk", X, "cdik", 0.0, H, "Gci");
     C(2.0, Gab, "Gca", H, "Gci", 1.0, R1, "ai");
     C(1.0, Gai, "Gck", X, "cdik", 0.0, H, "Gdi");                  // :484-487
@@ -455,10 +482,16 @@ void Ccsd::residual(int it, const double *Tp, double *Rp) {
 // captured into a CUDA graph and replayed for every later iteration that
 // starts from the same state.
 void Ccsd::iteration_body() {
+  residual(it_, T_.as<double>(), R_.as<double>());                 // :95
+  mix_body();
+}
+
+// the device work of an iteration after the residual: update, mixer, energy
+// sums and their copy to the host
+void Ccsd::mix_body() {
   Context &ctx = ctx_;
   double *sc = scal_.as<double>();
   const int64_t n = L_.ntot;
-  residual(it_, T_.as<double>(), R_.as<double>());                 // :95
   double *amp = nullptr;
   if (o_.mixer == 1) {                                             // DiisMixer
     const int N = o_.max_residua;
@@ -548,11 +581,11 @@ void Ccsd::evaluate_energy() {
   exc_ = info.exchange;
 }
 
-IterInfo Ccsd::iterate() {
+// graph key of the state the next iteration starts from (-1: run eagerly);
+// allocates the DIIS slot that iteration writes
+int Ccsd::graph_key() {
   Context &ctx = ctx_;
   const int64_t n = L_.ntot;
-  IterInfo info;
-  // graph key of the state this iteration starts from (-1: run eagerly)
   int key = -1;
   if (o_.mixer == 1) {
     const int k = next_;
@@ -564,6 +597,12 @@ IterInfo Ccsd::iterate() {
   } else if (have_last_ && it_ >= 1) {
     key = (int)(swaps_ & 1);
   }
+  return key;
+}
+
+IterInfo Ccsd::iterate() {
+  Context &ctx = ctx_;
+  const int key = graph_key();
   if (key >= 0 && ctx.use_graphs && !ctx.prof) {
     if ((int)graphs_.size() <= key) graphs_.resize(key + 1);
     Graph &g = graphs_[key];
@@ -595,7 +634,14 @@ IterInfo Ccsd::iterate() {
   } else {
     iteration_body();
   }
-  // host state after the iteration
+  return finish_iteration();
+}
+
+// host state after the iteration's device work; waits for it and reads the
+// sums back
+IterInfo Ccsd::finish_iteration() {
+  Context &ctx = ctx_;
+  IterInfo info;
   if (o_.mixer == 1) {
     if (count_ < o_.max_residua) ++count_;                         // DiisMixer.cxx:141
     next_ = (next_ + 1) % o_.max_residua;                          // :179
@@ -634,49 +680,55 @@ gbcc_status Ccsd::run(int n, double *energy, int *converged) {
   gbcc_status st = GBCC_OK;
   for (int c = 0; c < n && !converged_; ++c) {
     if (it_ >= o_.max_iterations) break;
-    IterInfo info = iterate();
-    e_ = info.energy;
-    dir_ = info.direct;
-    exc_ = info.exchange;
-    hist_.push_back(e_);
-    ++it_;
-    if (o_.mixer == 1 && ctx_.take_fault(GBCC_FAULT_DIIS_SINGULAR)) info.diis_status = 1;
-    if (ctx_.take_fault(GBCC_FAULT_NAN)) info.dtdt = std::numeric_limits<double>::quiet_NaN();
-    if (info.diis_status == 1) {
-      // an exact zero pivot: dsysv's info != 0 (DiisMixer.cxx:37-41)
-      ctx_.last_error = "DIIS subspace matrix singular at iteration " +
-                        std::to_string(it_ - 1) + " (|dT|^2 = " +
-                        std::to_string(info.dtdt) + ")";
-      st = GBCC_DIIS_SINGULAR;
-      break;
-    }
-    if (info.diis_status == 2) {
-      // overlaps or weights overflowed: the reference's dsysv returns
-      // info == 0 there and its amplitudes become NaN
-      ctx_.last_error = "DIIS subspace matrix or weights not finite at iteration " +
-                        std::to_string(it_ - 1) + " (|dT|^2 = " +
-                        std::to_string(info.dtdt) + ", E = " + std::to_string(e_) + ")";
-      st = GBCC_DIVERGED;
-      break;
-    }
-    if (!std::isfinite(e_) || !std::isfinite(info.dtdt) || !std::isfinite(info.tt)) {
-      ctx_.last_error = "energy or amplitude norms not finite at iteration " +
-                        std::to_string(it_ - 1);
-      st = GBCC_DIVERGED;
-      break;
-    }
-    // ClusterSinglesDoublesAlgorithm.cxx:103-106
-    if (std::abs((e_ - prev_) / e_) < std::abs(o_.energy_convergence) &&
-        std::abs(info.dtdt / info.tt) <
-            std::abs(o_.amplitudes_convergence * o_.amplitudes_convergence)) {
-      converged_ = true;
-      break;
-    }
-    prev_ = e_;
+    if (absorb(iterate(), st)) break;
   }
   if (energy) *energy = e_;
   if (converged) *converged = converged_ ? 1 : 0;
   return st;
+}
+
+// takes in one iteration's results (ClusterSinglesDoublesAlgorithm.cxx:
+// 98-112); true when the solve stops here: converged, or an error in st
+bool Ccsd::absorb(IterInfo info, gbcc_status &st) {
+  e_ = info.energy;
+  dir_ = info.direct;
+  exc_ = info.exchange;
+  hist_.push_back(e_);
+  ++it_;
+  if (o_.mixer == 1 && ctx_.take_fault(GBCC_FAULT_DIIS_SINGULAR)) info.diis_status = 1;
+  if (ctx_.take_fault(GBCC_FAULT_NAN)) info.dtdt = std::numeric_limits<double>::quiet_NaN();
+  if (info.diis_status == 1) {
+    // an exact zero pivot: dsysv's info != 0 (DiisMixer.cxx:37-41)
+    ctx_.last_error = "DIIS subspace matrix singular at iteration " +
+                      std::to_string(it_ - 1) + " (|dT|^2 = " +
+                      std::to_string(info.dtdt) + ")";
+    st = GBCC_DIIS_SINGULAR;
+    return true;
+  }
+  if (info.diis_status == 2) {
+    // overlaps or weights overflowed: the reference's dsysv returns
+    // info == 0 there and its amplitudes become NaN
+    ctx_.last_error = "DIIS subspace matrix or weights not finite at iteration " +
+                      std::to_string(it_ - 1) + " (|dT|^2 = " +
+                      std::to_string(info.dtdt) + ", E = " + std::to_string(e_) + ")";
+    st = GBCC_DIVERGED;
+    return true;
+  }
+  if (!std::isfinite(e_) || !std::isfinite(info.dtdt) || !std::isfinite(info.tt)) {
+    ctx_.last_error = "energy or amplitude norms not finite at iteration " +
+                      std::to_string(it_ - 1);
+    st = GBCC_DIVERGED;
+    return true;
+  }
+  // ClusterSinglesDoublesAlgorithm.cxx:103-106
+  if (std::abs((e_ - prev_) / e_) < std::abs(o_.energy_convergence) &&
+      std::abs(info.dtdt / info.tt) <
+          std::abs(o_.amplitudes_convergence * o_.amplitudes_convergence)) {
+    converged_ = true;
+    return true;
+  }
+  prev_ = e_;
+  return false;
 }
 
 }  // namespace gbcc

@@ -26,6 +26,19 @@ std::unique_ptr<CcsdInputs> upload_inputs(Context &ctx, const gbcc_ccsd_in &in,
                                           int precision, bool need_vaibj,
                                           bool stored = false);
 
+// One residual evaluation over nz systems of one shape (residual_program).
+// With nz > 1 the input tensors, T1, T2, R1 and R2 carry a trailing system
+// index (each system's block contiguous); R1 and R2 arrive zeroed.
+struct ResidualArgs {
+  const CcsdInputs *I = nullptr;
+  const gbcc_ccsd_opts *o = nullptr;
+  int64_t nz = 1;
+  int64_t slice = 0;          // integralsSliceSize of the particle ladder
+  bool init_doubles = false;  // initial doubles given: no MP2 start at it 0
+  Ten T1, T2, R1, R2;
+};
+void residual_program(Context &ctx, const ResidualArgs &a, int it);
+
 struct IterInfo {
   double energy = 0, direct = 0, exchange = 0, noncanonical = 0, dtdt = 0, tt = 0,
          lambda = 0;
@@ -43,6 +56,19 @@ class Ccsd {
   void residual(int it, const double *T, double *R);
   // one full iteration; returns the host-side info
   IterInfo iterate();
+  // the parts of an iteration, for a driver that evaluates the residuals of
+  // several solvers at once: the graph key of the next iteration (allocating
+  // its DIIS slot), the device work after the residual (which must be in
+  // residual_buffer()), the host state after it, and the convergence test
+  // (true: the solve stops, with an error in st or converged)
+  int graph_key();
+  void mix_body();
+  IterInfo finish_iteration();
+  bool absorb(IterInfo info, gbcc_status &st);
+  double *residual_buffer() { return R_.as<double>(); }
+  double *amplitude_buffer() { return T_.as<double>(); }
+  bool has_initial_doubles() const { return init_doubles_; }
+  const gbcc_ccsd_opts &options() const { return o_; }
   // runs up to n iterations; returns status
   gbcc_status run(int n, double *energy, int *converged);
   const double *amplitudes() const { return T_.as<double>(); }

@@ -32,18 +32,22 @@ __device__ __forceinline__ double block_sum(double v, double *sm) {
 __global__ void outer_add_kernel(double *__restrict__ X,
                                  const double *__restrict__ T2,
                                  const double *__restrict__ T1, double c,
-                                 int64_t Nv, int64_t No) {
+                                 int64_t Nv, int64_t No, int64_t nz) {
+  // nz systems of one shape, each contiguous (X, T2: n apart; T1: Nv No)
   const int64_t n = Nv * Nv * No * No;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
-       e += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; f < n * nz;
+       f += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t z = f / n;
+    const int64_t e = f - z * n;
+    const double *t1 = T1 + z * Nv * No;
     int64_t r = e;
     const int64_t a = r % Nv; r /= Nv;
     const int64_t b = r % Nv; r /= Nv;
     const int64_t i = r % No;
     const int64_t j = r / No;
-    double p = __dmul_rn(T1[a + Nv * i], T1[b + Nv * j]);
+    double p = __dmul_rn(t1[a + Nv * i], t1[b + Nv * j]);
     if (c != 1.0) p = __dmul_rn(c, p);
-    X[e] = __dadd_rn(T2[e], p);
+    X[f] = __dadd_rn(T2[f], p);
   }
 }
 
@@ -302,37 +306,62 @@ __global__ void linear_mix_kernel(double *__restrict__ next,
 __global__ void slice_add_kernel(double *__restrict__ R,
                                  const double *__restrict__ Rxy, int64_t Nv,
                                  int64_t No, int64_t a0, int64_t b0,
-                                 int64_t nx, int64_t ny, int mirror) {
+                                 int64_t nx, int64_t ny, int mirror, int64_t nz) {
   const int64_t n = nx * ny * No * No;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
-       e += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; f < n * nz;
+       f += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t z = f / n;
+    const int64_t e = f - z * n;
+    double *Rz = R + z * Nv * Nv * No * No;
     int64_t r = e;
     const int64_t x = r % nx; r /= nx;
     const int64_t y = r % ny; r /= ny;
     const int64_t i = r % No;
     const int64_t j = r / No;
-    const double v = Rxy[e];
-    double *p = R + (a0 + x) + Nv * ((b0 + y) + Nv * (i + No * j));
+    const double v = Rxy[f];
+    double *p = Rz + (a0 + x) + Nv * ((b0 + y) + Nv * (i + No * j));
     *p = __dadd_rn(*p, v);
     if (mirror) {
-      double *q = R + (b0 + y) + Nv * ((a0 + x) + Nv * (j + No * i));
+      double *q = Rz + (b0 + y) + Nv * ((a0 + x) + Nv * (j + No * i));
       *q = __dadd_rn(*q, v);
     }
   }
 }
 
-// gather slice [G, x0:x0+nx, :] of a [G, Nv, Nv] tensor into [G, nx, Nv]
+// gather slice [G, x0:x0+nx, :] of a [G, Nv, Nv] tensor into [G, nx, Nv],
+// for nz systems of one shape stored one after another
 __global__ void gather_slice_kernel(double *__restrict__ dst,
                                     const double *__restrict__ src, int64_t G,
-                                    int64_t Nv, int64_t x0, int64_t nx) {
+                                    int64_t Nv, int64_t x0, int64_t nx, int64_t nz) {
   const int64_t n = G * nx * Nv;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
-       e += (int64_t)gridDim.x * blockDim.x) {
-    int64_t r = e;
+  for (int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; f < n * nz;
+       f += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t z = f / n;
+    int64_t r = f - z * n;
     const int64_t g = r % G; r /= G;
     const int64_t x = r % nx;
     const int64_t c = r / nx;
-    dst[e] = src[g + G * ((x0 + x) + Nv * c)];
+    dst[f] = src[z * G * Nv * Nv + g + G * ((x0 + x) + Nv * c)];
+  }
+}
+
+// systems of one shape side by side: gather dst[z n + e] = src[z][e],
+// scatter dst[z][e] = src[z n + e] (the per-system pointers in device memory)
+__global__ void batch_gather_kernel(const double *const *__restrict__ src, int64_t n,
+                                    int64_t nz, double *__restrict__ dst) {
+  for (int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; f < n * nz;
+       f += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t z = f / n;
+    dst[f] = src[z][f - z * n];
+  }
+}
+
+__global__ void batch_scatter_kernel(const double *__restrict__ src, int64_t n, int64_t nz,
+                                     double *const *__restrict__ dst) {
+  for (int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; f < n * nz;
+       f += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t z = f / n;
+    dst[z][f - z * n] = src[f];
   }
 }
 
@@ -377,9 +406,9 @@ int reduction_blocks(const Context &ctx, int64_t n) {
 }
 
 void outer_add(Context &ctx, double *X, const double *T2, const double *T1,
-               double c, int64_t Nv, int64_t No) {
-  outer_add_kernel<<<ew_grid(ctx, Nv * Nv * No * No), 256, 0, ctx.stream>>>(
-      X, T2, T1, c, Nv, No);
+               double c, int64_t Nv, int64_t No, int64_t nz) {
+  outer_add_kernel<<<ew_grid(ctx, Nv * Nv * No * No * nz), 256, 0, ctx.stream>>>(
+      X, T2, T1, c, Nv, No, nz);
   GBCC_CHECK_LAUNCH(ctx);
 }
 
@@ -460,16 +489,28 @@ void linear_mix(Context &ctx, double *next, double *nres, double *last,
 
 void slice_add(Context &ctx, double *R, const double *Rxy, int64_t Nv,
                int64_t No, int64_t a0, int64_t b0, int64_t nx, int64_t ny,
-               bool mirror) {
-  slice_add_kernel<<<ew_grid(ctx, nx * ny * No * No), 256, 0, ctx.stream>>>(
-      R, Rxy, Nv, No, a0, b0, nx, ny, mirror ? 1 : 0);
+               bool mirror, int64_t nz) {
+  slice_add_kernel<<<ew_grid(ctx, nx * ny * No * No * nz), 256, 0, ctx.stream>>>(
+      R, Rxy, Nv, No, a0, b0, nx, ny, mirror ? 1 : 0, nz);
   GBCC_CHECK_LAUNCH(ctx);
 }
 
 void gather_slice(Context &ctx, double *dst, const double *src, int64_t G,
-                  int64_t Nv, int64_t x0, int64_t nx) {
-  gather_slice_kernel<<<ew_grid(ctx, G * nx * Nv), 256, 0, ctx.stream>>>(
-      dst, src, G, Nv, x0, nx);
+                  int64_t Nv, int64_t x0, int64_t nx, int64_t nz) {
+  gather_slice_kernel<<<ew_grid(ctx, G * nx * Nv * nz), 256, 0, ctx.stream>>>(
+      dst, src, G, Nv, x0, nx, nz);
+  GBCC_CHECK_LAUNCH(ctx);
+}
+
+void batch_gather(Context &ctx, const double *const *src_dev, int64_t n, int64_t nz,
+                  double *dst) {
+  batch_gather_kernel<<<ew_grid(ctx, n * nz), 256, 0, ctx.stream>>>(src_dev, n, nz, dst);
+  GBCC_CHECK_LAUNCH(ctx);
+}
+
+void batch_scatter(Context &ctx, const double *src, int64_t n, int64_t nz,
+                   double *const *dst_dev) {
+  batch_scatter_kernel<<<ew_grid(ctx, n * nz), 256, 0, ctx.stream>>>(src, n, nz, dst_dev);
   GBCC_CHECK_LAUNCH(ctx);
 }
 

@@ -21,8 +21,9 @@ struct FockLayout {
 
 int reduction_blocks(const Context &ctx, int64_t n);
 
+// X = T2 + c T1 (x) T1 for nz systems of one shape stored one after another
 void outer_add(Context &ctx, double *X, const double *T2, const double *T1,
-               double c, int64_t Nv, int64_t No);
+               double c, int64_t Nv, int64_t No, int64_t nz = 1);
 // sums: [0] dT.dT, [1] est.est, [2+q] dT.hist[q]; partials sized
 // reduction_blocks(ntot) * (2 + nhist)
 void jacobi_update(Context &ctx, const FockLayout &L, const double *R,
@@ -49,9 +50,15 @@ void linear_mix(Context &ctx, double *next, double *nres, double *last,
                 double *sums2);
 void slice_add(Context &ctx, double *R, const double *Rxy, int64_t Nv,
                int64_t No, int64_t a0, int64_t b0, int64_t nx, int64_t ny,
-               bool mirror);
+               bool mirror, int64_t nz = 1);
 void gather_slice(Context &ctx, double *dst, const double *src, int64_t G,
-                  int64_t Nv, int64_t x0, int64_t nx);
+                  int64_t Nv, int64_t x0, int64_t nx, int64_t nz = 1);
+// nz systems' blocks of n doubles: gather dst[z n + e] = src[z][e], scatter
+// dst[z][e] = src[z n + e]; src_dev / dst_dev are device arrays of nz pointers
+void batch_gather(Context &ctx, const double *const *src_dev, int64_t n, int64_t nz,
+                  double *dst);
+void batch_scatter(Context &ctx, const double *src, int64_t n, int64_t nz,
+                   double *const *dst_dev);
 void vertex_block(Context &ctx, double *dst, const double *src, int64_t G,
                   int64_t Np, int64_t p0, int64_t np, int64_t q0, int64_t nq);
 void any_nonzero(Context &ctx, const double *p, int64_t n, int *flag_dev);

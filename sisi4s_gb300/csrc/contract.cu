@@ -143,11 +143,19 @@ void assign(Context &ctx, double alpha, const Ten &A, const char *ia,
 void contract(Context &ctx, double alpha, const Ten &A, const char *ia,
               const Ten &B, const char *ib, double beta, const Ten &C,
               const char *ic, int precision) {
-  const std::string sa(ia), sb(ib), sc(ic);
-  require((int)sa.size() == A.order && (int)sb.size() == B.order &&
-              (int)sc.size() == C.order,
-          "contract: index string / order mismatch: " + sa + "," + sb + "->" +
-              sc);
+  const std::string fa(ia), fb(ib), fc(ic);
+  // a batch index (in A, B and C) must be the last index of all three: the
+  // contraction then runs once per batch entry, as one batched GEMM
+  char z = 0;
+  if (!fa.empty() && fa.back() == fb.back() && fa.back() == fc.back())
+    z = fa.back();
+  const std::string sa = z ? fa.substr(0, fa.size() - 1) : fa;
+  const std::string sb = z ? fb.substr(0, fb.size() - 1) : fb;
+  const std::string sc = z ? fc.substr(0, fc.size() - 1) : fc;
+  require((int)fa.size() == A.order && (int)fb.size() == B.order &&
+              (int)fc.size() == C.order,
+          "contract: index string / order mismatch: " + fa + "," + fb + "->" +
+              fc);
   int64_t len[256];
   for (auto &l : len) l = -1;
   auto bind = [&](const std::string &s, const Ten &t) {
@@ -159,14 +167,15 @@ void contract(Context &ctx, double alpha, const Ten &A, const char *ia,
                   " in " + sa + "," + sb + "->" + sc);
     }
   };
-  bind(sa, A);
-  bind(sb, B);
-  bind(sc, C);
+  bind(fa, A);
+  bind(fb, B);
+  bind(fc, C);
+  const int64_t nz = z ? len[(unsigned char)z] : 1;
   std::string M, N, K;
   for (char c : sa) {
     const bool inB = sb.find(c) != std::string::npos;
     const bool inC = sc.find(c) != std::string::npos;
-    require(!(inB && inC), "contract: batch indices are not supported");
+    require(!(inB && inC), "contract: a batch index must be the last index of A, B and C");
     require(inB || inC, "contract: index summed in one operand only");
     if (inC) M += c; else K += c;
   }
@@ -209,7 +218,7 @@ void contract(Context &ctx, double alpha, const Ten &A, const char *ia,
         if (p.cost < best.cost) best = p;
       }
   const Plan &p = best;
-  if (ctx.use_panel_cache && precision == GBCC_PREC_EMU && sK > 0 && sM > 1 && sN > 1 &&
+  if (!z && ctx.use_panel_cache && precision == GBCC_PREC_EMU && sK > 0 && sM > 1 && sN > 1 &&
       2.0 * (double)sM * (double)sN * (double)sK >= ctx.emu_min_flops &&
       (ctx.is_constant(A.p, sizeof(double) * A.size()) ||
        ctx.is_constant(B.p, sizeof(double) * B.size()))) {
@@ -225,9 +234,9 @@ void contract(Context &ctx, double alpha, const Ten &A, const char *ia,
     ta_buf.alloc(ctx, sizeof(double) * A.size());
     Ten t = A;
     t.p = ta_buf.as<double>();
-    const std::string o = p.m + p.k;
+    const std::string o = p.m + p.k + (z ? std::string(1, z) : std::string());
     for (size_t d = 0; d < o.size(); ++d) t.lens[d] = len[(unsigned char)o[d]];
-    assign(ctx, 1.0, A, sa.c_str(), 0.0, t, o.c_str());
+    assign(ctx, 1.0, A, fa.c_str(), 0.0, t, o.c_str());
     pa = t.p;
     lda = sM;
   }
@@ -237,9 +246,9 @@ void contract(Context &ctx, double alpha, const Ten &A, const char *ia,
     tb_buf.alloc(ctx, sizeof(double) * B.size());
     Ten t = B;
     t.p = tb_buf.as<double>();
-    const std::string o = p.k + p.n;
+    const std::string o = p.k + p.n + (z ? std::string(1, z) : std::string());
     for (size_t d = 0; d < o.size(); ++d) t.lens[d] = len[(unsigned char)o[d]];
-    assign(ctx, 1.0, B, sb.c_str(), 0.0, t, o.c_str());
+    assign(ctx, 1.0, B, fb.c_str(), 0.0, t, o.c_str());
     pb = t.p;
     ldb = sK;
   }
@@ -250,20 +259,22 @@ void contract(Context &ctx, double alpha, const Ten &A, const char *ia,
     pc = tc_buf.as<double>();
     gbeta = 0.0;
   }
+  // per-entry strides of a batched contraction
+  const int64_t stA = sM * sK, stB = sK * sN, stC = sM * sN;
   if (!p.swap) {
     gemm(ctx, p.ta, p.tb, sM, sN, sK, alpha, pa, lda, pb, ldb, gbeta, pc, sM,
-         1, 0, 0, 0, precision);
+         nz, stA, stB, stC, precision);
   } else {
     // C^T[N,M] = op(B)^T op(A)^T
     gemm(ctx, !p.tb, !p.ta, sN, sM, sK, alpha, pb, ldb, pa, lda, gbeta, pc,
-         sN, 1, 0, 0, 0, precision);
+         sN, nz, stB, stA, stC, precision);
   }
   if (p.permC) {
     Ten t = C;
     t.p = pc;
-    const std::string o = p.m + p.n;
+    const std::string o = p.m + p.n + (z ? std::string(1, z) : std::string());
     for (size_t d = 0; d < o.size(); ++d) t.lens[d] = len[(unsigned char)o[d]];
-    assign(ctx, 1.0, t, o.c_str(), beta, C, sc.c_str());
+    assign(ctx, 1.0, t, o.c_str(), beta, C, fc.c_str());
   }
 }
 

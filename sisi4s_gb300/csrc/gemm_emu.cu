@@ -287,6 +287,9 @@ struct EmuArgs {
   // plain GEMM.  Grouped launches have ksplit = 1.
   int nprob = 1;
   const EmuProb *probs = nullptr;
+  // strided batch (probs = nullptr, nprob > 1): problem q uses the operands
+  // and output above advanced by q times these element strides
+  int64_t qsA = 0, qsB = 0, qsea = 0, qseb = 0, qsC = 0;
   // digit-panel output (the particle ladder): instead of C, the product
   // V[(x,c),(d,y)] is written as the S bf16 digits of the A operand of the
   // next product, rows r = x + px*y, K index k = d + pd*c (m = x + px*c,
@@ -304,7 +307,12 @@ struct EmuArgs {
 __device__ __forceinline__ EmuProb problem_of(const EmuArgs &a, int q) {
   if (a.probs) return a.probs[q];
   EmuProb p;
-  p.A = a.A; p.B = a.B; p.ea = a.ea; p.eb = a.eb; p.C = a.C; p.Cdf = a.Cdf;
+  p.A = a.A + q * a.qsA;
+  p.B = a.B + q * a.qsB;
+  p.ea = a.ea + q * a.qsea;
+  p.eb = a.eb + q * a.qseb;
+  p.C = a.C ? a.C + q * a.qsC : nullptr;
+  p.Cdf = a.Cdf ? a.Cdf + q * a.qsC : nullptr;
   return p;
 }
 
@@ -1203,30 +1211,46 @@ void gemm_panels(Context &ctx, const EmuPanels &A, int ia, const EmuPanels &B, i
 // share M, N, K, alpha, beta and ldc.  One persistent launch walks the tiles
 // of every problem, so a batch of small or short-K products fills the GPU
 // and pays one launch.
+// Without ia and ib (strided batch) problem q multiplies operand q of A with
+// operand q of B into C[0] + q sC: no table is uploaded, so the launch can be
+// captured into a graph.
 template <int S>
 void gemm_panels_grouped(Context &ctx, const EmuPanels &A, const int *ia, const EmuPanels &B,
                          const int *ib, int nprob, double alpha, double beta,
-                         double *const *C, df32 *const *Cdf, int64_t ldc) {
+                         double *const *C, df32 *const *Cdf, int64_t ldc, int64_t sC = 0) {
   const int64_t M = A.rows, N = B.rows, K = A.K;
   const EmuPlan P = emu_plan(S, M, N, K, ctx.sm_count, false);
   require((int64_t)P.mt * P.nt * nprob < (1LL << 31), "grouped GEMM: too many tiles");
   const int64_t aplane = (int64_t)A.rt * A.kt * TM * KB;
   const int64_t bplane = (int64_t)B.rt * B.kt * TN * KB;
-  std::vector<EmuProb> probs((size_t)nprob);
-  for (int q = 0; q < nprob; ++q) {
-    require(ia[q] >= 0 && ia[q] < A.count && ib[q] >= 0 && ib[q] < B.count,
-            "grouped GEMM: operand index");
-    EmuProb &e = probs[q];
-    e.A = A.panels.as<__nv_bfloat16>() + (int64_t)ia[q] * S * aplane;
-    e.B = B.panels.as<__nv_bfloat16>() + (int64_t)ib[q] * S * bplane;
-    e.ea = A.exps.as<int>() + (int64_t)ia[q] * M;
-    e.eb = B.exps.as<int>() + (int64_t)ib[q] * N;
-    e.C = C ? C[q] : nullptr;
-    e.Cdf = Cdf ? Cdf[q] : nullptr;
+  const bool strided = ia == nullptr;
+  DBuf table;
+  if (!strided) {
+    std::vector<EmuProb> probs((size_t)nprob);
+    for (int q = 0; q < nprob; ++q) {
+      require(ia[q] >= 0 && ia[q] < A.count && ib[q] >= 0 && ib[q] < B.count,
+              "grouped GEMM: operand index");
+      EmuProb &e = probs[q];
+      e.A = A.panels.as<__nv_bfloat16>() + (int64_t)ia[q] * S * aplane;
+      e.B = B.panels.as<__nv_bfloat16>() + (int64_t)ib[q] * S * bplane;
+      e.ea = A.exps.as<int>() + (int64_t)ia[q] * M;
+      e.eb = B.exps.as<int>() + (int64_t)ib[q] * N;
+      e.C = C ? C[q] : nullptr;
+      e.Cdf = Cdf ? Cdf[q] : nullptr;
+    }
+    // a copy from pageable memory has read its source when it returns, but
+    // a captured one would read it again at every replay
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    GBCC_CUDA(cudaStreamIsCapturing(ctx.stream, &cap));
+    require(cap == cudaStreamCaptureStatusNone,
+            "grouped GEMM: a problem table cannot be captured into a graph");
+    table.alloc(ctx, sizeof(EmuProb) * probs.size());
+    GBCC_CUDA(cudaMemcpyAsync(table.as<EmuProb>(), probs.data(),
+                              sizeof(EmuProb) * probs.size(), cudaMemcpyHostToDevice,
+                              ctx.stream));
+  } else {
+    require(nprob <= A.count && nprob <= B.count, "batched GEMM: operand count");
   }
-  DBuf table(ctx, sizeof(EmuProb) * probs.size());
-  GBCC_CUDA(cudaMemcpyAsync(table.as<EmuProb>(), probs.data(), sizeof(EmuProb) * probs.size(),
-                            cudaMemcpyHostToDevice, ctx.stream));
   constexpr int STAGE_BYTES = S * (A_TILE + B_TILE);
   constexpr int STAGES = (SMEM_BUDGET / STAGE_BYTES) > 4 ? 4 : (SMEM_BUDGET / STAGE_BYTES);
   const int smem = STAGES * STAGE_BYTES;
@@ -1244,7 +1268,21 @@ void gemm_panels_grouped(Context &ctx, const EmuPanels &A, const int *ia, const 
   args.beta = beta;
   args.err = ctx.device_error_word();
   args.nprob = nprob;
-  args.probs = table.as<EmuProb>();
+  if (strided) {
+    args.A = A.panels.as<__nv_bfloat16>();
+    args.B = B.panels.as<__nv_bfloat16>();
+    args.ea = A.exps.as<int>();
+    args.eb = B.exps.as<int>();
+    args.C = C ? C[0] : nullptr;
+    args.Cdf = Cdf ? Cdf[0] : nullptr;
+    args.qsA = S * aplane;
+    args.qsB = S * bplane;
+    args.qsea = M;
+    args.qseb = N;
+    args.qsC = sC;
+  } else {
+    args.probs = table.as<EmuProb>();
+  }
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   if (ctx.prof) {
     ev0 = ctx.prof_event();
@@ -1262,10 +1300,26 @@ void gemm_panels_grouped(Context &ctx, const EmuPanels &A, const int *ia, const 
 }
 }  // namespace
 
+void emu_gemm_panels_batched(Context &ctx, const EmuPanels &A, const EmuPanels &B, int nprob,
+                             double alpha, double beta, double *C, int64_t ldc, int64_t sC) {
+  require(nprob >= 1, "batched GEMM: no problems");
+  require(A.role_a && !B.role_a && A.K == B.K && A.S == B.S, "batched GEMM: operand mismatch");
+  double *const Cs[1] = {C};
+  switch (A.S) {
+    case 4: gemm_panels_grouped<4>(ctx, A, nullptr, B, nullptr, nprob, alpha, beta, Cs, nullptr, ldc, sC); break;
+    case 5: gemm_panels_grouped<5>(ctx, A, nullptr, B, nullptr, nprob, alpha, beta, Cs, nullptr, ldc, sC); break;
+    case 6: gemm_panels_grouped<6>(ctx, A, nullptr, B, nullptr, nprob, alpha, beta, Cs, nullptr, ldc, sC); break;
+    case 7: gemm_panels_grouped<7>(ctx, A, nullptr, B, nullptr, nprob, alpha, beta, Cs, nullptr, ldc, sC); break;
+    case 8: gemm_panels_grouped<8>(ctx, A, nullptr, B, nullptr, nprob, alpha, beta, Cs, nullptr, ldc, sC); break;
+    default: throw Error(GBCC_BAD_ARG, "emu_slices must be in [4, 8]");
+  }
+}
+
 void emu_gemm_panels_grouped(Context &ctx, const EmuPanels &A, const int *ia,
                              const EmuPanels &B, const int *ib, int nprob, double alpha,
                              double beta, double *const *C, df32 *const *Cdf, int64_t ldc) {
   require(nprob >= 1, "grouped GEMM: no problems");
+  require(ia != nullptr && ib != nullptr, "grouped GEMM: operand indices");
   require(A.role_a && !B.role_a && A.K == B.K && A.S == B.S, "grouped GEMM: operand mismatch");
   require((C == nullptr) != (Cdf == nullptr), "grouped GEMM: one output kind");
   if (Cdf)
@@ -1483,6 +1537,20 @@ void gemm_emu(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
               double alpha, const double *A, int64_t lda, const double *B,
               int64_t ldb, double beta, double *C, int64_t ldc, int64_t batch,
               int64_t sA, int64_t sB, int64_t sC) {
+  const EmuPlan P1 = emu_plan(ctx.emu_slices, M, N, K, ctx.sm_count, true, ctx.emu_max_ksplit);
+  if (batch > 1 && batch < (1 << 20) &&
+      (P1.ksplit == 1 || (int64_t)P1.mt * P1.nt * batch >= ctx.sm_count)) {
+    // a batch of same-shape products: the operands of all entries are split
+    // into one panel family each, and one grouped launch walks the tiles of
+    // every entry.  (A few-tile product with long K keeps its K-split
+    // instead, entry by entry, unless the batch alone fills the GPU.)
+    const int64_t ars = ta ? lda : 1, aks = ta ? 1 : lda;
+    const int64_t brs = tb ? 1 : ldb, bks = tb ? ldb : 1;
+    EmuPanels PA = emu_split(ctx, true, A, M, K, ars, aks, (int)batch, sA);
+    EmuPanels PB = emu_split(ctx, false, B, N, K, brs, bks, (int)batch, sB);
+    emu_gemm_panels_batched(ctx, PA, PB, (int)batch, alpha, beta, C, ldc, sC);
+    return;
+  }
   for (int64_t z = 0; z < batch; ++z) {
     const double *Az = A + z * sA;
     const double *Bz = B + z * sB;

@@ -387,7 +387,9 @@ void gemm(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
     ctx.flops += fl;
     return;
   }
-  if (precision == GBCC_PREC_EMU && K > 0 && fl >= ctx.emu_min_flops) {
+  // the tensor-core threshold is per batch entry, so that a product takes the
+  // same precision route alone and inside a batch of systems
+  if (precision == GBCC_PREC_EMU && K > 0 && fl / (double)batch >= ctx.emu_min_flops) {
     gemm_emu(ctx, ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, batch,
              sA, sB, sC);
     return;

@@ -261,6 +261,15 @@ inline Ten ten(double *p, std::initializer_list<int64_t> l) {
   for (auto x : l) t.lens[d++] = x;
   return t;
 }
+inline Ten ten(double *p, const std::vector<int64_t> &l) {
+  require(l.size() <= 6, "tensor order above 6");
+  Ten t;
+  t.p = p;
+  t.order = static_cast<int>(l.size());
+  int d = 0;
+  for (auto x : l) t.lens[d++] = x;
+  return t;
+}
 
 // Owned tensor = buffer + view.
 struct OTen {
@@ -268,6 +277,11 @@ struct OTen {
   Ten t;
   OTen() = default;
   OTen(Context &ctx, std::initializer_list<int64_t> l) {
+    t = ten(nullptr, l);
+    buf.alloc(ctx, sizeof(double) * t.size());
+    t.p = buf.as<double>();
+  }
+  OTen(Context &ctx, const std::vector<int64_t> &l) {
     t = ten(nullptr, l);
     buf.alloc(ctx, sizeof(double) * t.size());
     t.p = buf.as<double>();
@@ -321,6 +335,10 @@ void emu_gemm_panels(Context &ctx, const EmuPanels &A, int ia, const EmuPanels &
 void emu_gemm_panels_grouped(Context &ctx, const EmuPanels &A, const int *ia,
                              const EmuPanels &B, const int *ib, int nprob, double alpha,
                              double beta, double *const *C, df32 *const *Cdf, int64_t ldc);
+// Strided batch: problem q multiplies operand q of A with operand q of B into
+// C + q sC, in one launch that can be captured into a graph.
+void emu_gemm_panels_batched(Context &ctx, const EmuPanels &A, const EmuPanels &B, int nprob,
+                             double alpha, double beta, double *C, int64_t ldc, int64_t sC);
 // Panels of one operand, allocated but not filled (their digits and row
 // exponents are written by a producer such as gemm_emu_to_panels).
 EmuPanels emu_panels_alloc(Context &ctx, bool role_a, int64_t R, int64_t K);

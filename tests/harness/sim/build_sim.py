@@ -18,7 +18,7 @@ LIB = os.path.join(OUT, "libgbcc_sim.so")
 LD_DIR = os.path.join(OUT, "ld")
 
 #: the library's translation units that hold host code only
-HOST_UNITS = ["capi.cu", "ccsd.cu", "ccsd_complex.cu", "ccsd_stored.cu", "contract.cu",
+HOST_UNITS = ["capi.cu", "ccsd.cu", "ccsd_batch.cu", "ccsd_complex.cu", "ccsd_stored.cu", "contract.cu",
               "serve.cu"]
 SIM_UNITS = ["sim_runtime.cpp", "sim_kernels.cpp"]
 

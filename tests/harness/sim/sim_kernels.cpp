@@ -265,9 +265,14 @@ void gemm_emu_noalloc(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int6
 }
 
 // ---------------------------------------------------------- ccsd_kernels.cu
-void outer_add(Context &ctx, double *X, const double *T2, const double *T1, double c,
-               int64_t Nv, int64_t No) {
+void outer_add(Context &ctx, double *X0, const double *T20, const double *T10, double c,
+               int64_t Nv, int64_t No, int64_t nz) {
+  const int64_t n2 = Nv * Nv * No * No;
+  for (int64_t z = 0; z < nz; ++z)
   launch(ctx, [=]() {
+    double *X = X0 + z * n2;
+    const double *T2 = T20 + z * n2;
+    const double *T1 = T10 + z * Nv * No;
     for (int64_t j = 0; j < No; ++j)
       for (int64_t i = 0; i < No; ++i)
         for (int64_t b = 0; b < Nv; ++b)
@@ -469,9 +474,12 @@ void linear_mix(Context &ctx, double *next, double *nres, double *last, double *
   });
 }
 
-void slice_add(Context &ctx, double *R, const double *Rxy, int64_t Nv, int64_t No,
-               int64_t a0, int64_t b0, int64_t nx, int64_t ny, bool mirror) {
+void slice_add(Context &ctx, double *R0, const double *Rxy0, int64_t Nv, int64_t No,
+               int64_t a0, int64_t b0, int64_t nx, int64_t ny, bool mirror, int64_t nz) {
+  for (int64_t z = 0; z < nz; ++z)
   launch(ctx, [=]() {
+    double *R = R0 + z * Nv * Nv * No * No;
+    const double *Rxy = Rxy0 + z * nx * ny * No * No;
     for (int64_t j = 0; j < No; ++j)
       for (int64_t i = 0; i < No; ++i)
         for (int64_t y = 0; y < ny; ++y)
@@ -483,13 +491,32 @@ void slice_add(Context &ctx, double *R, const double *Rxy, int64_t Nv, int64_t N
   });
 }
 
-void gather_slice(Context &ctx, double *dst, const double *src, int64_t G, int64_t Nv,
-                  int64_t x0, int64_t nx) {
+void gather_slice(Context &ctx, double *dst0, const double *src0, int64_t G, int64_t Nv,
+                  int64_t x0, int64_t nx, int64_t nz) {
+  for (int64_t z = 0; z < nz; ++z)
   launch(ctx, [=]() {
+    double *dst = dst0 + z * G * nx * Nv;
+    const double *src = src0 + z * G * Nv * Nv;
     for (int64_t c = 0; c < Nv; ++c)
       for (int64_t x = 0; x < nx; ++x)
         for (int64_t g = 0; g < G; ++g)
           dst[g + G * (x + nx * c)] = src[g + G * ((x0 + x) + Nv * c)];
+  });
+}
+
+void batch_gather(Context &ctx, const double *const *src_dev, int64_t n, int64_t nz,
+                  double *dst) {
+  launch(ctx, [=]() {
+    for (int64_t z = 0; z < nz; ++z)
+      for (int64_t e = 0; e < n; ++e) dst[z * n + e] = src_dev[z][e];
+  });
+}
+
+void batch_scatter(Context &ctx, const double *src, int64_t n, int64_t nz,
+                   double *const *dst_dev) {
+  launch(ctx, [=]() {
+    for (int64_t z = 0; z < nz; ++z)
+      for (int64_t e = 0; e < n; ++e) dst_dev[z][e] = src[z * n + e];
   });
 }
 

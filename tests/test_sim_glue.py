@@ -37,7 +37,7 @@ RUNNER = ["tests/test_gpu_runner.py"]
 NEW_PATHS = ["tests/test_zzz_energy_terms.py", "tests/test_zzz_complex_branch.py",
              "tests/test_zzz_stored_formulation.py", "tests/test_zzz_golden_fixtures.py",
              "tests/test_zzz_solver_options.py", "tests/test_zzz_stepping_api.py",
-             "tests/test_zzz_failure_new_paths.py"]
+             "tests/test_zzz_failure_new_paths.py", "tests/test_gpu_batch.py"]
 
 
 @pytest.fixture(scope="module")
