@@ -238,6 +238,20 @@ gbcc_status gbcc_ccsd_solve_batch(gbcc_ctx *ctx, int nsys, const gbcc_ccsd_in *i
                                   const gbcc_ccsd_opts *opts, gbcc_ccsd_out *outs,
                                   gbcc_status *status);
 
+/* The same batch kept on the device (as gbcc_ccsd_setup / _step / _result do
+ * for one system): setup uploads 1 to 64 systems of one shape; step runs up
+ * to n more lockstep iterations and writes every system's status; result
+ * reads system z back; triples runs (T) on system z's amplitudes
+ * (gbcc_triples_from_solver for one member of the batch). */
+typedef struct gbcc_batch gbcc_batch;
+gbcc_status gbcc_ccsd_batch_setup(gbcc_ctx *ctx, int nsys, const gbcc_ccsd_in *ins,
+                                  const gbcc_ccsd_opts *opts, gbcc_batch **out);
+gbcc_status gbcc_ccsd_batch_step(gbcc_batch *b, int n, gbcc_status *status);
+gbcc_status gbcc_ccsd_batch_result(gbcc_batch *b, int z, gbcc_ccsd_out *out);
+gbcc_status gbcc_ccsd_batch_triples(gbcc_batch *b, int z, int precision, double *e_total,
+                                    double *e_t);
+void gbcc_ccsd_batch_destroy(gbcc_batch *b);
+
 /* Device-resident solver: setup uploads inputs and builds integrals once;
  * step runs n more iterations (stopping early on convergence);
  * amplitudes can then be read back or handed to the (T) step. */
@@ -357,6 +371,12 @@ typedef struct {
   int device;
   int slots;                 /* concurrent solves, default 8 */
   int64_t hbm_budget_bytes;  /* 0: 80 % of the free device memory */
+  int max_batch;             /* > 1: a slot that admits a request of a small
+                                shape (one whose particle-ladder block leaves
+                                most SMs idle) also takes up to max_batch - 1
+                                queued requests of the same shape, options and
+                                (T) flag, and solves them in lockstep
+                                (gbcc_ccsd_batch_*); default 8 */
 } gbcc_server_opts;
 
 typedef struct {

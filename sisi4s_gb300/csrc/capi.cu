@@ -30,6 +30,12 @@ struct gbcc_solver {
   gbcc_ccsd_opts opts;
 };
 
+struct gbcc_batch {
+  gbcc_ctx *ctx;
+  std::unique_ptr<gbcc::BatchCcsd> b;
+  gbcc_ccsd_opts opts;
+};
+
 namespace {
 
 thread_local std::string g_err;
@@ -346,15 +352,14 @@ void fill_result(gbcc::Ccsd &c, gbcc::Context &ctx, gbcc_ccsd_out *out) {
 }
 }  // namespace
 
-gbcc_status gbcc_ccsd_solve_batch(gbcc_ctx *ctx, int nsys, const gbcc_ccsd_in *ins,
-                                  const gbcc_ccsd_opts *opts, gbcc_ccsd_out *outs,
-                                  gbcc_status *status) {
-  if (!ctx || !ins || nsys < 1 || !status) return GBCC_BAD_ARG;
+gbcc_status gbcc_ccsd_batch_setup(gbcc_ctx *ctx, int nsys, const gbcc_ccsd_in *ins,
+                                  const gbcc_ccsd_opts *opts, gbcc_batch **out) {
+  if (!ctx || !ins || nsys < 1 || nsys > 64 || !out) return GBCC_BAD_ARG;
+  *out = nullptr;
   return guard(ctx, [&]() {
     gbcc_ccsd_opts o;
     if (opts) o = *opts; else gbcc_ccsd_opts_default(&o);
     check_opts(o);
-    gbcc::require(o.max_iterations >= 1, "a batch of systems needs maxIterations >= 1");
     apply_precision_opts(ctx->c, o);
     std::vector<std::unique_ptr<gbcc::Ccsd>> sys;
     for (int z = 0; z < nsys; ++z) {
@@ -362,29 +367,79 @@ gbcc_status gbcc_ccsd_solve_batch(gbcc_ctx *ctx, int nsys, const gbcc_ccsd_in *i
       sys.push_back(std::make_unique<gbcc::Ccsd>(ctx->c, std::move(inputs), o, ins[z].init_T1,
                                                  ins[z].init_T2));
     }
-    std::vector<gbcc_status> st((size_t)nsys, GBCC_OK);
-    std::vector<gbcc::Ccsd *> done;
-    std::unique_ptr<gbcc::BatchCcsd> batch;
-    if (nsys == 1) {
-      st[0] = sys[0]->run(o.max_iterations, nullptr, nullptr);
-      done.push_back(sys[0].get());
-    } else {
-      batch = std::make_unique<gbcc::BatchCcsd>(ctx->c, std::move(sys));
-      batch->run(o.max_iterations);
-      for (int z = 0; z < nsys; ++z) {
-        st[z] = batch->status(z);
-        done.push_back(&batch->system(z));
-      }
-    }
-    for (int z = 0; z < nsys; ++z) {
-      gbcc::Ccsd &c = *done[z];
-      status[z] = st[z] != GBCC_OK ? st[z] : (c.converged() ? GBCC_OK : GBCC_NOT_CONVERGED);
-      if (outs) fill_result(c, ctx->c, &outs[z]);
-    }
-    GBCC_CUDA(cudaStreamSynchronize(ctx->c.stream));
-    ctx->c.check_device_errors();
+    auto b = std::make_unique<gbcc_batch>();
+    b->ctx = ctx;
+    b->opts = o;
+    b->b = std::make_unique<gbcc::BatchCcsd>(ctx->c, std::move(sys));
+    *out = b.release();
     return GBCC_OK;
   });
+}
+
+gbcc_status gbcc_ccsd_batch_step(gbcc_batch *b, int n, gbcc_status *status) {
+  if (!b) return GBCC_BAD_ARG;
+  return guard(b->ctx, [&]() {
+    b->b->run(n);
+    if (status)
+      for (int z = 0; z < b->b->size(); ++z) {
+        const gbcc::Ccsd &c = b->b->system(z);
+        status[z] = b->b->status(z) != GBCC_OK
+                        ? b->b->status(z)
+                        : (c.converged() ? GBCC_OK : GBCC_NOT_CONVERGED);
+      }
+    return GBCC_OK;
+  });
+}
+
+gbcc_status gbcc_ccsd_batch_result(gbcc_batch *b, int z, gbcc_ccsd_out *out) {
+  if (!b || !out || z < 0 || z >= b->b->size()) return GBCC_BAD_ARG;
+  return guard(b->ctx, [&]() {
+    fill_result(b->b->system(z), b->ctx->c, out);
+    GBCC_CUDA(cudaStreamSynchronize(b->ctx->c.stream));
+    return GBCC_OK;
+  });
+}
+
+gbcc_status gbcc_ccsd_batch_triples(gbcc_batch *b, int z, int precision, double *e_total,
+                                    double *e_t) {
+  if (!b || z < 0 || z >= b->b->size()) return GBCC_BAD_ARG;
+  return guard(b->ctx, [&]() {
+    gbcc::Ccsd &c = b->b->system(z);
+    const double *T = c.amplitudes();
+    const double et = gbcc::triples_energy(b->ctx->c, c.inputs(), T, T + c.layout().off2,
+                                           precision);
+    if (e_t) *e_t = et;
+    if (e_total) *e_total = c.energy() + et;
+    return GBCC_OK;
+  });
+}
+
+void gbcc_ccsd_batch_destroy(gbcc_batch *b) {
+  if (!b) return;
+  cudaSetDevice(b->ctx->c.device);
+  b->b.reset();
+  cudaStreamSynchronize(b->ctx->c.stream);
+  delete b;
+}
+
+gbcc_status gbcc_ccsd_solve_batch(gbcc_ctx *ctx, int nsys, const gbcc_ccsd_in *ins,
+                                  const gbcc_ccsd_opts *opts, gbcc_ccsd_out *outs,
+                                  gbcc_status *status) {
+  if (!ctx || !ins || nsys < 1 || !status) return GBCC_BAD_ARG;
+  gbcc_ccsd_opts o;
+  if (opts) o = *opts; else gbcc_ccsd_opts_default(&o);
+  if (o.max_iterations < 1) {
+    ctx->c.last_error = "a batch of systems needs maxIterations >= 1";
+    return GBCC_BAD_ARG;
+  }
+  gbcc_batch *b = nullptr;
+  gbcc_status st = gbcc_ccsd_batch_setup(ctx, nsys, ins, &o, &b);
+  if (st != GBCC_OK) return st;
+  st = gbcc_ccsd_batch_step(b, o.max_iterations, status);
+  for (int z = 0; z < nsys && st == GBCC_OK && outs; ++z)
+    st = gbcc_ccsd_batch_result(b, z, &outs[z]);
+  gbcc_ccsd_batch_destroy(b);
+  return st;
 }
 
 gbcc_status gbcc_ccsd_result(gbcc_solver *s, gbcc_ccsd_out *out) {

@@ -394,35 +394,51 @@ void residual_program(Context &ctx, const ResidualArgs &ra, int it) {
     // takes its B operand as [G, d, y] and R sums over k = d + Nv c, so X
     // enters as X'[d,c,i,j] = X[c,d,i,j].
     const int64_t s_last = Nv - (ns - 1) * s;
-    const bool fused = nz == 1 && Nv % 8 == 0 && emulated(s_last * Nv, s_last * Nv, NG) &&
+    // (over a batch, when one system's V block alone fills half the GPU
+    // with output tiles; smaller ladders run as batched products below)
+    const int64_t vtiles = ((s * Nv + 127) / 128) * ((s * Nv + 63) / 64);
+    const bool fused = (nz == 1 || 2 * vtiles >= ctx.sm_count) && Nv % 8 == 0 &&
+                       emulated(s_last * Nv, s_last * Nv, NG) &&
                        emulated(s_last * s_last, No * No, Nv * Nv);
     if (fused) {
-      DBuf amax(ctx, sizeof(unsigned long long) * Nv);
-      ladder_amax(ctx, dG.p(), NG, Nv, amax.as<void>());
-      std::vector<OTen> slT;
-      for (int64_t v = 0; v < ns; ++v) {
-        const int64_t nx = sl[v].t.lens[1];
-        slT.emplace_back(ctx, std::initializer_list<int64_t>{NG, Nv, nx});
-        assign(ctx, 1.0, sl[v], "Gyd", 0.0, slT.back(), "Gdy");
-      }
-      EmuPanels Xq;
-      {
-        OTen Xt(ctx, {Nv, Nv, No, No});
-        assign(ctx, 1.0, X, "cdij", 0.0, Xt, "dcij");
-        Xq = emu_split(ctx, false, Xt.p(), No * No, Nv * Nv, Nv * Nv, 1, 1, 0);
-      }
-      for (int64_t m = 0; m < ns; ++m) {                           // :418
-        for (int64_t n = m; n < ns; ++n) {                         // :419
-          const int64_t nx = sl[n].t.lens[1], ny = sl[m].t.lens[1];
-          const int64_t a0 = n * s, b0 = m * s;
-          EmuPanels Vp = emu_panels_alloc(ctx, true, nx * ny, Nv * Nv);
-          ladder_row_exponents(ctx, amax.as<void>(), a0, nx, b0, ny, Vp.exps.as<int>());
-          // V[(x,c),(d,y)] = sum_G sl_n[G,(x,c)] slT_m[G,(d,y)]   :425-434
-          gemm_emu_to_panels(ctx, nx * Nv, ny * Nv, NG, sl[n].p(), NG, slT[m].p(), NG, nx,
-                             Nv, Vp);
-          OTen Rxy(ctx, {nx, ny, No, No});                         // :443
-          emu_gemm_panels(ctx, Vp, 0, Xq, 0, 1.0, 0.0, Rxy.p(), nx * ny);
-          slice_add(ctx, R2.p, Rxy.p(), Nv, No, a0, b0, nx, ny, a0 > b0);  // :444-447
+      // system by system over a batch (each system's V blocks fill the GPU)
+      for (int64_t z = 0; z < nz; ++z) {
+        const int64_t sz_dG = NG * Nv * Nv;
+        DBuf amax(ctx, sizeof(unsigned long long) * Nv);
+        ladder_amax(ctx, dG.p() + z * sz_dG, NG, Nv, amax.as<void>());
+        // every slice's digit panels, split once for all its slice pairs: as
+        // the A operand sl[G,(x,c)] and, transposed, as the B operand
+        // slT[G,(d,y)]
+        std::vector<EmuPanels> slA, slB;
+        for (int64_t v = 0; v < ns; ++v) {
+          const int64_t nx = sl[v].t.lens[1];
+          double *slz = sl[v].p() + z * NG * nx * Nv;
+          {
+            OTen slT(ctx, {NG, Nv, nx});
+            assign(ctx, 1.0, ten(slz, {NG, nx, Nv}), "Gyd", 0.0, slT, "Gdy");
+            slB.push_back(emu_split(ctx, false, slT.p(), nx * Nv, NG, NG, 1, 1, 0));
+          }
+          slA.push_back(emu_split(ctx, true, slz, nx * Nv, NG, NG, 1, 1, 0));
+        }
+        EmuPanels Xq;
+        {
+          OTen Xt(ctx, {Nv, Nv, No, No});
+          assign(ctx, 1.0, ten(X.p() + z * n2, {Nv, Nv, No, No}), "cdij", 0.0, Xt, "dcij");
+          Xq = emu_split(ctx, false, Xt.p(), No * No, Nv * Nv, Nv * Nv, 1, 1, 0);
+        }
+        for (int64_t m = 0; m < ns; ++m) {                         // :418
+          for (int64_t n = m; n < ns; ++n) {                       // :419
+            const int64_t nx = sl[n].t.lens[1], ny = sl[m].t.lens[1];
+            const int64_t a0 = n * s, b0 = m * s;
+            EmuPanels Vp = emu_panels_alloc(ctx, true, nx * ny, Nv * Nv);
+            ladder_row_exponents(ctx, amax.as<void>(), a0, nx, b0, ny, Vp.exps.as<int>());
+            // V[(x,c),(d,y)] = sum_G sl_n[G,(x,c)] slT_m[G,(d,y)]   :425-434
+            emu_gemm_panels_to_panels(ctx, slA[n], 0, slB[m], 0, nx, Nv, Vp);
+            OTen Rxy(ctx, {nx, ny, No, No});                       // :443
+            emu_gemm_panels(ctx, Vp, 0, Xq, 0, 1.0, 0.0, Rxy.p(), nx * ny);
+            slice_add(ctx, R2.p + z * n2, Rxy.p(), Nv, No, a0, b0, nx, ny,
+                      a0 > b0);                                    // :444-447
+          }
         }
       }
     }

@@ -9,10 +9,17 @@
 
 namespace gbcc {
 
+namespace {
+// the residual's inputs, stacked over the running systems
+constexpr OTen CcsdInputs::*kStacked[] = {
+    &CcsdInputs::Vabij, &CcsdInputs::Vx,  &CcsdInputs::Vaibj, &CcsdInputs::Vijkl,
+    &CcsdInputs::Vijka, &CcsdInputs::Gai, &CcsdInputs::Gab,   &CcsdInputs::Gij};
+}  // namespace
+
 BatchCcsd::BatchCcsd(Context &ctx, std::vector<std::unique_ptr<Ccsd>> systems)
     : ctx_(ctx), sys_(std::move(systems)) {
   nz_ = (int64_t)sys_.size();
-  require(nz_ >= 2 && nz_ <= 64, "a batch holds 2 to 64 systems");
+  require(nz_ >= 1 && nz_ <= 64, "a batch holds 1 to 64 systems");
   Ccsd &s0 = *sys_[0];
   o_ = s0.options();
   L_ = s0.layout();
@@ -53,27 +60,28 @@ BatchCcsd::BatchCcsd(Context &ctx, std::vector<std::unique_ptr<Ccsd>> systems)
   in_.No = No;
   in_.Nv = Nv;
   in_.NG = I0.NG;
-  auto stack = [&](OTen &dst, OTen CcsdInputs::*field) {
-    const Ten &t0 = sys_[0]->inputs().*field;
+  for (auto f : kStacked) {
+    OTen &dst = in_.*f;
+    const Ten &t0 = sys_[0]->inputs().*f;
+    if (nz_ == 1) {  // a batch of one: the system's own inputs, viewed
+      dst.t = t0;
+      continue;
+    }
     std::vector<int64_t> l(t0.lens.begin(), t0.lens.begin() + t0.order);
     l.push_back(nz_);
     dst = OTen(ctx_, l);
     const int64_t n = t0.size();
     for (int64_t z = 0; z < nz_; ++z) {
-      const Ten &t = sys_[z]->inputs().*field;
+      const Ten &t = sys_[z]->inputs().*f;
       require(t.p != nullptr && t.size() == n, "batch: missing input block");
       GBCC_CUDA(cudaMemcpyAsync(dst.p() + z * n, t.p, sizeof(double) * n,
                                 cudaMemcpyDeviceToDevice, ctx_.stream));
     }
-  };
-  stack(in_.Vabij, &CcsdInputs::Vabij);
-  stack(in_.Vx, &CcsdInputs::Vx);
-  stack(in_.Vaibj, &CcsdInputs::Vaibj);
-  stack(in_.Vijkl, &CcsdInputs::Vijkl);
-  stack(in_.Vijka, &CcsdInputs::Vijka);
-  stack(in_.Gai, &CcsdInputs::Gai);
-  stack(in_.Gab, &CcsdInputs::Gab);
-  stack(in_.Gij, &CcsdInputs::Gij);
+    // unchanged while the set of running systems is: their digit panels are
+    // split once (and dropped when the batch shrinks)
+    ctx_.register_constant(dst.p(), sizeof(double) * (size_t)dst.t.size());
+  }
+  if (nz_ > 1) in_.ctx = &ctx_;  // forgets the stacked inputs on destruction
   T1b_.alloc(ctx_, sizeof(double) * L_.n1 * nz_);
   T2b_.alloc(ctx_, sizeof(double) * L_.n2 * nz_);
   R1b_.alloc(ctx_, sizeof(double) * L_.n1 * nz_);
@@ -81,10 +89,10 @@ BatchCcsd::BatchCcsd(Context &ctx, std::vector<std::unique_ptr<Ccsd>> systems)
   // the residual is scattered into each system's T1 and T2 blocks only: the
   // padding between them stays zero, as the update's reductions expect
   for (auto &s : sys_) fill(ctx_, s->residual_buffer(), L_.ntot, 0.0);
-  zeros_.alloc(ctx_, sizeof(double) * std::max(L_.n1, L_.n2));
-  fill(ctx_, zeros_.as<double>(), std::max(L_.n1, L_.n2), 0.0);
   ptrs_.alloc(ctx_, sizeof(double *) * 4 * nz_);
-  upload_pointers(~0ull);
+  run_.resize(nz_);
+  for (int64_t z = 0; z < nz_; ++z) run_[z] = (int)z;
+  upload_pointers();
   ctx_.check_device_errors();
 }
 
@@ -94,49 +102,79 @@ BatchCcsd::~BatchCcsd() {
     if (g.second.exec) cudaGraphExecDestroy(g.second.exec);
 }
 
-// the gather and scatter pointers: a system that no longer runs gives zero
-// amplitudes to the residual program, so that its own amplitudes (not finite
-// after a failure) never reach a product; its residual buffer takes a
-// residual that nothing reads
-void BatchCcsd::upload_pointers(uint64_t mask) {
-  std::vector<double *> p((size_t)(4 * nz_));
-  for (int64_t z = 0; z < nz_; ++z) {
-    const bool on = (mask >> z) & 1;
-    double *T = sys_[z]->amplitude_buffer(), *R = sys_[z]->residual_buffer();
-    p[0 * nz_ + z] = on ? T : zeros_.as<double>();
-    p[1 * nz_ + z] = on ? T + L_.off2 : zeros_.as<double>();
-    p[2 * nz_ + z] = R;
-    p[3 * nz_ + z] = R + L_.off2;
+// the gather and scatter pointers of the running systems, in stacked order
+void BatchCcsd::upload_pointers() {
+  const int64_t n = (int64_t)run_.size();
+  std::vector<double *> p((size_t)(4 * n));
+  for (int64_t j = 0; j < n; ++j) {
+    double *T = sys_[run_[j]]->amplitude_buffer(), *R = sys_[run_[j]]->residual_buffer();
+    p[0 * n + j] = T;
+    p[1 * n + j] = T + L_.off2;
+    p[2 * n + j] = R;
+    p[3 * n + j] = R + L_.off2;
   }
   GBCC_CUDA(cudaMemcpyAsync(ptrs_.as<double *>(), p.data(), sizeof(double *) * p.size(),
                             cudaMemcpyHostToDevice, ctx_.stream));
-  ptr_mask_ = mask;
 }
 
-// device work of one lockstep iteration for the running systems in mask
-void BatchCcsd::body(uint64_t mask) {
+// Drops the systems that stopped from the stacked inputs: the blocks of the
+// running ones move down in place (in order, so no block overwrites one
+// still to be moved), and the residual program then works on them alone.
+void BatchCcsd::compact(uint64_t mask) {
+  std::vector<int> keep;
+  for (int z : run_)
+    if ((mask >> z) & 1) keep.push_back(z);
+  for (auto f : kStacked) {
+    OTen &t = in_.*f;
+    ctx_.forget_constant(t.p());
+    const int64_t n = t.t.size() / t.t.lens[t.t.order - 1];
+    for (size_t j = 0, p = 0; j < keep.size(); ++j) {
+      while (run_[p] != keep[j]) ++p;
+      if (p != j)
+        GBCC_CUDA(cudaMemcpyAsync(t.p() + j * n, t.p() + p * n, sizeof(double) * n,
+                                  cudaMemcpyDeviceToDevice, ctx_.stream));
+    }
+    // one system left: its inputs lose the system index (the plain program)
+    if (keep.size() == 1) t.t.order -= 1;
+    else t.t.lens[t.t.order - 1] = (int64_t)keep.size();
+    ctx_.register_constant(t.p(), sizeof(double) * (size_t)t.t.size());
+  }
+  run_ = keep;
+  upload_pointers();
+}
+
+// device work of one lockstep iteration of the running systems
+void BatchCcsd::body() {
   Context &ctx = ctx_;
-  const int64_t No = L_.No, Nv = L_.Nv;
+  const int64_t No = L_.No, Nv = L_.Nv, nz = (int64_t)run_.size();
   double *const *p = ptrs_.as<double *>();
-  batch_gather(ctx, p + 0 * nz_, L_.n1, nz_, T1b_.as<double>());
-  batch_gather(ctx, p + 1 * nz_, L_.n2, nz_, T2b_.as<double>());
-  fill(ctx, R1b_.as<double>(), L_.n1 * nz_, 0.0);                 // :37-38
-  fill(ctx, R2b_.as<double>(), L_.n2 * nz_, 0.0);
+  batch_gather(ctx, p + 0 * nz, L_.n1, nz, T1b_.as<double>());
+  batch_gather(ctx, p + 1 * nz, L_.n2, nz, T2b_.as<double>());
+  fill(ctx, R1b_.as<double>(), L_.n1 * nz, 0.0);                  // :37-38
+  fill(ctx, R2b_.as<double>(), L_.n2 * nz, 0.0);
   ResidualArgs a;
   a.I = &in_;
   a.o = &o_;
-  a.nz = nz_;
+  a.nz = nz;
   a.slice = slice_;
   a.init_doubles = sys_[0]->has_initial_doubles();
-  a.T1 = ten(T1b_.as<double>(), {Nv, No, nz_});
-  a.T2 = ten(T2b_.as<double>(), {Nv, Nv, No, No, nz_});
-  a.R1 = ten(R1b_.as<double>(), {Nv, No, nz_});
-  a.R2 = ten(R2b_.as<double>(), {Nv, Nv, No, No, nz_});
+  if (nz > 1) {
+    a.T1 = ten(T1b_.as<double>(), {Nv, No, nz});
+    a.T2 = ten(T2b_.as<double>(), {Nv, Nv, No, No, nz});
+    a.R1 = ten(R1b_.as<double>(), {Nv, No, nz});
+    a.R2 = ten(R2b_.as<double>(), {Nv, Nv, No, No, nz});
+  } else {
+    // one system left: the plain program, on the stacked inputs without
+    // their system index
+    a.T1 = ten(T1b_.as<double>(), {Nv, No});
+    a.T2 = ten(T2b_.as<double>(), {Nv, Nv, No, No});
+    a.R1 = ten(R1b_.as<double>(), {Nv, No});
+    a.R2 = ten(R2b_.as<double>(), {Nv, Nv, No, No});
+  }
   residual_program(ctx, a, it_);
-  batch_scatter(ctx, R1b_.as<double>(), L_.n1, nz_, p + 2 * nz_);
-  batch_scatter(ctx, R2b_.as<double>(), L_.n2, nz_, p + 3 * nz_);
-  for (int64_t z = 0; z < nz_; ++z)
-    if ((mask >> z) & 1) sys_[z]->mix_body();
+  batch_scatter(ctx, R1b_.as<double>(), L_.n1, nz, p + 2 * nz);
+  batch_scatter(ctx, R2b_.as<double>(), L_.n2, nz, p + 3 * nz);
+  for (int z : run_) sys_[z]->mix_body();
 }
 
 void BatchCcsd::run(int n) {
@@ -149,7 +187,9 @@ void BatchCcsd::run(int n) {
       if (active_[z]) mask |= 1ull << z;
     }
     if (!mask) break;
-    if (mask != ptr_mask_) upload_pointers(mask);
+    uint64_t cur = 0;
+    for (int z : run_) cur |= 1ull << z;
+    if (mask != cur) compact(mask);
     // the running systems have iterated together, so their DIIS rings are
     // in the same state and their graph keys agree
     int key = -2;
@@ -166,7 +206,7 @@ void BatchCcsd::run(int n) {
         const double f0 = ctx.flops;
         GBCC_CUDA(cudaStreamBeginCapture(ctx.stream, cudaStreamCaptureModeThreadLocal));
         try {
-          body(mask);
+          body();
         } catch (...) {
           cudaGraph_t bad = nullptr;
           cudaStreamEndCapture(ctx.stream, &bad);
@@ -187,7 +227,7 @@ void BatchCcsd::run(int n) {
       ctx.launches += g.launches;
       ctx.flops += g.flops;
     } else {
-      body(mask);
+      body();
     }
     ++it_;
     for (int64_t z = 0; z < nz_; ++z) {

@@ -19,8 +19,10 @@ namespace gbcc {
 // (ClusterSinglesDoublesAlgorithm.cxx:89-113 for each).  A system that
 // converges or fails is frozen at that iteration while the others go on, so
 // its result is the one it reaches alone, up to the rounding of the batched
-// products.  Steady-state iterations replay captured CUDA graphs, one per
-// DIIS ring position and set of running systems.
+// products; the stacked inputs then shrink to the systems still running, so
+// that a stopped system costs nothing.  Steady-state iterations replay
+// captured CUDA graphs, one per DIIS ring position and set of running
+// systems.
 class BatchCcsd {
  public:
   BatchCcsd(Context &ctx, std::vector<std::unique_ptr<Ccsd>> systems);
@@ -47,17 +49,17 @@ class BatchCcsd {
   int it_ = 0;
   CcsdInputs in_;              // residual inputs with the trailing system index
   DBuf T1b_, T2b_, R1b_, R2b_;
-  DBuf ptrs_;                  // device pointers: T1, T2, R1, R2 of each system
-  DBuf zeros_;                 // amplitudes fed for systems that stopped
-  uint64_t ptr_mask_ = 0;      // running systems the pointers were set for
-  void upload_pointers(uint64_t mask);
+  DBuf ptrs_;                  // device pointers: T1, T2, R1, R2 of each running system
+  std::vector<int> run_;       // the running systems, in stacked order
+  void upload_pointers();
+  void compact(uint64_t mask);
   struct Graph {
     cudaGraphExec_t exec = nullptr;
     uint64_t launches = 0;
     double flops = 0;
   };
   std::map<std::pair<int, uint64_t>, Graph> graphs_;
-  void body(uint64_t mask);
+  void body();
 };
 
 }  // namespace gbcc

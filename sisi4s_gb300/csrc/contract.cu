@@ -46,12 +46,16 @@ int64_t prod(const std::string &s, const int64_t *len) {
 // kept in the context; the other operand is permuted and split as usual.
 // The digits are those the plain route would produce, so the result is the
 // same bit for bit.
+// With a batch index z (nz entries, the last index of A, B and C; sa, sb,
+// sc the index strings without it) every operand is a family of nz panels
+// and the product one batched launch.
 void contract_cached(Context &ctx, double alpha, const Ten &A, const std::string &sa,
                      const Ten &B, const std::string &sb, double beta, const Ten &C,
                      const std::string &sc, const std::string &m, const std::string &n,
                      const std::string &k, bool permA, bool ta, bool permB, bool tb,
-                     bool permC, bool swap, const int64_t *len) {
+                     bool permC, bool swap, const int64_t *len, char z, int64_t nz) {
   const int64_t sM = prod(m, len), sN = prod(n, len), sK = prod(k, len);
+  const std::string zs = z ? std::string(1, z) : std::string();
   // panels of one operand: tensor T (index string st), GEMM order `order`
   // (permuted into it when perm), matrix with `rows` rows, element (r, q) at
   // r*rs + q*ks of the GEMM-ready buffer
@@ -65,7 +69,7 @@ void contract_cached(Context &ctx, double alpha, const Ten &A, const std::string
       std::snprintf(buf, sizeof buf, "%p", (const void *)T.p);
       key = std::string(buf) + "|" + st + ">" + order + "|" + (role_a ? "A" : "B") + "|" +
             std::to_string(rows) + "|" + std::to_string(rs) + "|" + std::to_string(ks) +
-            "|" + std::to_string(ctx.emu_slices);
+            "|" + std::to_string(ctx.emu_slices) + "|" + std::to_string(nz);
       auto it = ctx.panel_cache.find(key);
       if (it != ctx.panel_cache.end()) return it->second.panels;
     }
@@ -75,12 +79,13 @@ void contract_cached(Context &ctx, double alpha, const Ten &A, const std::string
       tmp = OTen(ctx, {T.size()});
       Ten t = T;
       t.p = tmp.p();
-      for (size_t d = 0; d < order.size(); ++d) t.lens[d] = len[(unsigned char)order[d]];
-      assign(ctx, 1.0, T, st.c_str(), 0.0, t, order.c_str());
+      const std::string oz = order + zs;
+      for (size_t d = 0; d < oz.size(); ++d) t.lens[d] = len[(unsigned char)oz[d]];
+      assign(ctx, 1.0, T, (st + zs).c_str(), 0.0, t, oz.c_str());
       base = t.p;
     }
     auto P = std::make_shared<EmuPanels>(
-        emu_split(ctx, role_a, base, rows, sK, rs, ks, 1, 0));
+        emu_split(ctx, role_a, base, rows, sK, rs, ks, (int)nz, rows * sK));
     if (constant) {
       cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
       const size_t bytes = P->panels.bytes() + P->exps.bytes();
@@ -114,14 +119,20 @@ void contract_cached(Context &ctx, double alpha, const Ten &A, const std::string
     pc = tc.p();
     gbeta = 0.0;
   }
-  if (!swap) emu_gemm_panels(ctx, *PA, 0, *PB, 0, alpha, gbeta, pc, sM);
-  else emu_gemm_panels(ctx, *PB, 0, *PA, 0, alpha, gbeta, pc, sN);
+  if (nz > 1) {
+    if (!swap) emu_gemm_panels_batched(ctx, *PA, *PB, (int)nz, alpha, gbeta, pc, sM, sM * sN);
+    else emu_gemm_panels_batched(ctx, *PB, *PA, (int)nz, alpha, gbeta, pc, sN, sM * sN);
+  } else if (!swap) {
+    emu_gemm_panels(ctx, *PA, 0, *PB, 0, alpha, gbeta, pc, sM);
+  } else {
+    emu_gemm_panels(ctx, *PB, 0, *PA, 0, alpha, gbeta, pc, sN);
+  }
   if (permC) {
     Ten t = C;
     t.p = pc;
-    const std::string o = m + n;
+    const std::string o = m + n + zs;
     for (size_t d = 0; d < o.size(); ++d) t.lens[d] = len[(unsigned char)o[d]];
-    assign(ctx, 1.0, t, o.c_str(), beta, C, sc.c_str());
+    assign(ctx, 1.0, t, o.c_str(), beta, C, (sc + zs).c_str());
   }
 }
 
@@ -218,12 +229,13 @@ void contract(Context &ctx, double alpha, const Ten &A, const char *ia,
         if (p.cost < best.cost) best = p;
       }
   const Plan &p = best;
-  if (!z && ctx.use_panel_cache && precision == GBCC_PREC_EMU && sK > 0 && sM > 1 && sN > 1 &&
+  if (ctx.use_panel_cache && precision == GBCC_PREC_EMU && sK > 0 && sM > 1 && sN > 1 &&
       2.0 * (double)sM * (double)sN * (double)sK >= ctx.emu_min_flops &&
+      nz < (1 << 20) &&
       (ctx.is_constant(A.p, sizeof(double) * A.size()) ||
        ctx.is_constant(B.p, sizeof(double) * B.size()))) {
     contract_cached(ctx, alpha, A, sa, B, sb, beta, C, sc, p.m, p.n, p.k, p.permA, p.ta,
-                    p.permB, p.tb, p.permC, p.swap, len);
+                    p.permB, p.tb, p.permC, p.swap, len, z, nz);
     return;
   }
   // operand A as a [M,K] (ta=0) or [K,M] (ta=1) matrix

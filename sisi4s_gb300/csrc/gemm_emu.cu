@@ -1304,6 +1304,14 @@ void emu_gemm_panels_batched(Context &ctx, const EmuPanels &A, const EmuPanels &
                              double alpha, double beta, double *C, int64_t ldc, int64_t sC) {
   require(nprob >= 1, "batched GEMM: no problems");
   require(A.role_a && !B.role_a && A.K == B.K && A.S == B.S, "batched GEMM: operand mismatch");
+  // a few-tile product with long K keeps its K-split, problem by problem,
+  // unless the batch alone fills the GPU with tiles
+  const EmuPlan P1 = emu_plan(A.S, A.rows, B.rows, A.K, ctx.sm_count, true, ctx.emu_max_ksplit);
+  if (P1.ksplit > 1 && (int64_t)P1.mt * P1.nt * nprob < ctx.sm_count) {
+    for (int q = 0; q < nprob; ++q)
+      emu_gemm_panels(ctx, A, q, B, q, alpha, beta, C + (int64_t)q * sC, ldc);
+    return;
+  }
   double *const Cs[1] = {C};
   switch (A.S) {
     case 4: gemm_panels_grouped<4>(ctx, A, nullptr, B, nullptr, nprob, alpha, beta, Cs, nullptr, ldc, sC); break;
@@ -1367,37 +1375,15 @@ void ladder_row_exponents(Context &ctx, const void *amax, int64_t x0, int64_t nx
 }
 
 namespace {
+// The panel-output launch from operand panels (A rows M = A.rows, B rows
+// N = B.rows, K): V = A B^T written as the digits of P (see EmuArgs).
 template <int S>
-void run_emu_to_panels(Context &ctx, int64_t M, int64_t N, int64_t K, const double *A,
-                       int64_t lda, const double *B, int64_t ldb, unsigned px, unsigned pd,
-                       EmuPanels &P) {
+void launch_to_panels(Context &ctx, const __nv_bfloat16 *Ap, const int *ea,
+                      const __nv_bfloat16 *Bp, const int *eb, int64_t M, int64_t N, int64_t K,
+                      unsigned px, unsigned pd, EmuPanels &P) {
   const EmuPlan pl = emu_plan(S, M, N, K, ctx.sm_count, false);
   const int mt = pl.mt, nt = pl.nt, kt = pl.kt;
   require((int64_t)mt * nt < (1LL << 31), "emu gemm: grid too large");
-  // op(A)(m, k) = A[k + m lda], op(B)^T(n, k) = B[k + n ldb]
-  DBuf ea(ctx, sizeof(int) * M), eb(ctx, sizeof(int) * N);
-  DBuf asl(ctx, (size_t)S * mt * kt * A_TILE), bsl(ctx, (size_t)S * nt * kt * B_TILE);
-  auto exponents = [&](const double *p, int64_t R, int64_t rs, int *e) {
-    GBCC_CUDA(cudaMemsetAsync(e, 0x80, sizeof(int) * R, ctx.stream));
-    const int64_t kchunk = std::max<int64_t>(1024, (K + 4095) / 4096);
-    const dim3 grid((unsigned)((R + 7) / 8), (unsigned)((K + kchunk - 1) / kchunk));
-    exponent_rows_warp_kernel<<<grid, 256, 0, ctx.stream>>>(p, R, K, rs, 1, kchunk, e);
-    GBCC_CHECK_LAUNCH(ctx);
-  };
-  exponents(A, M, lda, ea.as<int>());
-  exponents(B, N, ldb, eb.as<int>());
-  auto grid_for = [&](int64_t segs) {
-    require(segs < (1LL << 31), "emulated GEMM: operand too large to split");
-    int64_t g = (segs + 255) / 256;
-    const int64_t cap = (int64_t)std::max(ctx.sm_count, 1) * 16;
-    return (unsigned)std::max<int64_t>(1, std::min(g, cap));
-  };
-  split_kernel<S, TM><<<grid_for((int64_t)mt * TM * kt * 4), 256, 0, ctx.stream>>>(
-      A, M, K, lda, 1, ea.as<int>(), mt, kt, asl.as<__nv_bfloat16>());
-  GBCC_CHECK_LAUNCH(ctx);
-  split_kernel<S, TN><<<grid_for((int64_t)nt * TN * kt * 4), 256, 0, ctx.stream>>>(
-      B, N, K, ldb, 1, eb.as<int>(), nt, kt, bsl.as<__nv_bfloat16>());
-  GBCC_CHECK_LAUNCH(ctx);
   // rows past R are never written: give them the digits of zero
   if (P.rows % TM != 0) {
     const int64_t pad = (int64_t)P.rt * TM - P.rows;
@@ -1415,10 +1401,10 @@ void run_emu_to_panels(Context &ctx, int64_t M, int64_t N, int64_t K, const doub
   GBCC_CUDA(cudaFuncSetAttribute(emu_gemm_kernel<S, false>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
   EmuArgs args{};
-  args.A = asl.as<__nv_bfloat16>();
-  args.B = bsl.as<__nv_bfloat16>();
-  args.ea = ea.as<int>();
-  args.eb = eb.as<int>();
+  args.A = Ap;
+  args.B = Bp;
+  args.ea = ea;
+  args.eb = eb;
   args.M = M; args.N = N; args.ldc = 0;
   args.mt = mt; args.nt = nt; args.kt = kt;
   args.kc_blocks = pl.kc_blocks;
@@ -1451,22 +1437,34 @@ void run_emu_to_panels(Context &ctx, int64_t M, int64_t N, int64_t K, const doub
     ctx.prof_recs.push_back({ev0, ev1, f * S * (S + 1) / 2.0, f, M, N, K});
   }
 }
+
 }  // namespace
 
-void gemm_emu_to_panels(Context &ctx, int64_t M, int64_t N, int64_t K, const double *A,
-                        int64_t lda, const double *B, int64_t ldb, int64_t px, int64_t pd,
-                        EmuPanels &P) {
-  require(P.role_a && P.count == 1 && P.S == ctx.emu_slices, "gemm_emu_to_panels: panels");
+void emu_gemm_panels_to_panels(Context &ctx, const EmuPanels &A, int ia, const EmuPanels &B,
+                               int ib, int64_t px, int64_t pd, EmuPanels &P) {
+  const int64_t M = A.rows, N = B.rows, K = A.K;
+  require(A.role_a && !B.role_a && A.K == B.K && A.S == B.S && A.S == P.S,
+          "emu_gemm_panels_to_panels: operand mismatch");
+  require(ia >= 0 && ia < A.count && ib >= 0 && ib < B.count,
+          "emu_gemm_panels_to_panels: index");
+  require(P.role_a && P.count == 1, "emu_gemm_panels_to_panels: panels");
   require(px > 0 && pd > 0 && pd % 8 == 0 && M % px == 0 && N % pd == 0,
-          "gemm_emu_to_panels: shape");
-  require(P.rows == px * (N / pd) && P.K == pd * (M / px), "gemm_emu_to_panels: panel shape");
-  require(M < (1LL << 31) && N < (1LL << 31), "gemm_emu_to_panels: size");
-  switch (ctx.emu_slices) {
-    case 4: run_emu_to_panels<4>(ctx, M, N, K, A, lda, B, ldb, (unsigned)px, (unsigned)pd, P); break;
-    case 5: run_emu_to_panels<5>(ctx, M, N, K, A, lda, B, ldb, (unsigned)px, (unsigned)pd, P); break;
-    case 6: run_emu_to_panels<6>(ctx, M, N, K, A, lda, B, ldb, (unsigned)px, (unsigned)pd, P); break;
-    case 7: run_emu_to_panels<7>(ctx, M, N, K, A, lda, B, ldb, (unsigned)px, (unsigned)pd, P); break;
-    case 8: run_emu_to_panels<8>(ctx, M, N, K, A, lda, B, ldb, (unsigned)px, (unsigned)pd, P); break;
+          "emu_gemm_panels_to_panels: shape");
+  require(P.rows == px * (N / pd) && P.K == pd * (M / px),
+          "emu_gemm_panels_to_panels: panel shape");
+  require(M < (1LL << 31) && N < (1LL << 31), "emu_gemm_panels_to_panels: size");
+  const int64_t aplane = (int64_t)A.rt * A.kt * TM * KB;
+  const int64_t bplane = (int64_t)B.rt * B.kt * TN * KB;
+  const __nv_bfloat16 *Ap = A.panels.as<__nv_bfloat16>() + (int64_t)ia * A.S * aplane;
+  const __nv_bfloat16 *Bp = B.panels.as<__nv_bfloat16>() + (int64_t)ib * B.S * bplane;
+  const int *ea = A.exps.as<int>() + (int64_t)ia * M;
+  const int *eb = B.exps.as<int>() + (int64_t)ib * N;
+  switch (A.S) {
+    case 4: launch_to_panels<4>(ctx, Ap, ea, Bp, eb, M, N, K, (unsigned)px, (unsigned)pd, P); break;
+    case 5: launch_to_panels<5>(ctx, Ap, ea, Bp, eb, M, N, K, (unsigned)px, (unsigned)pd, P); break;
+    case 6: launch_to_panels<6>(ctx, Ap, ea, Bp, eb, M, N, K, (unsigned)px, (unsigned)pd, P); break;
+    case 7: launch_to_panels<7>(ctx, Ap, ea, Bp, eb, M, N, K, (unsigned)px, (unsigned)pd, P); break;
+    case 8: launch_to_panels<8>(ctx, Ap, ea, Bp, eb, M, N, K, (unsigned)px, (unsigned)pd, P); break;
     default: throw Error(GBCC_BAD_ARG, "emu_slices must be in [4, 8]");
   }
   ctx.flops += 2.0 * (double)M * (double)N * (double)K;
@@ -1537,13 +1535,10 @@ void gemm_emu(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
               double alpha, const double *A, int64_t lda, const double *B,
               int64_t ldb, double beta, double *C, int64_t ldc, int64_t batch,
               int64_t sA, int64_t sB, int64_t sC) {
-  const EmuPlan P1 = emu_plan(ctx.emu_slices, M, N, K, ctx.sm_count, true, ctx.emu_max_ksplit);
-  if (batch > 1 && batch < (1 << 20) &&
-      (P1.ksplit == 1 || (int64_t)P1.mt * P1.nt * batch >= ctx.sm_count)) {
+  if (batch > 1 && batch < (1 << 20)) {
     // a batch of same-shape products: the operands of all entries are split
     // into one panel family each, and one grouped launch walks the tiles of
-    // every entry.  (A few-tile product with long K keeps its K-split
-    // instead, entry by entry, unless the batch alone fills the GPU.)
+    // every entry
     const int64_t ars = ta ? lda : 1, aks = ta ? 1 : lda;
     const int64_t brs = tb ? 1 : ldb, bks = tb ? ldb : 1;
     EmuPanels PA = emu_split(ctx, true, A, M, K, ars, aks, (int)batch, sA);

@@ -340,16 +340,16 @@ void emu_gemm_panels_grouped(Context &ctx, const EmuPanels &A, const int *ia,
 void emu_gemm_panels_batched(Context &ctx, const EmuPanels &A, const EmuPanels &B, int nprob,
                              double alpha, double beta, double *C, int64_t ldc, int64_t sC);
 // Panels of one operand, allocated but not filled (their digits and row
-// exponents are written by a producer such as gemm_emu_to_panels).
+// exponents are written by a producer such as emu_gemm_panels_to_panels).
 EmuPanels emu_panels_alloc(Context &ctx, bool role_a, int64_t R, int64_t K);
-// The particle ladder's V[(x,c),(d,y)] = sum_G A[G,(x,c)] B[G,(d,y)]
-// (operand rows K-major: A[k + m lda], B[k + n ldb]; m = x + px c,
-// n = d + pd y) written straight into the digit panels P of the next
-// product's A operand: rows x + px y, K index d + pd c, with P's row
-// exponents set beforehand (ladder_row_exponents).  pd % 8 == 0.
-void gemm_emu_to_panels(Context &ctx, int64_t M, int64_t N, int64_t K, const double *A,
-                        int64_t lda, const double *B, int64_t ldb, int64_t px, int64_t pd,
-                        EmuPanels &P);
+// The particle ladder's V[(x,c),(d,y)] = sum_G A[G,(x,c)] B[G,(d,y)], from
+// the operands' digit panels (A_ia rows m = x + px c, B_ib rows n = d + pd y,
+// K = G), written straight into the digit panels P of the next product's A
+// operand: rows x + px y, K index d + pd c, with P's row exponents set
+// beforehand (ladder_row_exponents).  pd % 8 == 0.  Operands shared by
+// several products are split once.
+void emu_gemm_panels_to_panels(Context &ctx, const EmuPanels &A, int ia, const EmuPanels &B,
+                               int ib, int64_t px, int64_t pd, EmuPanels &P);
 // amax[a] = max_c ||dG[., a, c]|| (dG [G, Nv, Nv]); amax holds Nv 64-bit words
 void ladder_amax(Context &ctx, const double *dG, int64_t G, int64_t Nv, void *amax);
 // er[x + nx y]: exponent bound of V[x0 + x, y0 + y, ., .] from amax (Cauchy-Schwarz)

@@ -9,6 +9,10 @@
 // integrals, amplitudes and DIIS history resident from admission to result.
 // Every kernel is deterministic (fixed reduction orders, no floating-point
 // atomics), so a request gives bit-identical energies alone and in a mix.
+// A slot that admits a request also takes queued requests of the same shape,
+// options and (T) flag (up to max_batch in all) and solves them in lockstep,
+// one batched product per contraction for all of them; their energies then
+// agree with the solve alone up to the rounding of the batched products.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -77,6 +81,53 @@ size_t estimate_bytes(const gbcc_ccsd_in &in, const gbcc_ccsd_opts &o, int tripl
   return (size_t)(1.5 * bytes) + (64u << 20);
 }
 
+// what a request adds in a lockstep batch: its copy in the stacked residual
+// inputs (vertex blocks and integrals), with the same margins
+size_t batch_extra_bytes(const gbcc_ccsd_in &in, const gbcc_ccsd_opts &o) {
+  const double No = in.No, Nv = in.Nv, NG = in.NG;
+  const double n2 = Nv * Nv * No * No;
+  double bytes = 8.0 * (NG * (Nv * No + Nv * Nv + No * No) + 3.0 * n2 +
+                        No * No * No * No + No * No * No * Nv);
+  if (o.precision == GBCC_PREC_EMU) bytes *= 2.4;
+  return (size_t)(1.5 * bytes);
+}
+
+bool same_opts(const gbcc_ccsd_opts &a, const gbcc_ccsd_opts &b) {
+  return a.mixer == b.mixer && a.max_residua == b.max_residua &&
+         a.mixing_ratio == b.mixing_ratio && a.max_iterations == b.max_iterations &&
+         a.energy_convergence == b.energy_convergence &&
+         a.amplitudes_convergence == b.amplitudes_convergence &&
+         a.level_shift == b.level_shift && a.distinguishable == b.distinguishable &&
+         a.ppl == b.ppl && a.integrals_slice_size == b.integrals_slice_size &&
+         a.integrals_slice_factor == b.integrals_slice_factor && a.precision == b.precision &&
+         a.emu_slices == b.emu_slices && a.formulation == b.formulation &&
+         a.only_ppl == b.only_ppl && a.emu_min_flops == b.emu_min_flops &&
+         a.f64_split_blocks == b.f64_split_blocks && a.emu_max_ksplit == b.emu_max_ksplit;
+}
+
+// Lockstep batches pay where one system's kernels leave most of the GPU
+// idle.  The proxy is the particle ladder's V block, the largest product of
+// an iteration: a batch is formed when one system's block (at the default
+// integralsSliceSize of a batch) covers less than half the SMs with output
+// tiles.  Above that, requests on their own streams run faster side by side
+// (measured: No=8, Nv=64 and No=10, Nv=96 served faster unbatched, No=6,
+// Nv=40 faster in lockstep).
+bool lockstep_pays(const gbcc_ccsd_in &in, const gbcc_ccsd_opts &o, int sm_count) {
+  const int64_t Nv = in.Nv;
+  int64_t s = o.integrals_slice_size > 0 ? o.integrals_slice_size
+                                         : std::max<int64_t>(16, Nv / 8);
+  s = std::min<int64_t>(s, Nv);
+  const int64_t vtiles = ((s * Nv + 127) / 128) * ((s * Nv + 63) / 64);
+  return 2 * vtiles < sm_count;
+}
+
+// requests that can share a lockstep batch (DiisMixer, vertex formulation)
+bool batchable(const Request &a, const Request &b) {
+  return a.in.No == b.in.No && a.in.Nv == b.in.Nv && a.in.NG == b.in.NG &&
+         a.triples == b.triples && same_opts(a.opts, b.opts) && a.opts.mixer == 1 &&
+         a.opts.formulation == 0 && a.opts.max_iterations >= 1;
+}
+
 }  // namespace
 
 struct gbcc_server {
@@ -90,19 +141,66 @@ struct gbcc_server {
   bool stop = false;
   int64_t next_id = 1;
   int running = 0;
+  int busy = 0;  // slots solving a request or a batch
+  int max_batch = 8;
+  int sm_count = 152;
 
   void worker_main(int w);
   void run_one(gbcc_ctx *ctx, Request &r);
+  void run_batch(gbcc_ctx *ctx, const std::vector<Request *> &g);
 };
+
+// every request starts from the library's execution defaults; its own
+// options (e.g. a tuned configuration of its shape) are applied at setup
+static gbcc_status reset_ctx(gbcc_ctx *ctx, int64_t Nv) {
+  gbcc_status st = gbcc_ctx_set_emulation(ctx, 6, 1e7);
+  if (st == GBCC_OK) st = gbcc_ctx_set_splits(ctx, 3, 64);
+  if (st == GBCC_OK) st = gbcc_ctx_set_triples_batch(ctx, served_triples_images(Nv));
+  return st;
+}
+
+void gbcc_server::run_batch(gbcc_ctx *ctx, const std::vector<Request *> &g) {
+  const int n = (int)g.size();
+  const double t0 = now_s();
+  for (Request *r : g) r->res.t_start = t0;
+  const Request &r0 = *g[0];
+  gbcc_status st = reset_ctx(ctx, r0.in.Nv);
+  std::vector<gbcc_ccsd_in> ins;
+  for (Request *r : g) ins.push_back(r->in);
+  gbcc_batch *b = nullptr;
+  if (st == GBCC_OK) st = gbcc_ccsd_batch_setup(ctx, n, ins.data(), &r0.opts, &b);
+  std::vector<gbcc_status> sst((size_t)n, st);
+  if (st == GBCC_OK) st = gbcc_ccsd_batch_step(b, r0.opts.max_iterations, sst.data());
+  for (int z = 0; z < n; ++z) {
+    Request &r = *g[z];
+    gbcc_status s = st != GBCC_OK ? st : sst[z];
+    if (st == GBCC_OK) {
+      gbcc_ccsd_out out{};
+      const gbcc_status s2 = gbcc_ccsd_batch_result(b, z, &out);
+      r.res.e_ccsd = out.energy;
+      r.res.iterations = out.iterations;
+      r.res.converged = out.converged;
+      r.res.e_total = out.energy;
+      if (s2 != GBCC_OK) s = s2;
+      // as for a request alone: (T) also on amplitudes that did not converge
+      if ((s == GBCC_OK || s == GBCC_NOT_CONVERGED) && r.triples) {
+        double et = 0, etot = 0;
+        const gbcc_status s3 = gbcc_ccsd_batch_triples(b, z, r.opts.precision, &etot, &et);
+        r.res.e_t = et;
+        r.res.e_total = etot;
+        if (s3 != GBCC_OK) s = s3;
+      }
+    }
+    r.res.status = s;
+    r.res.t_done = now_s();
+  }
+  if (b) gbcc_ccsd_batch_destroy(b);
+}
 
 void gbcc_server::run_one(gbcc_ctx *ctx, Request &r) {
   gbcc_solver *s = nullptr;
   r.res.t_start = now_s();
-  // every request starts from the library's execution defaults; its own
-  // options (e.g. a tuned configuration of its shape) are applied at setup
-  gbcc_status st = gbcc_ctx_set_emulation(ctx, 6, 1e7);
-  if (st == GBCC_OK) st = gbcc_ctx_set_splits(ctx, 3, 64);
-  if (st == GBCC_OK) st = gbcc_ctx_set_triples_batch(ctx, served_triples_images(r.in.Nv));
+  gbcc_status st = reset_ctx(ctx, r.in.Nv);
   if (st == GBCC_OK) st = gbcc_ccsd_setup(ctx, &r.in, &r.opts, &s);
   if (st == GBCC_OK) {
     double e = 0;
@@ -134,7 +232,8 @@ void gbcc_server::worker_main(int w) {
   cudaSetDevice(device);
   const gbcc_status cst = gbcc_ctx_create(device, nullptr, &ctx);
   for (;;) {
-    Request *r = nullptr;
+    std::vector<Request *> g;
+    size_t bytes = 0;
     {
       std::unique_lock<std::mutex> lk(mu);
       cv_work.wait(lk, [&] {
@@ -143,23 +242,54 @@ void gbcc_server::worker_main(int w) {
       });
       if (stop && pending.empty()) break;
       if (pending.empty()) continue;
-      r = pending.front();
+      Request *r = pending.front();
       pending.pop_front();
-      in_use += r->bytes;
-      ++running;
-      r->res.t_admit = now_s();
+      g.push_back(r);
+      bytes = r->bytes;
+      // queued requests of the same shape join it, while the budget allows;
+      // the queued requests of the shape are shared out over the idle slots
+      // (a batch of ceil(m / idle)), so that no slot is left without work
+      if (max_batch > 1 && batchable(*r, *r) && lockstep_pays(r->in, r->opts, sm_count)) {
+        int m = 1;
+        for (Request *q : pending) m += batchable(*r, *q) ? 1 : 0;
+        const int idle = std::max(1, (int)workers.size() - busy);
+        const int take = std::min(max_batch, (m + idle - 1) / idle);
+        const size_t first_extra = batch_extra_bytes(r->in, r->opts);
+        for (auto it = pending.begin(); it != pending.end() && (int)g.size() < take;) {
+          Request *q = *it;
+          const size_t add = q->bytes + batch_extra_bytes(q->in, q->opts) +
+                             (g.size() == 1 ? first_extra : 0);
+          if (batchable(*r, *q) && in_use + bytes + add <= budget) {
+            g.push_back(q);
+            bytes += add;
+            it = pending.erase(it);
+          } else {
+            ++it;
+          }
+        }
+      }
+      in_use += bytes;
+      running += (int)g.size();
+      ++busy;
+      const double t = now_s();
+      for (Request *q : g) q->res.t_admit = t;
     }
-    if (cst == GBCC_OK) {
-      run_one(ctx, *r);
+    if (cst != GBCC_OK) {
+      for (Request *q : g) {
+        q->res.status = cst;
+        q->res.t_done = now_s();
+      }
+    } else if (g.size() == 1) {
+      run_one(ctx, *g[0]);
     } else {
-      r->res.status = cst;
-      r->res.t_done = now_s();
+      run_batch(ctx, g);
     }
     {
       std::lock_guard<std::mutex> lk(mu);
-      in_use -= r->bytes;
-      --running;
-      r->done = true;
+      in_use -= bytes;
+      running -= (int)g.size();
+      --busy;
+      for (Request *q : g) q->done = true;
     }
     cv_work.notify_all();
     cv_done.notify_all();
@@ -174,6 +304,7 @@ void gbcc_server_opts_default(gbcc_server_opts *o) {
   o->device = 0;
   o->slots = 8;
   o->hbm_budget_bytes = 0;  // 0: 80 % of the free device memory at creation
+  o->max_batch = 8;
 }
 
 gbcc_status gbcc_server_create(const gbcc_server_opts *opts, gbcc_server **out) {
@@ -181,7 +312,7 @@ gbcc_status gbcc_server_create(const gbcc_server_opts *opts, gbcc_server **out) 
   *out = nullptr;
   gbcc_server_opts o;
   if (opts) o = *opts; else gbcc_server_opts_default(&o);
-  if (o.slots < 1 || o.slots > 64) return GBCC_BAD_ARG;
+  if (o.slots < 1 || o.slots > 64 || o.max_batch < 0 || o.max_batch > 64) return GBCC_BAD_ARG;
   int n = 0;
   if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
     cudaGetLastError();
@@ -190,6 +321,13 @@ gbcc_status gbcc_server_create(const gbcc_server_opts *opts, gbcc_server **out) 
   if (o.device < 0 || o.device >= n) return GBCC_BAD_ARG;
   auto *s = new gbcc_server();
   s->device = o.device;
+  s->max_batch = std::max(1, o.max_batch);
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, o.device) == cudaSuccess &&
+      sms > 0)
+    s->sm_count = sms;
+  else
+    cudaGetLastError();
   if (o.hbm_budget_bytes > 0) {
     s->budget = (size_t)o.hbm_budget_bytes;
   } else {

@@ -21,7 +21,7 @@ __all__ = ["Server", "request_shape", "make_requests", "run_stream",
 
 class ServerOpts(C.Structure):
     _fields_ = [("device", C.c_int), ("slots", C.c_int),
-                ("hbm_budget_bytes", C.c_int64)]
+                ("hbm_budget_bytes", C.c_int64), ("max_batch", C.c_int)]
 
 
 class Result(C.Structure):
@@ -61,11 +61,16 @@ def _result_dict(r):
 
 
 class Server:
-    def __init__(self, slots=8, budget_bytes=0, device=0):
+    def __init__(self, slots=8, budget_bytes=0, device=0, max_batch=None):
+        """``max_batch``: most queued requests of one shape that a slot
+        solves together in lockstep (None: the library default, 8; 1: every
+        request on its own)."""
         self.lib = _lib()
         o = ServerOpts()
         self.lib.gbcc_server_opts_default(C.byref(o))
         o.device, o.slots, o.hbm_budget_bytes = device, slots, int(budget_bytes)
+        if max_batch is not None:
+            o.max_batch = int(max_batch)
         h = C.c_void_p()
         st = self.lib.gbcc_server_create(C.byref(o), C.byref(h))
         if st != capi.OK:

@@ -181,6 +181,13 @@ void emu_gemm_panels(Context &ctx, const EmuPanels &A, int ia, const EmuPanels &
   });
 }
 
+void emu_gemm_panels_batched(Context &ctx, const EmuPanels &A, const EmuPanels &B, int nprob,
+                             double alpha, double beta, double *C, int64_t ldc, int64_t sC) {
+  require(nprob >= 1 && nprob <= A.count && nprob <= B.count, "batched GEMM: operand count");
+  for (int q = 0; q < nprob; ++q)
+    emu_gemm_panels(ctx, A, q, B, q, alpha, beta, C + (int64_t)q * sC, ldc, nullptr);
+}
+
 void gemm_emu_mapped(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
                      double alpha, const double *A, int64_t lda, const double *B, int64_t ldb,
                      double *C, const OutMap &map) {
@@ -216,22 +223,30 @@ EmuPanels emu_panels_alloc(Context &ctx, bool role_a, int64_t R, int64_t K) {
 }
 
 // the V product stored as the next product's operand, panels[k][r] with
-// r = x + px y, k = d + pd c (m = x + px c, n = d + pd y)
-void gemm_emu_to_panels(Context &ctx, int64_t M, int64_t N, int64_t K, const double *A,
-                        int64_t lda, const double *B, int64_t ldb, int64_t px, int64_t pd,
-                        EmuPanels &P) {
-  require(P.role_a && P.count == 1 && P.S == ctx.emu_slices, "gemm_emu_to_panels: panels");
+// r = x + px y, k = d + pd c (m = x + px c, n = d + pd y), from operand
+// panels (panels[p][k][r] as emu_split stores them)
+void emu_gemm_panels_to_panels(Context &ctx, const EmuPanels &A, int ia, const EmuPanels &B,
+                               int ib, int64_t px, int64_t pd, EmuPanels &P) {
+  const int64_t M = A.rows, N = B.rows, K = A.K;
+  require(A.role_a && !B.role_a && A.K == B.K && A.S == B.S && A.S == P.S,
+          "emu_gemm_panels_to_panels: operand mismatch");
+  require(ia >= 0 && ia < A.count && ib >= 0 && ib < B.count,
+          "emu_gemm_panels_to_panels: index");
+  require(P.role_a && P.count == 1, "emu_gemm_panels_to_panels: panels");
   require(px > 0 && pd > 0 && pd % 8 == 0 && M % px == 0 && N % pd == 0,
-          "gemm_emu_to_panels: shape");
-  require(P.rows == px * (N / pd) && P.K == pd * (M / px), "gemm_emu_to_panels: panel shape");
+          "emu_gemm_panels_to_panels: shape");
+  require(P.rows == px * (N / pd) && P.K == pd * (M / px),
+          "emu_gemm_panels_to_panels: panel shape");
   ctx.flops += 2.0 * (double)M * (double)N * (double)K;
+  const double *a = A.panels.as<double>() + M * K * ia;
+  const double *b = B.panels.as<double>() + N * K * ib;
   double *out = P.panels.as<double>();
   const int64_t R = P.rows;
   launch(ctx, [=]() {
     for (int64_t n = 0; n < N; ++n)
       for (int64_t m = 0; m < M; ++m) {
         double acc = 0.0;
-        for (int64_t k = 0; k < K; ++k) acc += A[k + m * lda] * B[k + n * ldb];
+        for (int64_t k = 0; k < K; ++k) acc += a[m + M * k] * b[n + N * k];
         const int64_t x = m % px, c = m / px, d = n % pd, y = n / pd;
         out[(x + px * y) + R * (d + pd * c)] = acc;
       }
