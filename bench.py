@@ -373,7 +373,10 @@ def main():
     ap.add_argument("--impl", default="gbcc", choices=["gbcc", "reference"])
     ap.add_argument("--workload", default="c2", choices=sorted(SYSTEMS),
                     help="c2: No=32 Nv=256 NG=1024 (default); c5: No=24 Nv=360 NG=1440")
-    ap.add_argument("--slices", type=int, default=6)
+    ap.add_argument("--slices", type=int, default=5,
+                    help="bf16 digits per operand in the CCSD iterations (4-8)")
+    ap.add_argument("--triples-slices", type=int, default=0,
+                    help="bf16 digits per operand in (T) (5-8; 0: one more than --slices)")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
@@ -391,6 +394,8 @@ def main():
     ap.add_argument("--no-triples", action="store_true",
                     help="skip the (T) correction on the 12th-iteration amplitudes")
     args = ap.parse_args()
+    if args.triples_slices <= 0:
+        args.triples_slices = min(8, args.slices + 1)
     select_workload(args.workload)
     ws, rank, local, pg = dist_init()
     if args.impl == "reference":
@@ -454,10 +459,13 @@ def main():
             torch.cuda.synchronize()
             t0 = torch.cuda.Event(enable_timing=True)
             t1 = torch.cuda.Event(enable_timing=True)
+            # (T) runs with one digit more than the context's setting
+            ctx.set_emulation(args.triples_slices - 1, 1e7)
             t0.record(stream)
             e_t, _ = sol.triples("emu")
             t1.record(stream)
             torch.cuda.synchronize()
+            ctx.set_emulation(args.slices, 1e7)
             No, Nv, NG = SYSTEM["No"], SYSTEM["Nv"], SYSTEM["NG"]
             f_t = 2.0 * No ** 3 * Nv ** 4 + 2.0 * No ** 4 * Nv ** 3 + 2.0 * NG * No * Nv ** 3
             sec = t0.elapsed_time(t1) / 1e3
@@ -465,7 +473,7 @@ def main():
                        "hole_triples": No * (No + 1) * (No + 2) // 6,
                        "fp64_equiv_tflops": f_t / sec / 1e12,
                        "precision": "emulated fp64 GEMMs (%d bf16 digits), float-float "
-                                    "epilogue" % min(8, args.slices + 1),
+                                    "epilogue" % args.triples_slices,
                        "amplitudes": "after the 12th iteration"}
             if fx is not None and "gpu_fp64" in fx:
                 g = fx["gpu_fp64"]
@@ -613,7 +621,8 @@ def main():
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                 "data": "synthetic",
                 "config": dict(WORKLOAD, parallelism="replicas" if ws > 1 else "single",
-                               precision="emulated fp64, %d bf16 digits" % args.slices,
+                               precision="emulated fp64, %d bf16 digits (%d in (T))"
+                                         % (args.slices, args.triples_slices),
                                l2="inputs larger than L2 (T2, V, Gamma >= 0.5 GB)",
                                timed_segments=walker.segments),
                 "energies": energies, "memory": memory, "fp64": fp64, "e2e": e2e,

@@ -38,6 +38,42 @@ int64_t prod(const std::string &s, const int64_t *len) {
   return p;
 }
 
+// Offsets of the index group g (mixed radix, first index fastest) inside a
+// tensor with index string s, as v s0 or, for two runs of indices whose
+// strides chain, (v % l) s0 + (v / l) s1.  False for three or more runs.
+bool group_offsets(const std::string &s, const std::string &g, const int64_t *len,
+                   int64_t &s0, unsigned &l, int64_t &s1) {
+  int64_t st[256] = {};
+  int64_t acc = 1;
+  for (char c : s) {
+    st[(unsigned char)c] = acc;
+    acc *= len[(unsigned char)c];
+  }
+  int64_t rs[2] = {0, 0}, rl[2] = {1, 1};
+  int n = 0;
+  for (char c : g) {
+    const int64_t sc = st[(unsigned char)c], lc = len[(unsigned char)c];
+    if (lc == 1) continue;  // a length-1 index moves nothing
+    if (n > 0 && rs[n - 1] * rl[n - 1] == sc) {
+      rl[n - 1] *= lc;
+      continue;
+    }
+    if (n == 2) return false;
+    rs[n] = sc;
+    rl[n] = lc;
+    ++n;
+  }
+  s0 = n > 0 ? rs[0] : 0;
+  l = 0;
+  s1 = 0;
+  if (n == 2) {
+    if (rl[0] >= (1LL << 31)) return false;
+    l = (unsigned)rl[0];
+    s1 = rs[1];
+  }
+  return true;
+}
+
 }  // namespace
 
 // The plan of contract() with emulated panels, for a contraction with a
@@ -60,9 +96,27 @@ void contract_cached(Context &ctx, double alpha, const Ten &A, const std::string
   // (permuted into it when perm), matrix with `rows` rows, element (r, q) at
   // r*rs + q*ks of the GEMM-ready buffer
   auto panels = [&](const Ten &T, const std::string &st, bool perm, const std::string &order,
-                    bool role_a, int64_t rows, int64_t rs, int64_t ks)
+                    const std::string &rg, bool role_a, int64_t rows, int64_t rs, int64_t ks)
       -> std::shared_ptr<EmuPanels> {
-    const bool constant = ctx.is_constant(T.p, sizeof(double) * T.size());
+    const bool constant =
+        ctx.use_panel_cache && ctx.is_constant(T.p, sizeof(double) * T.size());
+    if (perm && !constant) {
+      // an operand that changes from call to call is read in place when its
+      // row indices (rg) and K indices each form at most two runs, one of
+      // them contiguous; its digits are those of the permuted copy
+      int64_t r0, r1, k0, k1;
+      unsigned rl, kl;
+      if (group_offsets(st, rg, len, r0, rl, r1) && group_offsets(st, k, len, k0, kl, k1) &&
+          (r0 == 1 || k0 == 1) && rows < (1LL << 31) && sK < (1LL << 31)) {
+        IdxMap mp;
+        mp.rl = rl;
+        mp.rs1 = r1;
+        mp.kl = kl;
+        mp.ks1 = k1;
+        return std::make_shared<EmuPanels>(
+            emu_split(ctx, role_a, T.p, rows, sK, r0, k0, (int)nz, rows * sK, mp));
+      }
+    }
     std::string key;
     if (constant) {
       char buf[64];
@@ -109,8 +163,8 @@ void contract_cached(Context &ctx, double alpha, const Ten &A, const std::string
   const int64_t ldb = tB ? sN : sK;
   // kernel roles: C = A_role (rows M) x B_role (rows N)^T, or the transposed
   // product when the plan computes C^T
-  auto PA = panels(A, sa, permA, oa, !swap, sM, tA ? lda : 1, tA ? 1 : lda);
-  auto PB = panels(B, sb, permB, ob, swap, sN, tB ? 1 : ldb, tB ? ldb : 1);
+  auto PA = panels(A, sa, permA, oa, m, !swap, sM, tA ? lda : 1, tA ? 1 : lda);
+  auto PB = panels(B, sb, permB, ob, n, swap, sN, tB ? 1 : ldb, tB ? ldb : 1);
   double *pc = C.p;
   double gbeta = beta;
   OTen tc;
@@ -229,11 +283,16 @@ void contract(Context &ctx, double alpha, const Ten &A, const char *ia,
         if (p.cost < best.cost) best = p;
       }
   const Plan &p = best;
-  if (ctx.use_panel_cache && precision == GBCC_PREC_EMU && sK > 0 && sM > 1 && sN > 1 &&
-      2.0 * (double)sM * (double)sN * (double)sK >= ctx.emu_min_flops &&
-      nz < (1 << 20) &&
-      (ctx.is_constant(A.p, sizeof(double) * A.size()) ||
-       ctx.is_constant(B.p, sizeof(double) * B.size()))) {
+  // emulated products with a constant operand (its panels cached) or an
+  // operand to reorder (read in place where its indices allow) take the
+  // panel route; its digits and products are those of the plain route
+  const bool emu_product = precision == GBCC_PREC_EMU && sK > 0 && sM > 1 && sN > 1 &&
+                           2.0 * (double)sM * (double)sN * (double)sK >= ctx.emu_min_flops &&
+                           nz < (1 << 20);
+  const bool has_constant = ctx.use_panel_cache &&
+                            (ctx.is_constant(A.p, sizeof(double) * A.size()) ||
+                             ctx.is_constant(B.p, sizeof(double) * B.size()));
+  if (emu_product && (has_constant || p.permA || p.permB)) {
     contract_cached(ctx, alpha, A, sa, B, sb, beta, C, sc, p.m, p.n, p.k, p.permA, p.ta,
                     p.permB, p.tb, p.permC, p.swap, len, z, nz);
     return;

@@ -766,15 +766,27 @@ __device__ __forceinline__ int frexp_exponent(double x) {
 }
 
 // row index contiguous (rs == 1): one thread per row, one K-chunk per blockIdx.y
+// offset of index v along one operand dimension: v s0, or with a second
+// level (l > 0) (v % l) s0 + (v / l) s1 (32-bit division: the host keeps
+// mapped dimensions below 2^31)
+__device__ __forceinline__ int64_t map_off(int64_t v, int64_t s0, unsigned l, int64_t s1) {
+  if (l == 0) return v * s0;
+  const unsigned u = (unsigned)v, q = u / l;
+  return (int64_t)(u - q * l) * s0 + (int64_t)q * s1;
+}
+
+// rows contiguous (rs = 1 at the first level): one thread per row
 __global__ void exponent_rows_contig_kernel(const double *__restrict__ base,
                                             int64_t R, int64_t K, int64_t ks,
-                                            int64_t kchunk, int *__restrict__ e) {
+                                            int64_t kchunk, int *__restrict__ e,
+                                            IdxMap mp) {
   const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= R) return;
   const int64_t k0 = (int64_t)blockIdx.y * kchunk;
   const int64_t k1 = min(K, k0 + kchunk);
+  const double *row = base + map_off(r, 1, mp.rl, mp.rs1);
   int m = INT_MIN;
-  for (int64_t k = k0; k < k1; ++k) m = max(m, frexp_exponent(base[r + k * ks]));
+  for (int64_t k = k0; k < k1; ++k) m = max(m, frexp_exponent(row[map_off(k, ks, mp.kl, mp.ks1)]));
   if (m != INT_MIN) atomicMax(&e[r], m);
 }
 
@@ -782,14 +794,16 @@ __global__ void exponent_rows_contig_kernel(const double *__restrict__ base,
 __global__ void exponent_rows_warp_kernel(const double *__restrict__ base,
                                           int64_t R, int64_t K, int64_t rs,
                                           int64_t ks, int64_t kchunk,
-                                          int *__restrict__ e) {
+                                          int *__restrict__ e, IdxMap mp) {
   const int64_t r = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
   if (r >= R) return;
   const int lane = threadIdx.x % 32;
   const int64_t k0 = (int64_t)blockIdx.y * kchunk;
   const int64_t k1 = min(K, k0 + kchunk);
+  const double *row = base + map_off(r, rs, mp.rl, mp.rs1);
   int m = INT_MIN;
-  for (int64_t k = k0 + lane; k < k1; k += 32) m = max(m, frexp_exponent(base[r * rs + k * ks]));
+  for (int64_t k = k0 + lane; k < k1; k += 32)
+    m = max(m, frexp_exponent(row[map_off(k, ks, mp.kl, mp.ks1)]));
   for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
   if (lane == 0 && m != INT_MIN) atomicMax(&e[r], m);
 }
@@ -819,7 +833,7 @@ template <int S, int TR>
 __global__ void split_kernel(const double *__restrict__ base, int64_t R,
                              int64_t K, int64_t rs, int64_t ks,
                              const int *__restrict__ e, int rt, int kt,
-                             __nv_bfloat16 *__restrict__ out) {
+                             __nv_bfloat16 *__restrict__ out, IdxMap mp) {
   const unsigned rows = (unsigned)rt * TR;
   const unsigned segs = rows * (unsigned)kt * (KB / 8);  // 16-byte segments per digit
   constexpr unsigned tile_elems = TR * KB;
@@ -838,12 +852,13 @@ __global__ void split_kernel(const double *__restrict__ base, int64_t R,
                         ((rr / 8) * (KB / 8) + kk) * 64 + (rr % 8) * 8;
     const int er = (r < R) ? e[r] : EXP_FLOOR - 1;
     const bool live = r < R && er >= EXP_FLOOR;  // rows below the floor are all zero
+    const double *row = base + (live ? map_off(r, rs, mp.rl, mp.rs1) : 0);
     uint32_t packed[S][4];
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
       const int64_t k = (int64_t)kg * 8 + j;
       long long X = 0;
-      if (live && k < K) X = to_fixed(base[r * rs + k * ks], er, 7 * S);
+      if (live && k < K) X = to_fixed(row[map_off(k, ks, mp.kl, mp.ks1)], er, 7 * S);
       const long long Y = X + bias;
 #pragma unroll
       for (int s = 0; s < S; ++s) {
@@ -1018,11 +1033,11 @@ void run_emu(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
     if (rs == 1) {
       const int64_t kchunk = std::max<int64_t>(64, (K + 4095) / 4096);
       const dim3 grid((unsigned)((R + 127) / 128), (unsigned)((K + kchunk - 1) / kchunk));
-      exponent_rows_contig_kernel<<<grid, 128, 0, ctx.stream>>>(p, R, K, ks, kchunk, e);
+      exponent_rows_contig_kernel<<<grid, 128, 0, ctx.stream>>>(p, R, K, ks, kchunk, e, IdxMap{});
     } else {
       const int64_t kchunk = std::max<int64_t>(1024, (K + 4095) / 4096);
       const dim3 grid((unsigned)((R + 7) / 8), (unsigned)((K + kchunk - 1) / kchunk));
-      exponent_rows_warp_kernel<<<grid, 256, 0, ctx.stream>>>(p, R, K, rs, ks, kchunk, e);
+      exponent_rows_warp_kernel<<<grid, 256, 0, ctx.stream>>>(p, R, K, rs, ks, kchunk, e, IdxMap{});
     }
     GBCC_CHECK_LAUNCH(ctx);
   };
@@ -1035,10 +1050,10 @@ void run_emu(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
     return (unsigned)std::max<int64_t>(1, std::min(g, cap));
   };
   split_kernel<S, TM><<<grid_for((int64_t)mt * TM * kt * 4), 256, 0, ctx.stream>>>(
-      A, M, K, ars, aks, ea.as<int>(), mt, kt, asl.as<__nv_bfloat16>());
+      A, M, K, ars, aks, ea.as<int>(), mt, kt, asl.as<__nv_bfloat16>(), IdxMap{});
   GBCC_CHECK_LAUNCH(ctx);
   split_kernel<S, TN><<<grid_for((int64_t)nt * TN * kt * 4), 256, 0, ctx.stream>>>(
-      B, N, K, brs, bks, eb.as<int>(), nt, kt, bsl.as<__nv_bfloat16>());
+      B, N, K, brs, bks, eb.as<int>(), nt, kt, bsl.as<__nv_bfloat16>(), IdxMap{});
   GBCC_CHECK_LAUNCH(ctx);
   constexpr int STAGE_BYTES = S * (A_TILE + B_TILE);
   constexpr int STAGES = (SMEM_BUDGET / STAGE_BYTES) > 4 ? 4 : (SMEM_BUDGET / STAGE_BYTES);
@@ -1131,20 +1146,20 @@ void split_batch(Context &ctx, EmuPanels &P, const double *base, int64_t pstride
     if (P.rs == 1) {
       const int64_t kchunk = std::max<int64_t>(64, (K + 4095) / 4096);
       const dim3 grid((unsigned)((P.rows + 127) / 128), (unsigned)((K + kchunk - 1) / kchunk));
-      exponent_rows_contig_kernel<<<grid, 128, 0, ctx.stream>>>(b, P.rows, K, P.ks, kchunk, e);
+      exponent_rows_contig_kernel<<<grid, 128, 0, ctx.stream>>>(b, P.rows, K, P.ks, kchunk, e, P.map);
     } else {
       const int64_t kchunk = std::max<int64_t>(1024, (K + 4095) / 4096);
       const dim3 grid((unsigned)((P.rows + 7) / 8), (unsigned)((K + kchunk - 1) / kchunk));
-      exponent_rows_warp_kernel<<<grid, 256, 0, ctx.stream>>>(b, P.rows, K, P.rs, P.ks, kchunk, e);
+      exponent_rows_warp_kernel<<<grid, 256, 0, ctx.stream>>>(b, P.rows, K, P.rs, P.ks, kchunk, e, P.map);
     }
     GBCC_CHECK_LAUNCH(ctx);
     __nv_bfloat16 *out = P.panels.as<__nv_bfloat16>() + (int64_t)p * S * plane;
     if (P.role_a)
       split_kernel<S, TM><<<grid_for((int64_t)P.rt * TM * P.kt * 4), 256, 0, ctx.stream>>>(
-          b, P.rows, K, P.rs, P.ks, e, P.rt, P.kt, out);
+          b, P.rows, K, P.rs, P.ks, e, P.rt, P.kt, out, P.map);
     else
       split_kernel<S, TN><<<grid_for((int64_t)P.rt * TN * P.kt * 4), 256, 0, ctx.stream>>>(
-          b, P.rows, K, P.rs, P.ks, e, P.rt, P.kt, out);
+          b, P.rows, K, P.rs, P.ks, e, P.rt, P.kt, out, P.map);
     GBCC_CHECK_LAUNCH(ctx);
   }
 }
@@ -1471,8 +1486,11 @@ void emu_gemm_panels_to_panels(Context &ctx, const EmuPanels &A, int ia, const E
 }
 
 EmuPanels emu_split(Context &ctx, bool role_a, const double *base, int64_t R,
-                    int64_t K, int64_t rs, int64_t ks, int count, int64_t pstride) {
+                    int64_t K, int64_t rs, int64_t ks, int count, int64_t pstride,
+                    const IdxMap &map) {
   require(R > 0 && K > 0 && count > 0, "emu_split: empty operand");
+  require((map.rl == 0 || R < (1LL << 31)) && (map.kl == 0 || K < (1LL << 31)),
+          "emu_split: mapped dimension too large");
   EmuPanels P;
   P.role_a = role_a;
   P.S = ctx.emu_slices;
@@ -1480,6 +1498,7 @@ EmuPanels emu_split(Context &ctx, bool role_a, const double *base, int64_t R,
   P.K = K;
   P.rs = rs;
   P.ks = ks;
+  P.map = map;
   P.count = count;
   P.rt = (int)((R + (role_a ? TM : TN) - 1) / (role_a ? TM : TN));
   P.kt = (int)((K + KB - 1) / KB);
@@ -1645,11 +1664,11 @@ void run_emu_static(Context &ctx, bool ta, bool tb, int64_t M, int64_t N,
     if (rs == 1) {
       const int64_t kchunk = std::max<int64_t>(64, (K + 4095) / 4096);
       const dim3 grid((unsigned)((R + 127) / 128), (unsigned)((K + kchunk - 1) / kchunk));
-      exponent_rows_contig_kernel<<<grid, 128, 0, ctx.stream>>>(p, R, K, ks, kchunk, e);
+      exponent_rows_contig_kernel<<<grid, 128, 0, ctx.stream>>>(p, R, K, ks, kchunk, e, IdxMap{});
     } else {
       const int64_t kchunk = std::max<int64_t>(1024, (K + 4095) / 4096);
       const dim3 grid((unsigned)((R + 7) / 8), (unsigned)((K + kchunk - 1) / kchunk));
-      exponent_rows_warp_kernel<<<grid, 256, 0, ctx.stream>>>(p, R, K, rs, ks, kchunk, e);
+      exponent_rows_warp_kernel<<<grid, 256, 0, ctx.stream>>>(p, R, K, rs, ks, kchunk, e, IdxMap{});
     }
     GBCC_CHECK_LAUNCH(ctx);
   };
@@ -1662,10 +1681,10 @@ void run_emu_static(Context &ctx, bool ta, bool tb, int64_t M, int64_t N,
     return (unsigned)std::max<int64_t>(1, std::min(g, cap));
   };
   split_kernel<S, TM><<<grid_for((int64_t)mt * TM * kt * 4), 256, 0, ctx.stream>>>(
-      A, M, K, ars, aks, ea, mt, kt, asl);
+      A, M, K, ars, aks, ea, mt, kt, asl, IdxMap{});
   GBCC_CHECK_LAUNCH(ctx);
   split_kernel<S, TN><<<grid_for((int64_t)nt * TN * kt * 4), 256, 0, ctx.stream>>>(
-      B, N, K, brs, bks, eb, nt, kt, bsl);
+      B, N, K, brs, bks, eb, nt, kt, bsl, IdxMap{});
   GBCC_CHECK_LAUNCH(ctx);
   constexpr int STAGE_BYTES = S * (A_TILE + B_TILE);
   constexpr int STAGES = (SMEM_BUDGET / STAGE_BYTES) > 4 ? 4 : (SMEM_BUDGET / STAGE_BYTES);

@@ -315,14 +315,24 @@ void gemm_emu(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
 // Digit panels of a family of `count` same-shape operands (operand p at
 // base + p*pstride, element (r, k) at r*rs + k*ks), split once and reused by
 // many emulated GEMMs.  role_a: A operand (rows = M), else B (rows = N).
+// Second level of an operand's row and K offsets: with rl > 0, row r sits
+// at (r % rl) rs + (r / rl) rs1 (likewise K index k with kl, ks, ks1), so an
+// operand whose row (or K) indices form two runs of a tensor is read in
+// place; rl = kl = 0 is the plain r rs + k ks.
+struct IdxMap {
+  unsigned rl = 0, kl = 0;
+  int64_t rs1 = 0, ks1 = 0;
+};
 struct EmuPanels {
   DBuf panels, exps;
   bool role_a = true;
   int S = 6, count = 0, rt = 0, kt = 0;
   int64_t rows = 0, K = 0, rs = 0, ks = 0;
+  IdxMap map;
 };
 EmuPanels emu_split(Context &ctx, bool role_a, const double *base, int64_t R,
-                    int64_t K, int64_t rs, int64_t ks, int count, int64_t pstride);
+                    int64_t K, int64_t rs, int64_t ks, int count, int64_t pstride,
+                    const IdxMap &map = IdxMap{});
 // C[M,N] = alpha A_ia B_ib^T + beta C with M = A.rows, N = B.rows, K = A.K.
 // With Cdf given, C is a float-float array instead (hi and lo rounded from
 // the exact fixed-point totals; alpha = +-2^k, beta in {0, 1}).

@@ -138,8 +138,10 @@ void gemm(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K, doubl
 // operand p, element (r, k) at base + p pstride + r rs + k ks, copied as
 // panels[p][k][r]
 EmuPanels emu_split(Context &ctx, bool role_a, const double *base, int64_t R, int64_t K,
-                    int64_t rs, int64_t ks, int count, int64_t pstride) {
+                    int64_t rs, int64_t ks, int count, int64_t pstride, const IdxMap &map) {
   require(R > 0 && K > 0 && count > 0, "emu_split: empty operand");
+  require((map.rl == 0 || R < (1LL << 31)) && (map.kl == 0 || K < (1LL << 31)),
+          "emu_split: mapped dimension too large");
   EmuPanels P;
   P.role_a = role_a;
   P.S = ctx.emu_slices;
@@ -147,14 +149,20 @@ EmuPanels emu_split(Context &ctx, bool role_a, const double *base, int64_t R, in
   P.K = K;
   P.rs = rs;
   P.ks = ks;
+  P.map = map;
   P.count = count;
   P.panels.alloc(ctx, sizeof(double) * (size_t)count * R * K);
   double *out = P.panels.as<double>();
+  const IdxMap mp = map;
+  auto off = [](int64_t v, int64_t s0, unsigned l, int64_t s1) {
+    return l == 0 ? v * s0 : (v % l) * s0 + (v / l) * s1;
+  };
   launch(ctx, [=]() {
     for (int p = 0; p < count; ++p)
       for (int64_t k = 0; k < K; ++k)
         for (int64_t r = 0; r < R; ++r)
-          out[r + R * (k + K * p)] = base[p * pstride + r * rs + k * ks];
+          out[r + R * (k + K * p)] =
+              base[p * pstride + off(r, rs, mp.rl, mp.rs1) + off(k, ks, mp.kl, mp.ks1)];
   });
   return P;
 }

@@ -3,8 +3,9 @@
 (T) on the 12th-iteration amplitudes.
 
 The precision form (every large contraction emulated in FP64 on the bf16
-tensor cores: 6 digits per operand in the CCSD iterations, 7 in (T)) must
-reproduce the FP64 energies within 1 microhartree:
+tensor cores: 6 or 5 digits per operand in the CCSD iterations, one more in
+(T))
+must reproduce the FP64 energies within 1 microhartree:
 
 * every one of the 12 iteration energies against the CPU oracle's trajectory
   (committed in tests/golden/c2_trajectory.json);
@@ -39,15 +40,20 @@ def c2():
     return make_system(**C2), doc
 
 
-def test_precision_form_meets_one_microhartree_at_c2(ctx, c2):
+# (digits per operand in the CCSD iterations, digits in (T))
+@pytest.mark.parametrize("ccsd_digits,triples_digits", [(6, 7), (5, 6)])
+def test_precision_form_meets_one_microhartree_at_c2(ctx, c2, ccsd_digits, triples_digits):
     s, doc = c2
     ref = [r["energy"] for r in doc["oracle"]["energies"]]
-    ctx.set_emulation(6, 1e7)
+    ctx.set_emulation(ccsd_digits, 1e7)
     sol = gpu.Solver(ctx, s.eps_h, s.eps_p, s.gamma, precision="emu", **C2_SOLVE)
     try:
         es = [sol.step(1)[0] for _ in range(C2_SOLVE["max_iterations"])]
+        # (T) runs with one digit more than the context's setting
+        ctx.set_emulation(triples_digits - 1, 1e7)
         e_t, _ = sol.triples("emu")
     finally:
+        ctx.set_emulation(6, 1e7)
         sol.close()
     dE = [a - b for a, b in zip(es, ref)]
     assert len(dE) == 12

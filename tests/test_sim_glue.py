@@ -139,7 +139,8 @@ def test_host_code_under_address_and_undefined_behaviour_sanitizers(sim_env):
     env["LD_PRELOAD"] = asan + " " + cxx
     env["ASAN_OPTIONS"] = "detect_leaks=0:halt_on_error=1"
     env["UBSAN_OPTIONS"] = "halt_on_error=1:print_stacktrace=1"
-    args = NEW_PATHS + CALIBRATION[:-2] + RUNNER + [
+    # (the lockstep-batch files run on the plain simulation only, for time)
+    args = [f for f in NEW_PATHS if f != "tests/test_gpu_batch.py"] + CALIBRATION[:-2] + RUNNER + [
         "-k", CALIBRATION[-1] + " and not ueg_golden_through_the_complex"]
     r = subprocess.run([sys.executable, "-m", "pytest", "-m", "gpu", "-q", "-p",
                         "no:cacheprovider"] + args, cwd=ROOT, env=env,
