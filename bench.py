@@ -71,12 +71,15 @@ METRIC = "RCCSD iter/s mixed vs FP64 at |dE|<=1uHa; batched solves/s, p50/p99 la
 UNIT = "iter/s"
 REF_MAX_STEPS = 3
 FIXTURE = os.path.join(ROOT, "tests", "golden", "c2_trajectory.json")
-# DRAM bytes (read + write) per bf16 tensor flop of the emulated GEMM, from a
-# one-pass ncu capture of the same kernel on this workload
-# (dram__bytes_read.sum + dram__bytes_write.sum of 12 consecutive ladder
-# launches, V = G.G at 8192 x 8192 x 1024 and R = V.X at 1024 x 1024 x 65536,
-# 21 * 2 * 8192^2 * 1024 bf16 flop each: 17.458e9 + 5.292e9 bytes)
-EMU_GEMM_DRAM_PER_FLOP = (17.458e9 + 5.292e9) / (12 * 21 * 2.0 * 8192 ** 2 * 1024)
+# DRAM bytes (read + write) per bf16 tensor flop of the emulated GEMM, by
+# digits per operand, from one-pass ncu captures of the same kernel on this
+# workload (dram__bytes_read.sum + dram__bytes_write.sum of consecutive
+# ladder launches, V = G.G at 8192 x 8192 x 1024 and R = V.X at
+# 1024 x 1024 x 65536, S(S+1)/2 * 2 * 8192^2 * 1024 bf16 flop each):
+# 6 digits, 12 launches, 17.458e9 + 5.292e9 bytes; 5 digits, 24 launches,
+# 27.653e9 + 8.671e9 bytes
+EMU_GEMM_DRAM_PER_FLOP = {6: (17.458e9 + 5.292e9) / (12 * 21 * 2.0 * 8192 ** 2 * 1024),
+                          5: (27.653e9 + 8.671e9) / (24 * 15 * 2.0 * 8192 ** 2 * 1024)}
 
 
 def _peaks():
@@ -588,7 +591,8 @@ def main():
                 "avg_launch_ms": gs["ms"] / max(gs["launches"], 1),
                 "fp64_equiv_tflops": gs["fp64_flops"] / (gs["ms"] / 1e3) / 1e12,
                 "gemm_share_of_step": gs["ms"] / prof_ms if prof_ms else None,
-                "traffic": EMU_GEMM_DRAM_PER_FLOP * gs["tc_flops"] / gs["launches"],
+                "traffic": (EMU_GEMM_DRAM_PER_FLOP[args.slices] * gs["tc_flops"] / gs["launches"]
+                            if args.slices in EMU_GEMM_DRAM_PER_FLOP else None),
                 "traffic_unit": "bytes per launch",
                 "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of "
                                   "the ladder's launches on this workload, per bf16 flop, "
