@@ -153,6 +153,34 @@ void contract_cached(Context &ctx, double alpha, const Ten &A, const std::string
     }
     return P;
   };
+  // The output is written in place through an index map when its row and
+  // column indices each form at most two runs of C and one of the groups
+  // starts contiguous; that group becomes the kernel's rows (a coalesced
+  // write-out), M or, for the transposed product, N.
+  bool sw = swap;
+  OutMap cmap{};
+  if (permC) {
+    auto group_map = [&](const std::string &g, int64_t cnt, int64_t &l0, int64_t &s0,
+                         int64_t &s1) {
+      int64_t a0, a1;
+      unsigned l;
+      if (!group_offsets(sc, g, len, a0, l, a1)) return false;
+      l0 = l ? (int64_t)l : cnt;  // one run: the whole range at the first level
+      s0 = a0;
+      s1 = l ? a1 : 0;
+      return cnt < (1LL << 31);
+    };
+    int64_t ml0, ms0, ms1, nl0, ns0, ns1;
+    if (group_map(m, sM, ml0, ms0, ms1) && group_map(n, sN, nl0, ns0, ns1)) {
+      if (ms0 == 1) {
+        sw = false;
+        cmap = OutMap{ml0, ms0, ms1, nl0, ns0, ns1};
+      } else if (ns0 == 1) {
+        sw = true;
+        cmap = OutMap{nl0, ns0, ns1, ml0, ms0, ms1};
+      }
+    }
+  }
   // op(A)(m, k): from A's buffer in order m+k (ta = 0) or k+m (ta = 1)
   const std::string oa = permA ? m + k : sa;
   const bool tA = permA ? false : ta;
@@ -163,8 +191,14 @@ void contract_cached(Context &ctx, double alpha, const Ten &A, const std::string
   const int64_t ldb = tB ? sN : sK;
   // kernel roles: C = A_role (rows M) x B_role (rows N)^T, or the transposed
   // product when the plan computes C^T
-  auto PA = panels(A, sa, permA, oa, m, !swap, sM, tA ? lda : 1, tA ? 1 : lda);
-  auto PB = panels(B, sb, permB, ob, n, swap, sN, tB ? 1 : ldb, tB ? ldb : 1);
+  auto PA = panels(A, sa, permA, oa, m, !sw, sM, tA ? lda : 1, tA ? 1 : lda);
+  auto PB = panels(B, sb, permB, ob, n, sw, sN, tB ? 1 : ldb, tB ? ldb : 1);
+  if (cmap.ml0 > 0) {
+    const EmuPanels &rows = sw ? *PB : *PA, &cols = sw ? *PA : *PB;
+    if (nz > 1) emu_gemm_panels_batched(ctx, rows, cols, (int)nz, alpha, beta, C.p, 0, sM * sN, cmap);
+    else emu_gemm_panels_mapped(ctx, rows, 0, cols, 0, alpha, beta, C.p, cmap);
+    return;
+  }
   double *pc = C.p;
   double gbeta = beta;
   OTen tc;
@@ -284,15 +318,16 @@ void contract(Context &ctx, double alpha, const Ten &A, const char *ia,
       }
   const Plan &p = best;
   // emulated products with a constant operand (its panels cached) or an
-  // operand to reorder (read in place where its indices allow) take the
-  // panel route; its digits and products are those of the plain route
+  // operand or output to reorder (read or written in place where its indices
+  // allow) take the panel route; its digits and products are those of the
+  // plain route
   const bool emu_product = precision == GBCC_PREC_EMU && sK > 0 && sM > 1 && sN > 1 &&
                            2.0 * (double)sM * (double)sN * (double)sK >= ctx.emu_min_flops &&
                            nz < (1 << 20);
   const bool has_constant = ctx.use_panel_cache &&
                             (ctx.is_constant(A.p, sizeof(double) * A.size()) ||
                              ctx.is_constant(B.p, sizeof(double) * B.size()));
-  if (emu_product && (has_constant || p.permA || p.permB)) {
+  if (emu_product && (has_constant || p.permA || p.permB || p.permC)) {
     contract_cached(ctx, alpha, A, sa, B, sb, beta, C, sc, p.m, p.n, p.k, p.permA, p.ta,
                     p.permB, p.tb, p.permC, p.swap, len, z, nz);
     return;

@@ -693,9 +693,10 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) emu_gemm_kernel(EmuArgs a) {
           continue;
         }
         if (a.mapped) {
-          // permuted output layout, beta = 0 (host-checked): row offset once,
-          // column offsets stepped through the mixed radix of n; every lane
-          // runs the same loop (the shuffles stay converged)
+          // permuted output layout: row offset once, column offsets stepped
+          // through the mixed radix of n; every lane runs the same loop (the
+          // shuffles stay converged); with beta, each output is read where it
+          // is written
           const unsigned mu = mrow ? (unsigned)m : 0u;
           const unsigned mq = mu / a.ml0;
           double *rp = pr.C + (int64_t)(mu - mq * a.ml0) * a.ms0 + (int64_t)mq * a.ms1;
@@ -703,8 +704,12 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) emu_gemm_kernel(EmuArgs a) {
 #pragma unroll
           for (int j = 0; j < EPI_COLS; ++j) {
             const int eb = __shfl_sync(0xffffffffu, ebl, j);
-            if (mrow && n0 + j < a.N)
-              rp[(int64_t)nr * a.ns0 + (int64_t)nq * a.ns1] = scaled_total(tot[j], ea + eb, a.os);
+            if (mrow && n0 + j < a.N) {
+              double *q = rp + (int64_t)nr * a.ns0 + (int64_t)nq * a.ns1;
+              double v = scaled_total(tot[j], ea + eb, a.os);
+              if (accumulate) v = fma(a.beta, *q, v);
+              *q = v;
+            }
             if (++nr == a.nl0) {
               nr = 0;
               ++nq;
@@ -1078,8 +1083,8 @@ void run_emu(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
   args.frac = P.frac;
   args.W = P.ksplit > 1 ? wsp.as<long long>() : nullptr;
   if (map.ml0 > 0) {
-    require(beta == 0.0 && map.ml0 < (1LL << 31) && map.nl0 > 0 && map.nl0 < (1LL << 31),
-            "emulated GEMM: output map needs beta = 0 and 32-bit index lengths");
+    require(map.ml0 < (1LL << 31) && map.nl0 > 0 && map.nl0 < (1LL << 31),
+            "emulated GEMM: output map needs 32-bit index lengths");
     args.mapped = 1;
     args.ml0 = (unsigned)map.ml0;
     args.nl0 = (unsigned)map.nl0;
@@ -1166,7 +1171,8 @@ void split_batch(Context &ctx, EmuPanels &P, const double *base, int64_t pstride
 
 template <int S>
 void gemm_panels(Context &ctx, const EmuPanels &A, int ia, const EmuPanels &B, int ib,
-                 double alpha, double beta, double *C, df32 *Cdf, int64_t ldc) {
+                 double alpha, double beta, double *C, df32 *Cdf, int64_t ldc,
+                 const OutMap &map = OutMap{}) {
   const int64_t M = A.rows, N = B.rows, K = A.K;
   // float-float output is written directly (no K-split workspace)
   const EmuPlan P = emu_plan(S, M, N, K, ctx.sm_count, Cdf == nullptr, ctx.emu_max_ksplit);
@@ -1194,6 +1200,17 @@ void gemm_panels(Context &ctx, const EmuPanels &A, int ia, const EmuPanels &B, i
   args.ksplit = P.ksplit;
   args.frac = P.frac;
   args.W = P.ksplit > 1 ? wsp.as<long long>() : nullptr;
+  if (map.ml0 > 0) {
+    require(Cdf == nullptr && map.ml0 < (1LL << 31) && map.nl0 > 0 && map.nl0 < (1LL << 31),
+            "emulated GEMM: output map needs FP64 output and 32-bit index lengths");
+    args.mapped = 1;
+    args.ml0 = (unsigned)map.ml0;
+    args.nl0 = (unsigned)map.nl0;
+    args.ms0 = map.ms0;
+    args.ms1 = map.ms1;
+    args.ns0 = map.ns0;
+    args.ns1 = map.ns1;
+  }
   args.os = out_scale(alpha);
   args.inject_wait = ctx.take_fault(GBCC_FAULT_DEVICE_WAIT) ? 1 : 0;
   args.beta = beta;
@@ -1216,7 +1233,7 @@ void gemm_panels(Context &ctx, const EmuPanels &A, int ia, const EmuPanels &B, i
     const int64_t n = M * N;
     const int64_t g = std::min<int64_t>((n + 255) / 256, (int64_t)std::max(ctx.sm_count, 1) * 8);
     emu_splitk_reduce_kernel<<<(unsigned)std::max<int64_t>(g, 1), 256, 0, ctx.stream>>>(
-        wsp.as<long long>(), P.ksplit, M, N, args.ea, args.eb, P.frac, args.os, beta, C, ldc, OutMap{});
+        wsp.as<long long>(), P.ksplit, M, N, args.ea, args.eb, P.frac, args.os, beta, C, ldc, map);
     GBCC_CHECK_LAUNCH(ctx);
   }
   ctx.flops += 2.0 * (double)M * (double)N * (double)K;
@@ -1232,7 +1249,8 @@ void gemm_panels(Context &ctx, const EmuPanels &A, int ia, const EmuPanels &B, i
 template <int S>
 void gemm_panels_grouped(Context &ctx, const EmuPanels &A, const int *ia, const EmuPanels &B,
                          const int *ib, int nprob, double alpha, double beta,
-                         double *const *C, df32 *const *Cdf, int64_t ldc, int64_t sC = 0) {
+                         double *const *C, df32 *const *Cdf, int64_t ldc, int64_t sC = 0,
+                         const OutMap &map = OutMap{}) {
   const int64_t M = A.rows, N = B.rows, K = A.K;
   const EmuPlan P = emu_plan(S, M, N, K, ctx.sm_count, false);
   require((int64_t)P.mt * P.nt * nprob < (1LL << 31), "grouped GEMM: too many tiles");
@@ -1295,7 +1313,20 @@ void gemm_panels_grouped(Context &ctx, const EmuPanels &A, const int *ia, const 
     args.qsea = M;
     args.qseb = N;
     args.qsC = sC;
+    if (map.ml0 > 0) {
+      require(Cdf == nullptr && map.ml0 < (1LL << 31) && map.nl0 > 0 &&
+                  map.nl0 < (1LL << 31),
+              "batched GEMM: output map needs FP64 output and 32-bit index lengths");
+      args.mapped = 1;
+      args.ml0 = (unsigned)map.ml0;
+      args.nl0 = (unsigned)map.nl0;
+      args.ms0 = map.ms0;
+      args.ms1 = map.ms1;
+      args.ns0 = map.ns0;
+      args.ns1 = map.ns1;
+    }
   } else {
+    require(map.ml0 == 0, "grouped GEMM: no output map with a problem table");
     args.probs = table.as<EmuProb>();
   }
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -1316,24 +1347,29 @@ void gemm_panels_grouped(Context &ctx, const EmuPanels &A, const int *ia, const 
 }  // namespace
 
 void emu_gemm_panels_batched(Context &ctx, const EmuPanels &A, const EmuPanels &B, int nprob,
-                             double alpha, double beta, double *C, int64_t ldc, int64_t sC) {
+                             double alpha, double beta, double *C, int64_t ldc, int64_t sC,
+                             const OutMap &map) {
   require(nprob >= 1, "batched GEMM: no problems");
   require(A.role_a && !B.role_a && A.K == B.K && A.S == B.S, "batched GEMM: operand mismatch");
   // a few-tile product with long K keeps its K-split, problem by problem,
   // unless the batch alone fills the GPU with tiles
   const EmuPlan P1 = emu_plan(A.S, A.rows, B.rows, A.K, ctx.sm_count, true, ctx.emu_max_ksplit);
   if (P1.ksplit > 1 && (int64_t)P1.mt * P1.nt * nprob < ctx.sm_count) {
-    for (int q = 0; q < nprob; ++q)
-      emu_gemm_panels(ctx, A, q, B, q, alpha, beta, C + (int64_t)q * sC, ldc);
+    for (int q = 0; q < nprob; ++q) {
+      if (map.ml0 > 0)
+        emu_gemm_panels_mapped(ctx, A, q, B, q, alpha, beta, C + (int64_t)q * sC, map);
+      else
+        emu_gemm_panels(ctx, A, q, B, q, alpha, beta, C + (int64_t)q * sC, ldc);
+    }
     return;
   }
   double *const Cs[1] = {C};
   switch (A.S) {
-    case 4: gemm_panels_grouped<4>(ctx, A, nullptr, B, nullptr, nprob, alpha, beta, Cs, nullptr, ldc, sC); break;
-    case 5: gemm_panels_grouped<5>(ctx, A, nullptr, B, nullptr, nprob, alpha, beta, Cs, nullptr, ldc, sC); break;
-    case 6: gemm_panels_grouped<6>(ctx, A, nullptr, B, nullptr, nprob, alpha, beta, Cs, nullptr, ldc, sC); break;
-    case 7: gemm_panels_grouped<7>(ctx, A, nullptr, B, nullptr, nprob, alpha, beta, Cs, nullptr, ldc, sC); break;
-    case 8: gemm_panels_grouped<8>(ctx, A, nullptr, B, nullptr, nprob, alpha, beta, Cs, nullptr, ldc, sC); break;
+    case 4: gemm_panels_grouped<4>(ctx, A, nullptr, B, nullptr, nprob, alpha, beta, Cs, nullptr, ldc, sC, map); break;
+    case 5: gemm_panels_grouped<5>(ctx, A, nullptr, B, nullptr, nprob, alpha, beta, Cs, nullptr, ldc, sC, map); break;
+    case 6: gemm_panels_grouped<6>(ctx, A, nullptr, B, nullptr, nprob, alpha, beta, Cs, nullptr, ldc, sC, map); break;
+    case 7: gemm_panels_grouped<7>(ctx, A, nullptr, B, nullptr, nprob, alpha, beta, Cs, nullptr, ldc, sC, map); break;
+    case 8: gemm_panels_grouped<8>(ctx, A, nullptr, B, nullptr, nprob, alpha, beta, Cs, nullptr, ldc, sC, map); break;
     default: throw Error(GBCC_BAD_ARG, "emu_slices must be in [4, 8]");
   }
 }
@@ -1514,6 +1550,22 @@ EmuPanels emu_split(Context &ctx, bool role_a, const double *base, int64_t R,
     default: throw Error(GBCC_BAD_ARG, "emu_slices must be in [4, 8]");
   }
   return P;
+}
+
+void emu_gemm_panels_mapped(Context &ctx, const EmuPanels &A, int ia, const EmuPanels &B,
+                            int ib, double alpha, double beta, double *C, const OutMap &map) {
+  require(A.role_a && !B.role_a && A.K == B.K && A.S == B.S,
+          "emu_gemm_panels_mapped: operand mismatch");
+  require(ia >= 0 && ia < A.count && ib >= 0 && ib < B.count, "emu_gemm_panels_mapped: index");
+  require(map.ml0 > 0 && map.nl0 > 0, "emu_gemm_panels_mapped: empty map");
+  switch (A.S) {
+    case 4: gemm_panels<4>(ctx, A, ia, B, ib, alpha, beta, C, nullptr, 0, map); break;
+    case 5: gemm_panels<5>(ctx, A, ia, B, ib, alpha, beta, C, nullptr, 0, map); break;
+    case 6: gemm_panels<6>(ctx, A, ia, B, ib, alpha, beta, C, nullptr, 0, map); break;
+    case 7: gemm_panels<7>(ctx, A, ia, B, ib, alpha, beta, C, nullptr, 0, map); break;
+    case 8: gemm_panels<8>(ctx, A, ia, B, ib, alpha, beta, C, nullptr, 0, map); break;
+    default: throw Error(GBCC_BAD_ARG, "emu_slices must be in [4, 8]");
+  }
 }
 
 void emu_gemm_panels(Context &ctx, const EmuPanels &A, int ia, const EmuPanels &B,

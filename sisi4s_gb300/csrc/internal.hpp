@@ -345,10 +345,20 @@ void emu_gemm_panels(Context &ctx, const EmuPanels &A, int ia, const EmuPanels &
 void emu_gemm_panels_grouped(Context &ctx, const EmuPanels &A, const int *ia,
                              const EmuPanels &B, const int *ib, int nprob, double alpha,
                              double beta, double *const *C, df32 *const *Cdf, int64_t ldc);
+// Output index map of an emulated GEMM: C(m, n) at C + (m % ml0) ms0 +
+// (m / ml0) ms1 + (n % nl0) ns0 + (n / nl0) ns1 (ml0 = 0: no map).
+struct OutMap {
+  int64_t ml0, ms0, ms1, nl0, ns0, ns1;
+};
 // Strided batch: problem q multiplies operand q of A with operand q of B into
-// C + q sC, in one launch that can be captured into a graph.
+// C + q sC (through the output map, if one is given, instead of ldc), in one
+// launch that can be captured into a graph.
 void emu_gemm_panels_batched(Context &ctx, const EmuPanels &A, const EmuPanels &B, int nprob,
-                             double alpha, double beta, double *C, int64_t ldc, int64_t sC);
+                             double alpha, double beta, double *C, int64_t ldc, int64_t sC,
+                             const OutMap &map = OutMap{});
+// C = alpha A_ia B_ib^T + beta C written through an output index map.
+void emu_gemm_panels_mapped(Context &ctx, const EmuPanels &A, int ia, const EmuPanels &B,
+                            int ib, double alpha, double beta, double *C, const OutMap &map);
 // Panels of one operand, allocated but not filled (their digits and row
 // exponents are written by a producer such as emu_gemm_panels_to_panels).
 EmuPanels emu_panels_alloc(Context &ctx, bool role_a, int64_t R, int64_t K);
@@ -368,9 +378,6 @@ void ladder_row_exponents(Context &ctx, const void *amax, int64_t x0, int64_t nx
 // Output index map of an emulated GEMM with two indices on each side: C(m, n)
 // lives at C + (m % ml0) ms0 + (m / ml0) ms1 + (n % nl0) ns0 + (n / nl0) ns1,
 // so a product can write a permuted layout directly (beta must be 0).
-struct OutMap {
-  int64_t ml0, ms0, ms1, nl0, ns0, ns1;
-};
 void gemm_emu_mapped(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
                      double alpha, const double *A, int64_t lda, const double *B,
                      int64_t ldb, double *C, const OutMap &map);

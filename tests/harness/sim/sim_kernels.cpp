@@ -189,11 +189,39 @@ void emu_gemm_panels(Context &ctx, const EmuPanels &A, int ia, const EmuPanels &
   });
 }
 
+void emu_gemm_panels_mapped(Context &ctx, const EmuPanels &A, int ia, const EmuPanels &B,
+                            int ib, double alpha, double beta, double *C, const OutMap &map) {
+  require(A.role_a && !B.role_a && A.K == B.K && A.S == B.S,
+          "emu_gemm_panels_mapped: operand mismatch");
+  require(ia >= 0 && ia < A.count && ib >= 0 && ib < B.count, "emu_gemm_panels_mapped: index");
+  require(map.ml0 > 0 && map.nl0 > 0, "emu_gemm_panels_mapped: empty map");
+  const int64_t M = A.rows, N = B.rows, K = A.K;
+  const double *a = A.panels.as<double>() + M * K * ia;
+  const double *b = B.panels.as<double>() + N * K * ib;
+  const OutMap mp = map;
+  ctx.flops += 2.0 * (double)M * (double)N * (double)K;
+  launch(ctx, [=]() {
+    for (int64_t n = 0; n < N; ++n)
+      for (int64_t m = 0; m < M; ++m) {
+        double acc = 0.0;
+        for (int64_t k = 0; k < K; ++k) acc += a[m + M * k] * b[n + N * k];
+        double *q = C + (m % mp.ml0) * mp.ms0 + (m / mp.ml0) * mp.ms1 + (n % mp.nl0) * mp.ns0 +
+                    (n / mp.nl0) * mp.ns1;
+        double v = alpha * acc;
+        if (beta != 0.0) v += beta * *q;
+        *q = v;
+      }
+  });
+}
+
 void emu_gemm_panels_batched(Context &ctx, const EmuPanels &A, const EmuPanels &B, int nprob,
-                             double alpha, double beta, double *C, int64_t ldc, int64_t sC) {
+                             double alpha, double beta, double *C, int64_t ldc, int64_t sC,
+                             const OutMap &map) {
   require(nprob >= 1 && nprob <= A.count && nprob <= B.count, "batched GEMM: operand count");
-  for (int q = 0; q < nprob; ++q)
-    emu_gemm_panels(ctx, A, q, B, q, alpha, beta, C + (int64_t)q * sC, ldc, nullptr);
+  for (int q = 0; q < nprob; ++q) {
+    if (map.ml0 > 0) emu_gemm_panels_mapped(ctx, A, q, B, q, alpha, beta, C + (int64_t)q * sC, map);
+    else emu_gemm_panels(ctx, A, q, B, q, alpha, beta, C + (int64_t)q * sC, ldc, nullptr);
+  }
 }
 
 void gemm_emu_mapped(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
