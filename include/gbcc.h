@@ -446,9 +446,9 @@ gbcc_status gbcc_dgemm(gbcc_ctx *ctx, int transA, int transB, int64_t M,
  * GPU race; order them.  Each call waits for its GEMM to finish (it reads the
  * kernel's error word back) before it returns.  The first call on a device
  * looks up the array's device address and keeps it for the life of the
- * process; make it before any stream capture, and do not call this entry point
- * on a device after resetting it (cudaDeviceReset).  Device pointers, context
- * stream, digits from gbcc_ctx_set_emulation. */
+ * process; do not call this entry point on a device after resetting it
+ * (cudaDeviceReset).  Device pointers, context stream, digits from
+ * gbcc_ctx_set_emulation. */
 gbcc_status gbcc_dgemm_emu_noalloc(gbcc_ctx *ctx, int transA, int transB,
                                    int64_t M, int64_t N, int64_t K,
                                    double alpha, const double *A, int64_t lda,

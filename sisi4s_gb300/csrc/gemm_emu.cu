@@ -1656,9 +1656,8 @@ void gemm_emu(Context &ctx, bool ta, bool tb, int64_t M, int64_t N, int64_t K,
 // by the caller.  Each call reads the kernel's error word back, so it returns
 // only when its GEMM has finished.  The device address of the array is looked
 // up once per device, on the first call made with that device current, and
-// kept for the life of the process: that first call should come before any
-// stream capture, and a device reset (cudaDeviceReset) makes the kept address
-// stale, so the entry point is not for use after one.
+// kept for the life of the process: a device reset (cudaDeviceReset) makes
+// the kept address stale, so the entry point is not for use after one.
 namespace gbcc {
 namespace {
 
