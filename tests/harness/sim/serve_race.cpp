@@ -1,6 +1,7 @@
 // The serving layer's host threading under ThreadSanitizer, on the host
-// simulation of the device side: a server with 4 worker threads solves ten
-// small CCSD(T) requests submitted back to back while another thread polls
+// simulation of the device side: a server with 4 worker threads solves
+// sixteen small CCSD(T) requests submitted back to back (the last six of one
+// shape, which the slots take in lockstep batches) while another thread polls
 // its statistics.  Prints one line per result; ThreadSanitizer reports any
 // data race on stderr.
 #include <algorithm>
@@ -41,6 +42,7 @@ int main() {
   if (gbcc_server_create(&so, &srv) != GBCC_OK) { std::puts("create failed"); return 1; }
   std::vector<Sys> sys;
   for (int k = 0; k < 10; ++k) sys.push_back(make(2 + k % 2, 4 + k % 3, 8, 100 + k));
+  for (int k = 0; k < 6; ++k) sys.push_back(make(2, 5, 8, 200 + k));
   std::vector<int64_t> ids(sys.size());
   std::thread poller([&]() {
     for (int t = 0; t < 200; ++t) {

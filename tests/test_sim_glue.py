@@ -164,7 +164,7 @@ def test_serving_threads_have_no_data_race():
     assert "ThreadSanitizer" not in r.stderr, r.stderr[-4000:]
     assert r.returncode == 0, r.stdout + r.stderr[-2000:]
     lines = [l for l in r.stdout.splitlines() if l.startswith("id ")]
-    assert len(lines) == 10 and all(" st 0 status 0 " in l for l in lines), r.stdout
+    assert len(lines) == 16 and all(" st 0 status 0 " in l for l in lines), r.stdout
 
 
 @pytest.mark.parametrize("module,argv", [
