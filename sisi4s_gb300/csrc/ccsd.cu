@@ -271,6 +271,12 @@ void residual_program(Context &ctx, const ResidualArgs &ra, int it) {
 
   OTen X(ctx, shp({Nv, Nv, No, No}));                                   // :136-138
   outer_add(ctx, X.p(), T2.p, T1.p, 1.0, Nv, No, nz);
+  // T1, T2 and X stay unchanged until the residual is complete: operands
+  // taken from them in the same layout are split once
+  FrozenScope frozen(ctx);
+  frozen.add(T1.p, sizeof(double) * (size_t)T1.size());
+  frozen.add(T2.p, sizeof(double) * (size_t)T2.size());
+  frozen.add(X.p(), sizeof(double) * (size_t)X.t.size());
   OTen Kac(ctx, shp({Nv, Nv})), Kki(ctx, shp({No, No}));
   {
     OTen Lac(ctx, shp({Nv, Nv})), Lki(ctx, shp({No, No}));
@@ -369,6 +375,8 @@ void residual_program(Context &ctx, const ResidualArgs &ra, int it) {
     else C(1.0, Xklij, "klij", X, "abkl", 1.0, R2, "abij");          // :332
   }
   if (o.ppl) {                                                    // :374-452
+    // the ladder holds the largest temporaries: no kept panels meanwhile
+    ctx.drop_frozen_panels();
     OTen dG(ctx, shp({NG, Nv, Nv}));                               // :392-400
     copy(ctx, dG.p(), Gab.p, Gab.size());
     C(-1.0, Gai, "Gbk", T1, "ak", 1.0, dG, "Gab");

@@ -100,6 +100,26 @@ void contract_cached(Context &ctx, double alpha, const Ten &A, const std::string
       -> std::shared_ptr<EmuPanels> {
     const bool constant =
         ctx.use_panel_cache && ctx.is_constant(T.p, sizeof(double) * T.size());
+    // an operand unchanged for this residual evaluation: its panels of this
+    // layout and role, if already split, are reused
+    std::string fkey;
+    if (!constant && ctx.is_frozen(T.p, sizeof(double) * T.size())) {
+      char buf[64];
+      std::snprintf(buf, sizeof buf, "%p", (const void *)T.p);
+      fkey = std::string(buf) + "|" + st + "|" + rg + "|" + k + "|" + (role_a ? "A" : "B") +
+             "|" + std::to_string(rows) + "|" + std::to_string(nz) + "|" +
+             std::to_string(ctx.emu_slices);
+      auto it = ctx.frozen_panels.find(fkey);
+      if (it != ctx.frozen_panels.end()) return it->second;
+    }
+    auto keep = [&](std::shared_ptr<EmuPanels> P) {
+      const size_t b = P->panels.bytes() + P->exps.bytes();
+      if (!fkey.empty() && ctx.frozen_bytes + b <= Context::FROZEN_PANEL_LIMIT) {
+        ctx.frozen_panels[fkey] = P;
+        ctx.frozen_bytes += b;
+      }
+      return P;
+    };
     if (perm && !constant) {
       // an operand that changes from call to call is read in place when its
       // row indices (rg) and K indices each form at most two runs, one of
@@ -113,8 +133,8 @@ void contract_cached(Context &ctx, double alpha, const Ten &A, const std::string
         mp.rs1 = r1;
         mp.kl = kl;
         mp.ks1 = k1;
-        return std::make_shared<EmuPanels>(
-            emu_split(ctx, role_a, T.p, rows, sK, r0, k0, (int)nz, rows * sK, mp));
+        return keep(std::make_shared<EmuPanels>(
+            emu_split(ctx, role_a, T.p, rows, sK, r0, k0, (int)nz, rows * sK, mp)));
       }
     }
     std::string key;
@@ -151,7 +171,7 @@ void contract_cached(Context &ctx, double alpha, const Ten &A, const std::string
         ctx.panel_cache_bytes += bytes;
       }
     }
-    return P;
+    return keep(P);
   };
   // The output is written in place through an index map when its row and
   // column indices each form at most two runs of C and one of the groups

@@ -113,6 +113,23 @@ struct Context {
       return;
     }
   }
+  // Operands unchanged for the length of one residual evaluation (the
+  // amplitudes and X = T2 + T1 T1): their digit panels, split once per layout
+  // and role, are kept for the evaluation and dropped at its end (so inside a
+  // captured iteration they live and die within the graph).
+  std::vector<ConstRange> frozen_tensors;
+  std::map<std::string, std::shared_ptr<EmuPanels>> frozen_panels;
+  size_t frozen_bytes = 0;
+  static constexpr size_t FROZEN_PANEL_LIMIT = (size_t)3 << 30;
+  void drop_frozen_panels() {
+    frozen_panels.clear();
+    frozen_bytes = 0;
+  }
+  bool is_frozen(const double *p, size_t bytes) const {
+    for (const auto &r : frozen_tensors)
+      if (p >= r.p && (const char *)(p) + bytes <= (const char *)(r.p) + r.bytes) return true;
+    return false;
+  }
   // injected fault (GBCC_FAULT_*), consumed by the first matching event
   // (never while the stream is being captured into a graph: the fault would
   // be baked into every replay)
@@ -272,6 +289,22 @@ inline Ten ten(double *p, const std::vector<int64_t> &l) {
 }
 
 // Owned tensor = buffer + view.
+// Marks tensors as unchanged until the scope ends (Context::frozen_tensors)
+// and drops their kept panels then.
+struct FrozenScope {
+  Context &ctx;
+  explicit FrozenScope(Context &c) : ctx(c) {}
+  void add(const double *p, size_t bytes) {
+    if (p && bytes) ctx.frozen_tensors.push_back({p, bytes});
+  }
+  ~FrozenScope() {
+    ctx.drop_frozen_panels();
+    ctx.frozen_tensors.clear();
+  }
+  FrozenScope(const FrozenScope &) = delete;
+  FrozenScope &operator=(const FrozenScope &) = delete;
+};
+
 struct OTen {
   DBuf buf;
   Ten t;
