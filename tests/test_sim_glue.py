@@ -108,7 +108,7 @@ def test_calibration_set_passes_on_the_simulation(sim_env):
     assert " passed" in out and "failed" not in out
 
 
-def test_gpu_tests_not_yet_run_on_a_gpu_pass_on_the_simulation(sim_env):
+def test_newer_path_gpu_tests_pass_on_the_simulation(sim_env):
     out = _pytest(sim_env, NEW_PATHS)
     assert " passed" in out and "failed" not in out
 
