@@ -9,10 +9,11 @@
 // integrals, amplitudes and DIIS history resident from admission to result.
 // Every kernel is deterministic (fixed reduction orders, no floating-point
 // atomics), so a request gives bit-identical energies alone and in a mix.
-// A slot that admits a request also takes queued requests of the same shape,
-// options and (T) flag (up to max_batch in all) and solves them in lockstep,
-// one batched product per contraction for all of them; their energies then
-// agree with the solve alone up to the rounding of the batched products.
+// A slot that admits a request of a small shape (lockstep_pays) also takes
+// queued requests of the same shape, options and (T) flag (up to max_batch
+// in all) and solves them in lockstep, one batched product per contraction
+// for all of them; their energies then agree with the solve alone up to the
+// rounding of the batched products.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
